@@ -1,0 +1,56 @@
+/*
+ * irwls_gpu.h -- entry points of libirwls_gb300.so that the reference does not
+ * have: the error channel (the reference's training API has none), device
+ * residency for callers that train repeatedly on one dataset, dataset
+ * builders for the Python module, and kernel timing for benchmarks.
+ */
+#ifndef IRWLS_GB300_GPU_H
+#define IRWLS_GB300_GPU_H
+
+#include "IOStructures.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status of the last call that can fail on the device: 0 = success. Training
+ * and prediction functions return NULL after a failure and set this. */
+int irwls_last_error(void);
+const char *irwls_last_error_message(void);
+/* 1 when a CUDA device is usable. The library has no CPU path: without a
+ * device every training or prediction call fails with an error. */
+int irwls_gpu_available(void);
+
+/* A training set uploaded to the GPU once (rows l + 2 when the class-mean
+ * rows exist), for repeated training without host-to-device traffic. */
+typedef struct irwls_resident irwls_resident;
+irwls_resident *irwls_resident_upload(svm_dataset dataset, properties props, int with_mean_rows);
+void irwls_resident_free(irwls_resident *r);
+/* Budgeted training (SGMA or random centroids, then IRWLS) on a resident set;
+ * fills centroids[props.size] and weights[props.size]. 0 on success. */
+int irwls_resident_budgeted(irwls_resident *r, properties props, int *centroids, double *weights);
+/* Full IRWLS on a resident set; fills beta[l + 1]. 0 on success. */
+int irwls_resident_full(irwls_resident *r, properties props, double *beta);
+
+/* Python-module dataset builders (reference python-package/pythonmodule.c):
+ * dense row-major n x d doubles, every non-zero stored as feature j+1,
+ * sparse = 1 when any value is non-zero (:213-263). The _with_means variant
+ * appends the two class-mean rows as the module builds them (:277-355).
+ * Free with freeDataset. */
+svm_dataset irwls_dataset_from_dense(const double *X, const double *y, int n, int d);
+svm_dataset irwls_dataset_from_dense_with_means(const double *X, const double *y, int n, int d);
+
+/* Kernel timing with CUDA events on the library's stream. */
+void irwls_profile_enable(int on);
+void irwls_profile_reset(void);
+/* slot: 0 SGMA score GEMM, 1 Gram update, 2 kernel row sums, 3 Cholesky
+ * solve, 4 prediction. Total milliseconds and launches since the reset. */
+void irwls_profile_read(int slot, double *ms, long long *launches);
+/* Kernel launches issued by the library since it was loaded. */
+long long irwls_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,72 @@
+"""GB300-native implementation of LIBIRWLS's training and prediction hot path.
+
+The product is the C-ABI shared library ``libirwls_gb300.so`` built in this
+folder (``python -m libirwls_gb300.build``); it exports the reference's C API
+(include/*.h). ``load()`` opens it; there is no CPU fallback: if the library
+is missing the call raises, and without a CUDA device every training or
+prediction call returns NULL with an error message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libirwls_gb300.so")
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Opens libirwls_gb300.so (once) and declares its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            "libirwls_gb300.so is not built (run `python -m libirwls_gb300.build`); "
+            "this package has no CPU fallback")
+    lib = _abi.load_library(LIB_PATH)
+    PD = C.POINTER(C.c_double)
+    PI = C.POINTER(C.c_int)
+    extra = {
+        "irwls_last_error": (C.c_int, []),
+        "irwls_last_error_message": (C.c_char_p, []),
+        "irwls_gpu_available": (C.c_int, []),
+        "irwls_resident_upload": (C.c_void_p, [_abi.SvmDataset, _abi.Properties, C.c_int]),
+        "irwls_resident_free": (None, [C.c_void_p]),
+        "irwls_resident_budgeted": (C.c_int, [C.c_void_p, _abi.Properties, PI, PD]),
+        "irwls_resident_full": (C.c_int, [C.c_void_p, _abi.Properties, PD]),
+        "irwls_dataset_from_dense": (_abi.SvmDataset, [PD, PD, C.c_int, C.c_int]),
+        "irwls_dataset_from_dense_with_means": (_abi.SvmDataset, [PD, PD, C.c_int, C.c_int]),
+        "irwls_profile_enable": (None, [C.c_int]),
+        "irwls_profile_reset": (None, []),
+        "irwls_profile_read": (None, [C.c_int, PD, C.POINTER(C.c_longlong)]),
+        "irwls_kernel_launches": (C.c_longlong, []),
+        "storeModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
+        "readModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
+    }
+    for name, (res, args) in extra.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    lib = load()
+    code = lib.irwls_last_error()
+    return "" if code == 0 else "%d: %s" % (code, lib.irwls_last_error_message().decode())
+
+
+class DeviceError(RuntimeError):
+    pass
+
+
+def check(ptr, what: str):
+    """Raises DeviceError when a training/prediction entry point returned NULL."""
+    if not ptr:
+        raise DeviceError("%s failed: %s" % (what, last_error() or "unknown error"))
+    return ptr

@@ -1,0 +1,540 @@
+// dev_budget.cu -- device steps of budgeted IRWLS: SGMA centroid selection
+// (reference src/budgeted-train.c:114-309) and IRWLSpar (:324-505).
+//
+// SGMA keeps, per selected centroid s, the column KSC[:, s] = k(x_i, c_s)
+// (column-major, l rows) and the lower Cholesky factor L of K_CC + jitter
+// (row-major). One step scores 64 candidates:
+//   z_c = (L L^T)^-1 k_C(c)      one CTA per candidate, blocked substitution
+//   r_c = KSC z_c - k(c, .)      FP64 GEMM l x s x 64, the candidate kernel
+//                                row is evaluated in the epilogue (never stored)
+//   score_c = |r_c|^2 / eta_c    column norms reduced per CTA, then in a fixed
+//                                order; strict ">" argmax, first index wins.
+// IRWLSpar's Gram matrix K1 = KC + sum_i a_i a_i^T with a_i = sqrt(Da_i) KSC_i
+// over active rows is a split-K SYRK on the lower triangle; the right-hand
+// side K2 = sum_i a_i (sqrt(Da_i) y_i) is computed as the extra row m of the
+// same product, which is exactly where the Cholesky solver wants it.
+#include <math.h>
+
+#include <algorithm>
+
+#include "dev_common.cuh"
+
+namespace {
+
+constexpr int NCAND = 64;
+constexpr int CT = 1024;
+
+// --------------------------------------------------------------------------
+// SGMA
+// --------------------------------------------------------------------------
+
+// Per candidate: KNC row, forward then backward substitution with L, eta.
+// smem: v[s] (working vector), A row of the candidate (ld doubles).
+__global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__restrict__ cand,
+                                                        const int *__restrict__ cent, int s,
+                                                        const double *__restrict__ L, int ldL,
+                                                        double *__restrict__ W, double *__restrict__ Z,
+                                                        double *__restrict__ KN, int ldz,
+                                                        double *__restrict__ eta) {
+    extern __shared__ double sm[];
+    double *v = sm;
+    double *sA = sm + s;
+    const int c = blockIdx.x, tid = threadIdx.x;
+    const int gc = cand[c];
+    for (int t = tid; t < X.ld; t += blockDim.x) sA[t] = X.X[(size_t)gc * X.ld + t];
+    __syncthreads();
+    const double qa = X.q[gc];
+    for (int e = tid; e < s; e += blockDim.x) {
+        const double kv = kentry(X, sA, qa, cent[e]);
+        v[e] = kv;
+        KN[(size_t)c * ldz + e] = kv;
+    }
+    __syncthreads();
+    // forward: L w = v
+    const int nblk = (s + 31) / 32;
+    for (int b = 0; b < nblk; ++b) {
+        const int r0 = b * 32, r1 = min(s, r0 + 32);
+        if (tid < 32) {
+            const int r = r0 + tid;
+            double x = (r < r1) ? v[r] : 0.0;
+            for (int cc = r0; cc < r1; ++cc) {
+                double wc = 0.0;
+                if (r == cc) wc = x / L[(size_t)cc * ldL + cc];
+                wc = __shfl_sync(0xffffffffu, wc, cc - r0);
+                if (r == cc) x = wc;
+                else if (r > cc && r < r1) x = fma(-L[(size_t)r * ldL + cc], wc, x);
+            }
+            if (r < r1) v[r] = x;
+        }
+        __syncthreads();
+        for (int r = r1 + tid; r < s; r += blockDim.x) {
+            double x = v[r];
+            const double *row = L + (size_t)r * ldL;
+            for (int cc = r0; cc < r1; ++cc) x = fma(-row[cc], v[cc], x);
+            v[r] = x;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < s; e += blockDim.x) W[(size_t)c * ldz + e] = v[e];
+    __syncthreads();
+    // backward: L^T z = w
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int r0 = b * 32, r1 = min(s, r0 + 32);
+        if (tid < 32) {
+            const int r = r0 + tid;
+            double x = (r < r1) ? v[r] : 0.0;
+            for (int cc = r1 - 1; cc >= r0; --cc) {
+                double zc = 0.0;
+                if (r == cc) zc = x / L[(size_t)cc * ldL + cc];
+                zc = __shfl_sync(0xffffffffu, zc, cc - r0);
+                if (r == cc) x = zc;
+                else if (r < cc) x = fma(-L[(size_t)cc * ldL + r], zc, x);
+            }
+            if (r < r1) v[r] = x;
+        }
+        __syncthreads();
+        for (int r = tid; r < r0; r += blockDim.x) {
+            double x = v[r];
+            for (int cc = r0; cc < r1; ++cc) x = fma(-L[(size_t)cc * ldL + r], v[cc], x);
+            v[r] = x;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < s; e += blockDim.x) Z[(size_t)c * ldz + e] = v[e];
+    if (tid == 0) {
+        // eta = 1 - sum_e k_e z_e, left to right (src/budgeted-train.c:192-194)
+        double val = 1.0;
+        for (int e = 0; e < s; ++e) val = __dsub_rn(val, __dmul_rn(KN[(size_t)c * ldz + e], v[e]));
+        eta[c] = val;
+    }
+}
+
+// acc[i][c] = sum_k KSC[k*l + i] Z[c*ldz + k]; r = acc - k(cand_c, x_i);
+// part[blk][c] = sum over the CTA's 128 rows of r^2.
+constexpr int GM = 128, GK = 16;
+__global__ void __launch_bounds__(256) sgma_gemm_kernel(KView X, int l, const int *__restrict__ cand, int s,
+                                                        const double *__restrict__ KSC, const double *__restrict__ Z,
+                                                        int ldz, double *__restrict__ part) {
+    __shared__ double As[2][GK][GM];
+    __shared__ double Bs[2][GK][NCAND + 1];
+    __shared__ double red[16][NCAND + 1];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;  // tx: candidate group, ty: row group
+    const int i0 = blockIdx.x * GM;
+    double acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+
+    auto load = [&](int buf, int k0) {
+        // A: GK x GM, coalesced along rows of a KSC column
+        for (int t = tid; t < GK * GM; t += 256) {
+            const int kk = t / GM, r = t % GM;
+            const int k = k0 + kk, i = i0 + r;
+            As[buf][kk][r] = (k < s && i < l) ? KSC[(size_t)k * l + i] : 0.0;
+        }
+        for (int t = tid; t < GK * NCAND; t += 256) {
+            const int c = t / GK, kk = t % GK;
+            const int k = k0 + kk;
+            Bs[buf][kk][c] = (k < s) ? Z[(size_t)c * ldz + k] : 0.0;
+        }
+    };
+    const int nk = (s + GK - 1) / GK;
+    if (nk > 0) load(0, 0);
+    __syncthreads();
+    for (int kt = 0; kt < nk; ++kt) {
+        const int buf = kt & 1;
+        if (kt + 1 < nk) load(buf ^ 1, (kt + 1) * GK);
+#pragma unroll
+        for (int kk = 0; kk < GK; ++kk) {
+            double av[8], bv[4];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) av[a] = As[buf][kk][ty + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[buf][kk][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+        }
+        __syncthreads();
+    }
+    // epilogue: subtract the candidate kernel value, square, reduce
+    double ps[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int c = tx + 16 * b;
+        const int gc = cand[c];
+        const double *arow = X.X + (size_t)gc * X.ld;
+        const double qa = X.q[gc];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const int i = i0 + ty + 16 * a;
+            if (i < l) {
+                const double kv = kentry(X, arow, qa, i);
+                const double r = acc[a][b] - kv;
+                ps[b] = fma(r, r, ps[b]);
+            }
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) red[ty][tx + 16 * b] = ps[b];
+    __syncthreads();
+    if (tid < NCAND) {
+        double t = 0.0;
+        for (int g = 0; g < 16; ++g) t += red[g][tid];
+        part[(size_t)blockIdx.x * NCAND + tid] = t;
+    }
+}
+
+// Fixed-order reduction of the partial norms, scores, argmax
+// (src/budgeted-train.c:197-216).
+__global__ void __launch_bounds__(NCAND) sgma_select_kernel(const double *__restrict__ part, int nblk,
+                                                            const double *__restrict__ eta,
+                                                            const int *__restrict__ cand, int s, int *cent,
+                                                            int *best, double *bestval) {
+    __shared__ double sc[NCAND];
+    const int c = threadIdx.x;
+    double v = 0.0;
+    for (int b = 0; b < nblk; ++b) v += part[(size_t)b * NCAND + c];
+    const double et = eta[c];
+    sc[c] = (et > 0.0) ? __dmul_rn(__ddiv_rn(1.0, et), v) : 0.0;
+    __syncthreads();
+    if (c == 0) {
+        double val = sc[0];
+        int bb = 0;
+        for (int i = 1; i < NCAND; ++i)
+            if (sc[i] > val) {
+                val = sc[i];
+                bb = i;
+            }
+        cent[s] = cand[bb];
+        best[0] = bb;
+        bestval[s] = val;
+    }
+}
+
+// Appends centroid s: KSC column (separate launch), and row s of L:
+// L[s, :s] = L^-1 k_C(c_s) (the forward result of the winning candidate),
+// L[s, s] = sqrt(k(c_s, c_s) + jitter - |L[s, :s]|^2)  (src/budgeted-train.c:247-279).
+__global__ void sgma_factor_kernel(KView X, int s, const int *__restrict__ cent, const int *__restrict__ best,
+                                   const double *__restrict__ W, int ldz, double *__restrict__ L, int ldL) {
+    extern __shared__ double sA[];
+    const int gc = cent[s];
+    for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sA[t] = X.X[(size_t)gc * X.ld + t];
+    __syncthreads();
+    if (s >= 2) {
+        const int bb = best[0];
+        for (int t = threadIdx.x; t < s; t += blockDim.x) L[(size_t)s * ldL + t] = W[(size_t)bb * ldz + t];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double kcc = kentry(X, sA, X.q[gc], gc);
+        if (s == 0) {
+            L[0] = sqrt(__dadd_rn(kcc, 0.000001));
+        } else {
+            if (s == 1) {
+                // L2 = (1 / L00) k(c0, c1) as the reference's inverse-factor product
+                const double k01 = kentry(X, sA, X.q[gc], cent[0]);
+                L[(size_t)1 * ldL + 0] = __dmul_rn(__ddiv_rn(1.0, L[0]), k01);
+            }
+            double l3 = __dadd_rn(kcc, 0.00001);
+            for (int t = 0; t < s; ++t) {
+                const double v = L[(size_t)s * ldL + t];
+                l3 = __dsub_rn(l3, __dmul_rn(v, v));
+            }
+            L[(size_t)s * ldL + s] = sqrt(l3);
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// IRWLSpar
+// --------------------------------------------------------------------------
+
+__global__ void add_diag_kernel(double *KC, int m, double v) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        KC[(size_t)i * m + i] = __dadd_rn(KC[(size_t)i * m + i], v);
+}
+
+// Partial Gram tiles. A' row p = [sd_p * KSC[act_p, :], day_p] (m + 1 values).
+// Tile (bi, bj), bi >= bj, of the lower triangle of A'^T A' restricted to
+// columns < m; chunk z of the active rows. part layout: [P][m+1 rows][m cols]
+// row-major by output row.
+constexpr int TT = 64, TK = 16;
+__global__ void __launch_bounds__(256) gram_kernel(const double *__restrict__ KSC, int m, const int *__restrict__ act,
+                                                   int nact, const double *__restrict__ sd,
+                                                   const double *__restrict__ day, int chunk,
+                                                   double *__restrict__ part) {
+    const int bj = blockIdx.x, bi = blockIdx.y, z = blockIdx.z;
+    if (bi < bj) return;
+    const int r0 = bi * TT, c0 = bj * TT;  // output rows (0..m), output cols (0..m-1)
+    const int p0 = z * chunk, p1 = min(nact, p0 + chunk);
+    __shared__ double Ai[TK][TT + 1];
+    __shared__ double Aj[TK][TT + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int p = p0; p < p1; p += TK) {
+        for (int t = tid; t < TK * TT; t += 256) {
+            const int kk = t / TT, cc = t % TT;
+            const int pp = p + kk;
+            double vi = 0.0, vj = 0.0;
+            if (pp < p1) {
+                const int g = act[pp];
+                const double s = sd[pp];
+                const double *row = KSC + (size_t)g * m;
+                const int ci = r0 + cc, cj = c0 + cc;
+                vi = (ci < m) ? __dmul_rn(s, row[ci]) : ((ci == m) ? day[pp] : 0.0);
+                vj = (cj < m) ? __dmul_rn(s, row[cj]) : 0.0;
+            }
+            Ai[kk][cc] = vi;
+            Aj[kk][cc] = vj;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TK; ++kk) {
+            double ai[4], aj[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) ai[a] = Ai[kk][ty + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) aj[b] = Aj[kk][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = fma(ai[a], aj[b], acc[a][b]);
+        }
+        __syncthreads();
+    }
+    double *out = part + (size_t)z * (m + 1) * m;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int r = r0 + ty + 16 * a;
+        if (r > m) continue;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int c = c0 + tx + 16 * b;
+            if (c < m && c <= r) out[(size_t)r * m + c] = acc[a][b];
+        }
+    }
+}
+
+// K1 (column-major, leading dimension ld >= m + 1, lower part) = KC + sum_z
+// part_z; row m = K2 = sum_z part_z[m][:].
+__global__ void gram_reduce_kernel(const double *__restrict__ part, int P, int m, const double *__restrict__ KC,
+                                   double *__restrict__ K1, int ld) {
+    const long long total = (long long)(m + 1) * m;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(t / m), c = (int)(t % m);
+        if (c > r) continue;
+        double v = 0.0;
+        for (int z = 0; z < P; ++z) v += part[(size_t)z * total + t];
+        if (r < m) v = __dadd_rn(v, KC[(size_t)r * m + c]);
+        K1[(size_t)c * ld + r] = v;
+    }
+}
+
+// e = y - KSC beta, then Da (src/budgeted-train.c:431-457). One warp per row.
+__global__ void residual_kernel(const double *__restrict__ KSC, int l, int m, const double *__restrict__ beta,
+                                const double *__restrict__ y, double C, double M, double *__restrict__ e,
+                                double *__restrict__ Da) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = warp; i < l; i += nw) {
+        const double *row = KSC + (size_t)i * m;
+        double acc = 0.0;
+        for (int j = lane; j < m; j += 32) acc = fma(row[j], beta[j], acc);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double yi = y[i];
+            const double ei = yi - acc;
+            e[i] = ei;
+            double d = (__dmul_rn(ei, yi) < 0.0) ? 0.0 : __ddiv_rn(__dmul_rn(1.0, C), __dmul_rn(yi, ei));
+            if (d > M) d = M;
+            Da[i] = d;
+        }
+    }
+}
+
+__device__ int block_exclusive_scan(int *s, int v) {
+    const int t = threadIdx.x;
+    s[t] = v;
+    __syncthreads();
+    for (int o = 1; o < CT; o <<= 1) {
+        int x = (t >= o) ? s[t - o] : 0;
+        __syncthreads();
+        s[t] += x;
+        __syncthreads();
+    }
+    const int incl = s[t];
+    const int total = s[CT - 1];
+    __syncthreads();
+    s[t] = incl - v;
+    __syncthreads();
+    return total;
+}
+
+// Active rows (Da != 0) in ascending order with sqrt(Da) and sqrt(Da) y
+// (src/budgeted-train.c:459-474).
+__global__ void __launch_bounds__(CT) weights_kernel(const double *__restrict__ Da, const double *__restrict__ y,
+                                                     int l, int *act, double *sd, double *day, int *nact) {
+    __shared__ int s_scan[CT];
+    const int ch = (l + CT - 1) / CT;
+    const int b = threadIdx.x * ch, e = min(l, b + ch);
+    int c = 0;
+    for (int i = b; i < e; ++i) c += (Da[i] != 0.0);
+    const int total = block_exclusive_scan(s_scan, c);
+    int off = s_scan[threadIdx.x];
+    for (int i = b; i < e; ++i) {
+        const double d = Da[i];
+        if (d != 0.0) {
+            act[off] = i;
+            const double r = sqrt(d);
+            sd[off] = r;
+            day[off] = __dmul_rn(r, y[i]);
+            ++off;
+        }
+    }
+    if (threadIdx.x == 0) nact[0] = total;
+}
+
+// First IRWLSpar pass: every row, unscaled, with Day = y M (src/budgeted-train.c:348-352).
+__global__ void first_weights_kernel(const double *__restrict__ y, int l, double M, int *act, double *sd,
+                                     double *day) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l; i += gridDim.x * blockDim.x) {
+        act[i] = i;
+        sd[i] = 1.0;
+        day[i] = __dmul_rn(y[i], M);
+    }
+}
+
+__global__ void delta_kernel(const double *__restrict__ bnew, double *beta, int m, double *out2) {
+    if (threadIdx.x || blockIdx.x) return;
+    double dW = 0.0, nW = 0.0;
+    for (int i = 0; i < m; ++i) {
+        const double d = __dsub_rn(bnew[i], beta[i]);
+        dW = __dadd_rn(dW, __dmul_rn(d, d));
+        nW = __dadd_rn(nW, __dmul_rn(bnew[i], bnew[i]));
+        beta[i] = bnew[i];
+    }
+    out2[0] = dW;
+    out2[1] = nW;
+}
+
+}  // namespace
+
+extern "C" int irwls_dev_kernel_block_t(const irwls_dev_set *A, const int *d_ia, int nA, const irwls_dev_set *B,
+                                        const int *d_ib, int nB, double *d_out, long long ld_out, int trans);
+
+extern "C" int irwls_sgma_first(const irwls_dev_set *X, int l, int *d_cent, double *d_L, int ldL, double *d_KSC) {
+    // centroid 0 = row l (the positive class mean), set by the caller in d_cent
+    if (irwls_dev_kernel_block_t(X, d_cent, 1, X, nullptr, l, d_KSC, l, 0)) return -2;
+    const size_t smem = (size_t)X->ld * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), 0, d_cent, nullptr, nullptr, 0, d_L, ldL);
+    IRWLS_LAUNCH_CHECK("sgma_factor");
+    return 0;
+}
+
+extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand, int ncand, const int *d_cent, int s,
+                                const double *d_L, int ldL, const double *d_KSC, double *d_W, double *d_Z,
+                                double *d_KN, int ldz, double *d_eta, double *d_part) {
+    if (ncand != NCAND) {
+        irwls_set_error(-7, "SGMA scores exactly %d candidates per step", NCAND);
+        return -7;
+    }
+    const size_t smem = ((size_t)s + X->ld) * sizeof(double);
+    if (smem > 200 * 1024) {
+        irwls_set_error(-7, "SGMA budget %d with feature width %d exceeds the substitution tile", s, X->width);
+        return -7;
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sgma_cand_kernel<<<NCAND, 256, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_L, ldL, d_W, d_Z, d_KN, ldz,
+                                                          d_eta);
+    IRWLS_LAUNCH_CHECK("sgma_cand");
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
+    sgma_gemm_kernel<<<ceil_div(l, GM), 256, 0, irwls_stream()>>>(kview(X), l, d_cand, s, d_KSC, d_Z, ldz, d_part);
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_GEMM);
+    IRWLS_LAUNCH_CHECK("sgma_gemm");
+    return 0;
+}
+
+extern "C" int irwls_sgma_partials(int l) { return ceil_div(l, GM); }
+
+extern "C" int irwls_sgma_select(const double *d_part, int l, const double *d_eta, const int *d_cand, int s,
+                                 int *d_cent, int *d_best, double *d_bestval) {
+    sgma_select_kernel<<<1, NCAND, 0, irwls_stream()>>>(d_part, ceil_div(l, GM), d_eta, d_cand, s, d_cent, d_best,
+                                                        d_bestval);
+    IRWLS_LAUNCH_CHECK("sgma_select");
+    return 0;
+}
+
+extern "C" int irwls_sgma_extend(const irwls_dev_set *X, int l, int s, const int *d_cent, const int *d_best,
+                                 const double *d_W, int ldz, double *d_L, int ldL, double *d_KSC) {
+    if (irwls_dev_kernel_block_t(X, d_cent + s, 1, X, nullptr, l, d_KSC + (size_t)s * l, l, 0)) return -2;
+    const size_t smem = (size_t)X->ld * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL);
+    IRWLS_LAUNCH_CHECK("sgma_factor");
+    return 0;
+}
+
+extern "C" int irwls_par_build(const irwls_dev_set *X, int l, const int *d_idx, int m, double *d_KC, double *d_KSC) {
+    if (irwls_dev_kernel_block_t(X, d_idx, m, X, d_idx, m, d_KC, m, 0)) return -2;
+    add_diag_kernel<<<ceil_div(m, 256), 256, 0, irwls_stream()>>>(d_KC, m, 0.00001);
+    IRWLS_LAUNCH_CHECK("add_diag");
+    // KSC row-major l x m: out[row * m + centroid]
+    return irwls_dev_kernel_block_t(X, d_idx, m, X, nullptr, l, d_KSC, m, 1);
+}
+
+extern "C" int irwls_par_first(const double *d_y, int l, double M, int *d_act, double *d_sd, double *d_day) {
+    first_weights_kernel<<<ceil_div(l, 256), 256, 0, irwls_stream()>>>(d_y, l, M, d_act, d_sd, d_day);
+    IRWLS_LAUNCH_CHECK("first_weights");
+    return 0;
+}
+
+extern "C" size_t irwls_par_gram_part_bytes(int m, int P) { return (size_t)P * (m + 1) * m * sizeof(double); }
+
+extern "C" int irwls_par_gram(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
+                              const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P) {
+    const int T = ceil_div(m + 1, TT);
+    const int Tc = ceil_div(m, TT);
+    const int chunk = nact > 0 ? ceil_div(nact, P) : 1;
+    dim3 grid(Tc, T, P);
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM);
+    gram_kernel<<<grid, 256, 0, irwls_stream()>>>(d_KSC, m, d_act, nact, d_sd, d_day, chunk, d_part);
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_GRAM);
+    IRWLS_LAUNCH_CHECK("gram");
+    const long long total = (long long)(m + 1) * m;
+    gram_reduce_kernel<<<(int)std::min<long long>(ceil_div(total, 256), 65535), 256, 0, irwls_stream()>>>(
+        d_part, P, m, d_KC, d_K1, ldK1);
+    IRWLS_LAUNCH_CHECK("gram_reduce");
+    return 0;
+}
+
+extern "C" int irwls_par_residual(const double *d_KSC, int l, int m, const double *d_beta, const double *d_y, double C,
+                                  double M, double *d_e, double *d_Da) {
+    const int blocks = std::min(ceil_div(l, 8), 8 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
+    residual_kernel<<<blocks, 256, 0, irwls_stream()>>>(d_KSC, l, m, d_beta, d_y, C, M, d_e, d_Da);
+    IRWLS_LAUNCH_CHECK("residual");
+    return 0;
+}
+
+extern "C" int irwls_par_weights(const double *d_Da, const double *d_y, int l, int *d_act, double *d_sd,
+                                 double *d_day, int *d_nact) {
+    weights_kernel<<<1, CT, 0, irwls_stream()>>>(d_Da, d_y, l, d_act, d_sd, d_day, d_nact);
+    IRWLS_LAUNCH_CHECK("weights");
+    return 0;
+}
+
+extern "C" int irwls_par_delta(const double *d_bnew, double *d_beta, int m, double *d_out2) {
+    delta_kernel<<<1, 32, 0, irwls_stream()>>>(d_bnew, d_beta, m, d_out2);
+    IRWLS_LAUNCH_CHECK("delta");
+    return 0;
+}

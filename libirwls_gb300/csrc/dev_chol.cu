@@ -1,0 +1,270 @@
+// dev_chol.cu -- blocked right-looking Cholesky factorization and solve in
+// FP64 (reference src/ParallelAlgorithms.c:361-447, which ends in LAPACK
+// dpotrf/dpotrs).
+//
+// M is column-major with leading dimension ld >= n + 1. The right-hand side b
+// is carried as row n: the factorization then produces, in that row, the
+// forward-substitution result z = L^-1 b, and one backward sweep gives x.
+//
+// Failed pivots keep LAPACK's behaviour: a pivot that is not positive is
+// stored without its square root and reported (first failure, 1-based) in
+// device flag 0. In full IRWLS the system matrix is bordered by the labels
+// with a zero corner, so its last pivot fails by construction; the reference
+// ignores that failure and solves with the stored negative Schur complement,
+// and so does this code.
+//
+// Per panel of 32 columns: one launch factors the diagonal block (redundantly
+// in every CTA, in shared memory) and solves the rows below it against it;
+// one launch applies the rank-32 update to the lower trailing matrix.
+#include <math.h>
+
+#include "dev_common.cuh"
+
+namespace {
+
+constexpr int NB = 32;
+
+// Every CTA reads the (updated) diagonal block from M and factors it; CTA 0
+// stores the factor in Dout, not in M, because other CTAs of the same launch
+// may still be reading the block from M. The stored blocks are copied into M
+// after the last panel (chol_store_diag_kernel).
+__global__ void __launch_bounds__(128) chol_panel_kernel(double *__restrict__ M, int n, int ld, int k0, int nb,
+                                                         int nrows, int *__restrict__ flags,
+                                                         double *__restrict__ Dout) {
+    __shared__ double D[NB][NB + 1];
+    __shared__ int failed_at;
+    const int tid = threadIdx.x;
+    for (int t = tid; t < NB * NB; t += blockDim.x) {
+        const int r = t / NB, c = t % NB;
+        D[r][c] = (r < nb && c <= r) ? M[(size_t)(k0 + c) * ld + k0 + r] : (r == c ? 1.0 : 0.0);
+    }
+    if (tid == 0) failed_at = -1;
+    __syncthreads();
+    for (int c = 0; c < nb; ++c) {
+        if (tid == 0) {
+            const double s = D[c][c];
+            if (s > 0.0) {
+                D[c][c] = sqrt(s);
+            } else if (failed_at < 0) {
+                failed_at = c;  // stored unsquare-rooted, as dpotrf leaves it
+            }
+        }
+        __syncthreads();
+        const double piv = D[c][c];
+        for (int r = c + 1 + tid; r < nb; r += blockDim.x) D[r][c] = D[r][c] / piv;
+        __syncthreads();
+        const int m = nb - c - 1;
+        for (int t = tid; t < m * m; t += blockDim.x) {
+            const int r = c + 1 + t / m, j = c + 1 + t % m;
+            if (j <= r) D[r][j] = fma(-D[r][c], D[j][c], D[r][j]);
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0) {
+        for (int t = tid; t < NB * NB; t += blockDim.x) Dout[t] = D[t / NB][t % NB];
+        if (tid == 0 && failed_at >= 0) atomicCAS(flags, 0, k0 + failed_at + 1);
+    }
+    // rows below the block (and the right-hand-side row n when present)
+    const int i = k0 + nb + blockIdx.x * blockDim.x + tid;
+    if (i >= nrows) return;
+    double x[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) x[c] = (c < nb) ? M[(size_t)(k0 + c) * ld + i] : 0.0;
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        if (c < nb) {
+            double v = x[c];
+#pragma unroll
+            for (int t = 0; t < c; ++t) v = fma(-x[t], D[c][t], v);
+            x[c] = v / D[c][c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NB; ++c)
+        if (c < nb) M[(size_t)(k0 + c) * ld + i] = x[c];
+}
+
+__global__ void chol_store_diag_kernel(double *__restrict__ M, int n, int ld, const double *__restrict__ Dall) {
+    const int k0 = blockIdx.x * NB;
+    const int nb = min(NB, n - k0);
+    const double *D = Dall + (size_t)blockIdx.x * NB * NB;
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+        const int r = t / nb, c = t % nb;
+        if (c <= r) M[(size_t)(k0 + c) * ld + k0 + r] = D[r * NB + c];
+    }
+}
+
+__global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(t / n), r = (int)(t % n);
+        if (r < c) M[(size_t)c * ld + r] = 0.0;
+    }
+}
+
+// Trailing update of the lower part: M[i][j] -= sum_t L[i][t] L[j][t] over the
+// panel columns t, for k1 <= j <= i < nrows, j < n. One 32x32 tile per CTA.
+__global__ void __launch_bounds__(256) chol_update_kernel(double *__restrict__ M, int n, int ld, int k0, int nb,
+                                                          int nrows) {
+    const int bj = blockIdx.x, bi = blockIdx.y;
+    if (bi < bj) return;
+    const int k1 = k0 + nb;
+    const int r0 = k1 + bi * 32, c0 = k1 + bj * 32;
+    __shared__ double Li[32][NB + 1];
+    __shared__ double Lj[32][NB + 1];
+    const int tid = threadIdx.x;
+    for (int t = tid; t < 32 * NB; t += 256) {
+        const int r = t % 32, k = t / 32;
+        const int gi = r0 + r, gj = c0 + r;
+        Li[r][k] = (k < nb && gi < nrows) ? M[(size_t)(k0 + k) * ld + gi] : 0.0;
+        Lj[r][k] = (k < nb && gj < n) ? M[(size_t)(k0 + k) * ld + gj] : 0.0;
+    }
+    __syncthreads();
+    const int r = tid % 32;
+    for (int cc = tid / 32; cc < 32; cc += 8) {
+        const int gi = r0 + r, gj = c0 + cc;
+        if (gi >= nrows || gj >= n || gj > gi) continue;
+        double acc = 0.0;
+#pragma unroll 8
+        for (int k = 0; k < NB; ++k) acc = fma(Li[r][k], Lj[cc][k], acc);
+        double *p = M + (size_t)gj * ld + gi;
+        *p = *p - acc;
+    }
+}
+
+// Backward sweep L^T x = z with z in row n of M; one CTA, z kept in shared
+// memory, 32-row blocks from the bottom: warp 0 solves the diagonal block,
+// then all threads update the rows above it.
+__global__ void __launch_bounds__(256) chol_backsolve_kernel(const double *__restrict__ M, int n, int ld,
+                                                             double *__restrict__ x) {
+    extern __shared__ double z[];
+    const int tid = threadIdx.x;
+    for (int c = tid; c < n; c += blockDim.x) z[c] = M[(size_t)c * ld + n];
+    __syncthreads();
+    const int nblk = (n + 31) / 32;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int r0 = b * 32, r1 = min(n, r0 + 32);
+        if (tid < 32) {
+            const int r = r0 + tid;
+            double v = (r < r1) ? z[r] : 0.0;
+            for (int c = r1 - 1; c >= r0; --c) {
+                double xc = 0.0;
+                if (r == c) xc = v / M[(size_t)c * ld + c];
+                xc = __shfl_sync(0xffffffffu, xc, c - r0);
+                if (r == c) v = xc;
+                else if (r < c) v = fma(-M[(size_t)r * ld + c], xc, v);
+            }
+            if (r < r1) z[r] = v;
+        }
+        __syncthreads();
+        for (int r = tid; r < r0; r += blockDim.x) {
+            double v = z[r];
+            const double *col = M + (size_t)r * ld;
+            for (int c = r0; c < r1; ++c) v = fma(-col[c], z[c], v);
+            z[r] = v;
+        }
+        __syncthreads();
+    }
+    for (int c = tid; c < n; c += blockDim.x) x[c] = z[c];
+}
+
+double *g_diag = nullptr;  // factored diagonal blocks, grow-only
+size_t g_diag_bytes = 0;
+
+}  // namespace
+
+extern "C" int irwls_dev_zero_upper(double *d_M, int n, int ld) {
+    if (n <= 1) return 0;
+    zero_upper_kernel<<<ceil_div((long long)n * n, 256) < 4096 ? ceil_div((long long)n * n, 256) : 4096, 256, 0,
+                        irwls_stream()>>>(d_M, n, ld);
+    IRWLS_LAUNCH_CHECK("zero_upper");
+    return 0;
+}
+
+extern "C" int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_b, double *d_x) {
+    if (n <= 0) return 0;
+    if (ld < n + 1) {
+        irwls_set_error(-6, "Cholesky leading dimension %d < n + 1 = %d", ld, n + 1);
+        return -6;
+    }
+    int *flags = irwls_dev_flags();
+    if (irwls_dev_memset(flags, 0, sizeof(int))) return -2;
+    const int has_b = d_x != nullptr;  // the right-hand side is (or is copied into) row n
+    const int nrows = n + has_b;
+    if (d_b) {
+        // b becomes row n: M[c*ld + n] = b[c]
+        cudaError_t e = cudaMemcpy2DAsync(d_M + n, (size_t)ld * sizeof(double), d_b, sizeof(double), sizeof(double), n,
+                                          cudaMemcpyDeviceToDevice, irwls_stream());
+        if (e != cudaSuccess) {
+            irwls_set_error(-2, "rhs copy: %s", cudaGetErrorString(e));
+            return -2;
+        }
+    }
+    const int npanel = ceil_div(n, NB);
+    const size_t dbytes = (size_t)npanel * NB * NB * sizeof(double);
+    if (dbytes > g_diag_bytes) {
+        if (g_diag) {
+            cudaStreamSynchronize(irwls_stream());
+            cudaFree(g_diag);
+        }
+        g_diag = nullptr;
+        g_diag_bytes = 0;
+        if (irwls_dev_malloc((void **)&g_diag, dbytes)) return -3;
+        g_diag_bytes = dbytes;
+    }
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_CHOL);
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = min(NB, n - k0);
+        const int below = nrows - (k0 + nb);
+        const int grid = below > 0 ? ceil_div(below, 128) : 1;
+        chol_panel_kernel<<<grid, 128, 0, irwls_stream()>>>(d_M, n, ld, k0, nb, nrows, flags,
+                                                             g_diag + (size_t)(k0 / NB) * NB * NB);
+        IRWLS_LAUNCH_CHECK("chol_panel");
+        if (below > 0 && k0 + nb < n) {
+            dim3 g(ceil_div(n - (k0 + nb), 32), ceil_div(below, 32));
+            chol_update_kernel<<<g, 256, 0, irwls_stream()>>>(d_M, n, ld, k0, nb, nrows);
+            IRWLS_LAUNCH_CHECK("chol_update");
+        }
+    }
+    chol_store_diag_kernel<<<npanel, 256, 0, irwls_stream()>>>(d_M, n, ld, g_diag);
+    IRWLS_LAUNCH_CHECK("chol_store_diag");
+    if (has_b) {
+        const size_t smem = (size_t)n * sizeof(double);
+        if (smem > 48 * 1024) {
+            if (smem > 200 * 1024) {
+                irwls_set_error(-6, "system of order %d exceeds the backward-solve tile", n);
+                return -6;
+            }
+            cudaFuncSetAttribute(chol_backsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        chol_backsolve_kernel<<<1, 256, smem, irwls_stream()>>>(d_M, n, ld, d_x);
+        IRWLS_LAUNCH_CHECK("chol_backsolve");
+    }
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_CHOL);
+    return 0;
+}
+
+namespace {
+// out = A v (trans = 0) or out = A^T v (trans = 1) for a column-major size x
+// size matrix; one warp per output entry.
+__global__ void gemv_kernel(const double *__restrict__ A, const double *__restrict__ v, double *__restrict__ out,
+                            int size, int trans) {
+    const int lane = threadIdx.x & 31;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= size) return;
+    double acc = 0.0;
+    if (trans)
+        for (int i = lane; i < size; i += 32) acc = fma(A[(size_t)w * size + i], v[i], acc);
+    else
+        for (int j = lane; j < size; j += 32) acc = fma(A[(size_t)j * size + w], v[j], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[w] = acc;
+}
+}  // namespace
+
+extern "C" int irwls_dev_gemv(const double *d_A, const double *d_v, double *d_out, int size, int trans) {
+    if (size <= 0) return 0;
+    gemv_kernel<<<ceil_div((long long)size * 32, 256), 256, 0, irwls_stream()>>>(d_A, d_v, d_out, size, trans);
+    IRWLS_LAUNCH_CHECK("gemv");
+    return 0;
+}

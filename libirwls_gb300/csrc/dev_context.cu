@@ -1,0 +1,353 @@
+// dev_context.cu -- device context of the library: one CUDA stream, error
+// state, memory helpers, dataset upload and kernel timing.
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "dev_common.cuh"
+
+static cudaStream_t g_stream = nullptr;
+static int g_inited = 0;
+static int g_num_sms = 0;
+static int g_err = 0;
+static char g_msg[512] = "";
+static long long g_launches = 0;
+
+static int *g_flags = nullptr;  // device status words, see irwls_dev_flags()
+
+extern "C" void irwls_set_error(int code, const char *fmt, ...) {
+    if (g_err) return;  // keep the first error
+    g_err = code;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+    va_end(ap);
+}
+extern "C" int irwls_get_error(void) { return g_err; }
+extern "C" const char *irwls_get_error_message(void) { return g_msg; }
+extern "C" void irwls_clear_error(void) {
+    g_err = 0;
+    g_msg[0] = 0;
+}
+
+cudaStream_t irwls_stream() { return g_stream; }
+int *irwls_dev_flags() { return g_flags; }
+int irwls_num_sms() { return g_num_sms; }
+
+extern "C" long long irwls_launch_count(void) { return g_launches; }
+extern "C" void irwls_count_launch(int n) { g_launches += n; }
+
+static int cuda_fail(cudaError_t e, const char *what) {
+    irwls_set_error(-2, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+    return -2;
+}
+
+int irwls_check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    return 0;
+}
+
+extern "C" int irwls_dev_init(void) {
+    if (g_inited) return 0;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        irwls_set_error(-1, "no CUDA device available (%s); this library has no CPU path",
+                        e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        return -1;
+    }
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if ((e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return cuda_fail(e, "cudaDeviceGetAttribute");
+    if ((e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamCreate");
+    if ((e = cudaMalloc((void **)&g_flags, 8 * sizeof(int))) != cudaSuccess) return cuda_fail(e, "flags alloc");
+    if ((e = cudaMemset(g_flags, 0, 8 * sizeof(int))) != cudaSuccess) return cuda_fail(e, "flags init");
+    g_inited = 1;
+    return 0;
+}
+
+extern "C" int irwls_dev_sync(void) {
+    cudaError_t e = cudaStreamSynchronize(g_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
+    return 0;
+}
+
+extern "C" int irwls_dev_malloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        irwls_set_error(-3, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        *p = nullptr;
+        return -3;
+    }
+    return 0;
+}
+extern "C" int irwls_dev_free(void *p) {
+    if (p) cudaFree(p);
+    return 0;
+}
+extern "C" int irwls_dev_h2d(void *d, const void *h, size_t bytes) {
+    if (!bytes) return 0;
+    cudaError_t e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g_stream);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "H2D copy");
+}
+extern "C" int irwls_dev_d2h(void *h, const void *d, size_t bytes) {
+    if (!bytes) return 0;
+    cudaError_t e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, g_stream);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "D2H copy");
+}
+extern "C" int irwls_dev_d2d(void *d, const void *s, size_t bytes) {
+    if (!bytes) return 0;
+    cudaError_t e = cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToDevice, g_stream);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "D2D copy");
+}
+extern "C" int irwls_dev_memset(void *d, int byte, size_t bytes) {
+    if (!bytes) return 0;
+    cudaError_t e = cudaMemsetAsync(d, byte, bytes, g_stream);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "memset");
+}
+extern "C" int irwls_dev_host_alloc(void **p, size_t bytes) {
+    cudaError_t e = cudaMallocHost(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, "cudaMallocHost");
+    }
+    return 0;
+}
+extern "C" void irwls_dev_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+static void *g_ws = nullptr;
+static size_t g_ws_bytes = 0;
+extern "C" int irwls_dev_workspace(size_t bytes, void **d_ws) {
+    if (bytes > g_ws_bytes) {
+        if (g_ws) {
+            cudaStreamSynchronize(g_stream);
+            cudaFree(g_ws);
+            g_ws = nullptr;
+            g_ws_bytes = 0;
+        }
+        if (irwls_dev_malloc(&g_ws, bytes)) return -3;
+        g_ws_bytes = bytes;
+    }
+    *d_ws = g_ws;
+    return 0;
+}
+extern "C" void irwls_dev_release_workspace(void) {
+    if (g_ws) {
+        cudaStreamSynchronize(g_stream);
+        cudaFree(g_ws);
+    }
+    g_ws = nullptr;
+    g_ws_bytes = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Dataset upload. Rows are walked on the host exactly as the reference walks
+// its svm_sample lists; the device keeps a dense copy (raw values for the
+// raw-RBF mode, values by feature index otherwise) plus CSR by feature index.
+// ---------------------------------------------------------------------------
+extern "C" int irwls_feature_width(const svm_dataset *ds, int n_rows) {
+    int w = 1;
+    for (int i = 0; i < n_rows; ++i)
+        for (const svm_sample *p = ds->x[i]; p->index != -1; ++p)
+            if (p->index + 1 > w) w = p->index + 1;
+    return w;
+}
+extern "C" int irwls_model_feature_width(const model *m) {
+    int w = 1;
+    for (int i = 0; i < m->nSVs; ++i)
+        for (const svm_sample *p = m->x[i]; p->index != -1; ++p)
+            if (p->index + 1 > w) w = p->index + 1;
+    return w;
+}
+
+static int upload_rows(svm_sample *const *rows, const double *q, const double *y, int n_rows, int mode,
+                       double gamma, int raw_width, int width_hint, irwls_dev_set *out) {
+    memset(out, 0, sizeof *out);
+    if (irwls_dev_init()) return -1;
+    out->n_rows = n_rows;
+    out->mode = mode;
+    out->neg_gamma = -gamma;
+    long long nnz = 0;
+    int width = 1;
+    for (int i = 0; i < n_rows; ++i)
+        for (const svm_sample *p = rows[i]; p->index != -1; ++p) {
+            ++nnz;
+            if (p->index < 0) {
+                irwls_set_error(-4, "negative feature index %d in row %d", p->index, i);
+                return -4;
+            }
+            if (p->index + 1 > width) width = p->index + 1;
+        }
+    if (width_hint > width) width = width_hint;
+    if (mode == IRWLS_K_RAW_RBF) width = raw_width > 0 ? raw_width : 1;
+    out->width = width;
+    out->ld = (width + 1) & ~1;
+    out->nnz = nnz;
+    if (nnz > 2147483647LL) {
+        irwls_set_error(-4, "dataset has %lld stored entries; the device layout indexes them with int32", nnz);
+        return -4;
+    }
+    const size_t xbytes = (size_t)n_rows * out->ld * sizeof(double);
+    const size_t bytes = xbytes + (size_t)(n_rows + 1) * sizeof(int) + (size_t)nnz * (sizeof(int) + sizeof(double)) +
+                         2 * (size_t)n_rows * sizeof(double);
+    void *h = nullptr;
+    if (irwls_dev_host_alloc(&h, bytes)) return -3;
+    double *hX = (double *)h;
+    double *hq = hX + (size_t)n_rows * out->ld;
+    double *hy = hq + n_rows;
+    double *hcv = hy + n_rows;
+    int *hrp = (int *)(hcv + nnz);
+    int *hci = hrp + n_rows + 1;
+    memset(hX, 0, xbytes);
+    long long k = 0;
+    for (int i = 0; i < n_rows; ++i) {
+        hrp[i] = (int)k;
+        double *row = hX + (size_t)i * out->ld;
+        if (mode == IRWLS_K_RAW_RBF) {
+            // maxdim consecutive values from the row start, as src/kernels.c:93-97 reads them
+            const svm_sample *p = rows[i];
+            for (int t = 0; t < raw_width; ++t) row[t] = p[t].value;
+        }
+        for (const svm_sample *p = rows[i]; p->index != -1; ++p) {
+            if (mode != IRWLS_K_RAW_RBF) row[p->index] = p->value;
+            hci[k] = p->index;
+            hcv[k] = p->value;
+            ++k;
+        }
+        hq[i] = q ? q[i] : 0.0;
+        hy[i] = y ? y[i] : 0.0;
+    }
+    hrp[n_rows] = (int)k;
+    int rc = 0;
+    rc |= irwls_dev_malloc((void **)&out->X, xbytes);
+    rc |= irwls_dev_malloc((void **)&out->q, n_rows * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&out->y, n_rows * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&out->rp, (n_rows + 1) * sizeof(int));
+    rc |= irwls_dev_malloc((void **)&out->ci, (nnz ? nnz : 1) * sizeof(int));
+    rc |= irwls_dev_malloc((void **)&out->cv, (nnz ? nnz : 1) * sizeof(double));
+    if (!rc) {
+        rc |= irwls_dev_h2d(out->X, hX, xbytes);
+        rc |= irwls_dev_h2d(out->q, hq, n_rows * sizeof(double));
+        rc |= irwls_dev_h2d(out->y, hy, n_rows * sizeof(double));
+        rc |= irwls_dev_h2d(out->rp, hrp, (n_rows + 1) * sizeof(int));
+        rc |= irwls_dev_h2d(out->ci, hci, nnz * sizeof(int));
+        rc |= irwls_dev_h2d(out->cv, hcv, nnz * sizeof(double));
+    }
+    // the staging buffer is pinned: wait for the copies before freeing it
+    rc |= irwls_dev_sync();
+    irwls_dev_host_free(h);
+    if (rc) {
+        irwls_dev_release(out);
+        return rc ? rc : -3;
+    }
+    return 0;
+}
+
+extern "C" int irwls_dev_upload(const svm_dataset *ds, int n_rows, int kernelType, double gamma, int force_norm,
+                                int width_hint, irwls_dev_set *out) {
+    int mode = kernelType == 0 ? IRWLS_K_LINEAR
+                               : ((ds->sparse == 0 && !force_norm) ? IRWLS_K_RAW_RBF : IRWLS_K_NORM_RBF);
+    return upload_rows(ds->x, ds->quadratic_value, ds->y, n_rows, mode, gamma, ds->maxdim, width_hint, out);
+}
+
+extern "C" int irwls_dev_upload_model(const model *m, int width_hint, irwls_dev_set *out) {
+    int mode = m->kernelType == 0 ? IRWLS_K_LINEAR : IRWLS_K_NORM_RBF;
+    return upload_rows(m->x, m->quadratic_value, nullptr, m->nSVs, mode, m->Kgamma, m->maxdim, width_hint, out);
+}
+
+extern "C" void irwls_dev_release(irwls_dev_set *s) {
+    if (!s) return;
+    cudaStreamSynchronize(g_stream);
+    cudaFree(s->X);
+    cudaFree(s->q);
+    cudaFree(s->y);
+    cudaFree(s->rp);
+    cudaFree(s->ci);
+    cudaFree(s->cv);
+    memset(s, 0, sizeof *s);
+}
+
+// ---------------------------------------------------------------------------
+// Timing of selected kernels with CUDA events on the library stream.
+// ---------------------------------------------------------------------------
+struct ProfSlot {
+    std::vector<cudaEvent_t> pending;  // begin/end pairs not yet read
+    std::vector<cudaEvent_t> pool;
+    double ms = 0.0;
+    long long launches = 0;
+};
+static ProfSlot g_prof[IRWLS_PROF_SLOTS];
+static int g_prof_on = 0;
+
+static cudaEvent_t prof_event(ProfSlot &s) {
+    if (!s.pool.empty()) {
+        cudaEvent_t e = s.pool.back();
+        s.pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+extern "C" void irwls_prof_enable(int on) { g_prof_on = on; }
+extern "C" int irwls_prof_on(void) { return g_prof_on; }
+extern "C" void irwls_prof_begin(int slot) {
+    if (!g_prof_on) return;
+    ProfSlot &s = g_prof[slot];
+    cudaEvent_t e = prof_event(s);
+    cudaEventRecord(e, g_stream);
+    s.pending.push_back(e);
+}
+extern "C" void irwls_prof_end(int slot) {
+    if (!g_prof_on) return;
+    ProfSlot &s = g_prof[slot];
+    cudaEvent_t e = prof_event(s);
+    cudaEventRecord(e, g_stream);
+    s.pending.push_back(e);
+    if (s.pending.size() > 4096) irwls_prof_collect();
+}
+extern "C" int irwls_prof_collect(void) {
+    cudaStreamSynchronize(g_stream);
+    for (auto &s : g_prof) {
+        for (size_t i = 0; i + 1 < s.pending.size(); i += 2) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, s.pending[i], s.pending[i + 1]);
+            s.ms += ms;
+            s.launches += 1;
+            s.pool.push_back(s.pending[i]);
+            s.pool.push_back(s.pending[i + 1]);
+        }
+        s.pending.clear();
+    }
+    return 0;
+}
+extern "C" void irwls_prof_read(int slot, double *ms, long long *launches) {
+    *ms = g_prof[slot].ms;
+    *launches = g_prof[slot].launches;
+}
+extern "C" void irwls_prof_reset(void) {
+    irwls_prof_collect();
+    for (auto &s : g_prof) {
+        s.ms = 0.0;
+        s.launches = 0;
+    }
+}
+
+extern "C" int irwls_dev_chol_info(int *info) {
+    int flags[8];
+    cudaError_t e = cudaMemcpyAsync(flags, g_flags, sizeof flags, cudaMemcpyDeviceToHost, g_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "read flags");
+    if (irwls_dev_sync()) return -2;
+    *info = flags[0];
+    return 0;
+}

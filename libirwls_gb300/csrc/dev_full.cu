@@ -1,0 +1,449 @@
+// dev_full.cu -- device steps of full IRWLS (reference src/full-train.c).
+//
+// The O(w) and O(l) bookkeeping (a_i weights, groups, list compaction,
+// classification into working/inactive/candidate sets, convergence sums) runs
+// in single-CTA kernels whose list orders and summation orders are the
+// reference's: lists come out in ascending sample order, and the sums that
+// feed convergence tests are accumulated left to right by one thread.
+// Kernel tiles and solves are in dev_tiles.cu and dev_chol.cu.
+#include <string.h>
+
+#include "dev_common.cuh"
+
+namespace {
+
+constexpr int CT = 1024;  // threads of the single-CTA bookkeeping kernels
+
+// Exclusive scan of per-thread counts in shared memory; returns the total.
+__device__ int block_exclusive_scan(int *s, int v) {
+    const int t = threadIdx.x;
+    s[t] = v;
+    __syncthreads();
+    for (int o = 1; o < CT; o <<= 1) {
+        int x = (t >= o) ? s[t - o] : 0;
+        __syncthreads();
+        s[t] += x;
+        __syncthreads();
+    }
+    const int incl = s[t];
+    const int total = s[CT - 1];
+    __syncthreads();
+    s[t] = incl - v;
+    __syncthreads();
+    return total;
+}
+
+// Ordered compaction: writes, in ascending i, every i < n with pred(i) to
+// out (through emit(pos, i)); returns the count (same in every thread).
+template <class Pred, class Emit>
+__device__ int block_compact(int n, Pred pred, Emit emit, int *s_scan) {
+    const int ch = (n + CT - 1) / CT;
+    const int b = threadIdx.x * ch, e = min(n, b + ch);
+    int c = 0;
+    for (int i = b; i < e; ++i) c += pred(i) ? 1 : 0;
+    const int total = block_exclusive_scan(s_scan, c);
+    int off = s_scan[threadIdx.x];
+    for (int i = b; i < e; ++i)
+        if (pred(i)) emit(off++, i);
+    __syncthreads();
+    return total;
+}
+
+// --- inner IRWLS -----------------------------------------------------------
+
+// a_i and groups at entry (src/full-train.c:131-155).
+__global__ void __launch_bounds__(CT) sub_init_kernel(irwls_sub_ws ws, const double *__restrict__ yg, double C) {
+    __shared__ int s_scan[CT];
+    const int w = ws.w;
+    for (int i = threadIdx.x; i < w; i += CT) {
+        const double yi = yg[ws.map[i]];
+        ws.y[i] = yi;
+        const double ei = ws.e[i];
+        const double ai = (ei * yi < 0) ? 0.0 : __ddiv_rn(__dmul_rn(1.0 * yi, C), ei);
+        ws.a[i] = ai;
+        ws.grp[i] = (ai == 0) ? 2 : ((ws.beta[i] == __dmul_rn(yi, C)) ? 3 : 1);
+    }
+    for (int i = threadIdx.x; i <= w; i += CT) ws.G13[i] = 0.0;
+    __syncthreads();
+    const int n1 = block_compact(w, [&](int i) { return ws.grp[i] == 1; },
+                                 [&](int p, int i) { ws.S1[p] = i; ws.gl1[p] = ws.map[i]; }, s_scan);
+    const int n3 = block_compact(w, [&](int i) { return ws.grp[i] == 3; },
+                                 [&](int p, int i) { ws.S3[p] = i; ws.gl3[p] = ws.map[i]; }, s_scan);
+    if (threadIdx.x == 0) {
+        ws.stats->nS1 = n1;
+        ws.stats->nS3 = n3;
+        ws.stats->dW = 1e9;
+        ws.stats->nW = 1.0;
+        ws.stats->bmax = 0.0;
+        ws.stats->bmin = 0.0;
+    }
+}
+
+// H and its right-hand side (src/full-train.c:165-186). H is column-major
+// with leading dimension ldH; only the lower triangle is read by the solver.
+// grid: (ceil(n1 / 64), n1): CTA (bx, i) fills row i, columns bx*64 .. of the
+// lower part; the A row (S1_i) is staged in shared memory.
+__global__ void __launch_bounds__(64) build_H_kernel(irwls_sub_ws ws, KView X, int n1) {
+    extern __shared__ double sA[];
+    const int i = blockIdx.y;
+    const int gi = ws.map[ws.S1[i]];
+    for (int t = threadIdx.x; t < X.ld; t += 64) sA[t] = X.X[(size_t)gi * X.ld + t];
+    __syncthreads();
+    const double qa = X.q[gi];
+    const double yi = ws.y[ws.S1[i]];
+    const int j = blockIdx.x * 64 + threadIdx.x;
+    if (j > i) return;
+    const int lj = ws.S1[j];
+    const double kv = kentry(X, sA, qa, ws.map[lj]);
+    double h = __dmul_rn(__dmul_rn(kv, yi), ws.y[lj]);
+    if (i == j) h = __dadd_rn(h, __ddiv_rn(1.0, ws.a[ws.S1[i]]));
+    ws.H[(size_t)j * ws.ldH + i] = h;
+}
+
+__global__ void build_border_kernel(irwls_sub_ws ws, int n1) {
+    const int w = ws.w;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n1; i += gridDim.x * blockDim.x) {
+        if (i < n1) {
+            const int li = ws.S1[i];
+            ws.H[(size_t)i * ws.ldH + n1] = ws.y[li];  // row n1, column i
+            ws.rhs[i] = __dsub_rn(__dsub_rn(1.0, ws.G13[i]), ws.GIN[li]);
+        } else {
+            ws.H[(size_t)n1 * ws.ldH + n1] = 0.0;
+            ws.rhs[n1] = __dsub_rn(-ws.G13[n1], ws.GIN[w]);
+        }
+    }
+}
+
+// New weights, convergence sums and the list of changed weights
+// (src/full-train.c:205-230 and the skip test of :242).
+__global__ void __launch_bounds__(CT) sub_update_kernel(irwls_sub_ws ws, double C, int n1, int n3) {
+    __shared__ int s_scan[CT];
+    const int w = ws.w;
+    for (int i = threadIdx.x; i <= w; i += CT) ws.bnew[i] = 0.0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n1; i += CT) ws.bnew[ws.S1[i]] = __dmul_rn(ws.bsol[i], ws.y[ws.S1[i]]);
+    for (int i = threadIdx.x; i < n3; i += CT) ws.bnew[ws.S3[i]] = __dmul_rn(C, ws.y[ws.S3[i]]);
+    if (threadIdx.x == 0) ws.bnew[w] = ws.bsol[n1];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bmax = 0.0, bmin = 0.0, dW = 0.0, nW = 0.0;
+        for (int i = 0; i < n1; ++i) {
+            const double b = ws.bsol[i];
+            if (b > bmax) bmax = b;
+            if (b < bmin) bmin = b;
+        }
+        for (int i = 0; i <= w; ++i) {
+            const double d = __dsub_rn(ws.bnew[i], ws.beta[i]);
+            dW = __dadd_rn(dW, __dmul_rn(d, d));
+            nW = __dadd_rn(nW, __dmul_rn(ws.beta[i], ws.beta[i]));
+        }
+        ws.stats->bmax = bmax;
+        ws.stats->bmin = bmin;
+        ws.stats->dW = dW;
+        ws.stats->nW = nW;
+        ws.scal[0] = __dsub_rn(ws.bnew[w], ws.beta[w]);
+    }
+    const int nl = block_compact(w, [&](int j) { return ws.bnew[j] != ws.beta[j]; },
+                                 [&](int p, int j) {
+                                     ws.lst[p] = ws.map[j];
+                                     ws.dlt[p] = __dsub_rn(ws.bnew[j], ws.beta[j]);
+                                 },
+                                 s_scan);
+    if (threadIdx.x == 0) ws.cnt[0] = nl;
+}
+
+// a_i, groups, beta <- bnew, S1/S3 lists, G13[n1] (src/full-train.c:264-344).
+__global__ void __launch_bounds__(CT) sub_groups_kernel(irwls_sub_ws ws, double C) {
+    __shared__ int s_scan[CT];
+    const int w = ws.w;
+    for (int i = threadIdx.x; i < w; i += CT) {
+        const double yi = ws.y[i], ei = ws.e[i];
+        const double ey = __dmul_rn(ei, yi);
+        double ai;
+        if (ey < 0.0) ai = 0.0;
+        else if (ey < (1.0 / 10000)) ai = __dmul_rn(C, 10000.0);
+        else ai = __ddiv_rn(__dmul_rn(1.0 * yi, C), ei);
+        ws.a[i] = ai;
+        int g = ws.grp[i];
+        if (ey < 0.0 && g != 2) g = 2;
+        const double by = __dmul_rn(yi, ws.bnew[i]);
+        if (g == 1 && by >= __dmul_rn(0.99, C) && by <= __dmul_rn(1.01, C)) g = 3;
+        if (ai == 0.0 && g == 1) g = 2;
+        if (g == 2 && ai != 0.0) g = 1;
+        ws.grp[i] = g;
+        ws.beta[i] = ws.bnew[i];
+    }
+    if (threadIdx.x == 0) ws.beta[w] = ws.bnew[w];
+    __syncthreads();
+    const int n1 = block_compact(w, [&](int i) { return ws.grp[i] == 1; },
+                                 [&](int p, int i) {
+                                     ws.S1[p] = i;
+                                     ws.gl1[p] = ws.map[i];
+                                 },
+                                 s_scan);
+    const int n3 = block_compact(w, [&](int i) { return ws.grp[i] == 3; },
+                                 [&](int p, int i) {
+                                     ws.S3[p] = i;
+                                     ws.gl3[p] = ws.map[i];
+                                     ws.rhs[p] = C;
+                                 },
+                                 s_scan);
+    for (int i = threadIdx.x; i <= n1; i += CT) ws.G13[i] = 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (n3 > 0) {
+            double g = 0.0;
+            for (int o = 0; o < n3; ++o) g = __dadd_rn(g, __dmul_rn(ws.rhs[o], ws.y[ws.S3[o]]));
+            ws.G13[n1] = g;
+        }
+        ws.stats->nS1 = n1;
+        ws.stats->nS3 = n3;
+    }
+}
+
+// --- outer loop --------------------------------------------------------------
+
+// Inactive samples with a non-zero weight, their weights, and GIN[nSW] =
+// sum of the weights of every inactive sample (src/full-train.c:436-456).
+__global__ void __launch_bounds__(CT) gin_prepare_kernel(const int *__restrict__ SIN, int nSIN,
+                                                         const double *__restrict__ bnew, int *lst, double *cb,
+                                                         int *cnt, double *GIN, int nSW) {
+    __shared__ int s_scan[CT];
+    const int n = block_compact(nSIN, [&](int o) { return bnew[SIN[o]] != 0.0; },
+                                [&](int p, int o) {
+                                    lst[p] = SIN[o];
+                                    cb[p] = bnew[SIN[o]];
+                                },
+                                s_scan);
+    if (threadIdx.x == 0) {
+        cnt[0] = n;
+        double g = 0.0;
+        for (int o = 0; o < nSIN; ++o) g = __dadd_rn(g, bnew[SIN[o]]);
+        GIN[nSW] = g;
+    }
+}
+
+__global__ void gather_ws_kernel(const int *__restrict__ SW, int nSW, const double *__restrict__ e,
+                                 const double *__restrict__ beta, int l, double *esub, double *bsub) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nSW; i += gridDim.x * blockDim.x) {
+        if (i < nSW) {
+            esub[i] = e[SW[i]];
+            bsub[i] = beta[SW[i]];
+        } else {
+            bsub[nSW] = beta[l];
+        }
+    }
+}
+
+// betaNew over the working set, the changed entries and the bias change
+// (src/full-train.c:488-510).
+__global__ void __launch_bounds__(CT) apply_ws_kernel(const int *__restrict__ SW, int nSW,
+                                                      const double *__restrict__ bt, const double *__restrict__ beta,
+                                                      int l, double *bnew, int *lst, double *cb, int *cnt,
+                                                      double *dbias) {
+    __shared__ int s_scan[CT];
+    for (int i = threadIdx.x; i < nSW; i += CT) bnew[SW[i]] = bt[i];
+    if (threadIdx.x == 0) {
+        bnew[l] = bt[nSW];
+        dbias[0] = __dsub_rn(bt[nSW], beta[l]);
+    }
+    __syncthreads();
+    const int n = block_compact(nSW, [&](int j) { return bnew[SW[j]] != beta[SW[j]]; },
+                                [&](int p, int j) {
+                                    lst[p] = SW[j];
+                                    cb[p] = __dsub_rn(bnew[SW[j]], beta[SW[j]]);
+                                },
+                                s_scan);
+    if (threadIdx.x == 0) cnt[0] = n;
+}
+
+__global__ void norms_kernel(const double *__restrict__ beta, const double *__restrict__ bnew, int n, double *out2) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double dW = 0.0, nW = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double d = __dsub_rn(beta[i], bnew[i]);
+        dW = __dadd_rn(dW, __dmul_rn(d, d));
+        nW = __dadd_rn(nW, __dmul_rn(beta[i], beta[i]));
+    }
+    out2[0] = dW;
+    out2[1] = nW;
+}
+
+// Classification of every sample after an outer iteration
+// (src/full-train.c:540-615): the first violator of each (kind, label) slot
+// joins the working set, other violators and all free weights become
+// candidates, the rest stay inactive.
+__device__ __forceinline__ int classify_one(double bi, double ei, double yi, double C, int *slot) {
+    // returns 0: inactive, 1: candidate, 2: violator (slot set), -1: none
+    const double thr = 0.001;
+    const double by = __dmul_rn(bi, yi);
+    int kind;
+    bool viol;
+    if (by == C) {
+        kind = 0;
+        viol = __dmul_rn(ei, yi) < -1.0 * thr;
+        if (!viol) return 0;
+    } else if (bi == 0.0) {
+        kind = 1;
+        viol = __dmul_rn(ei, yi) > thr;
+        if (!viol) return 0;
+    } else if (by != 0.0 && by != C) {
+        kind = 2;
+        viol = fabs(__dmul_rn(ei, yi)) > thr;
+        if (!viol) return 1;
+    } else {
+        return -1;
+    }
+    *slot = (yi == -1) ? 2 * kind : ((yi == 1) ? 2 * kind + 1 : -1);
+    return 2;
+}
+
+__global__ void __launch_bounds__(CT) classify_kernel(const double *__restrict__ bnew, const double *__restrict__ e,
+                                                      const double *__restrict__ y, int l, double C, int *SW,
+                                                      int *SC, int *SIN, irwls_outer_counts *counts) {
+    __shared__ int s_scan[CT];
+    __shared__ int first[6];
+    if (threadIdx.x < 6) first[threadIdx.x] = 0x7fffffff;
+    __syncthreads();
+    for (int i = threadIdx.x; i < l; i += CT) {
+        int slot = -1;
+        if (classify_one(bnew[i], e[i], y[i], C, &slot) == 2 && slot >= 0) atomicMin(&first[slot], i);
+    }
+    __syncthreads();
+    auto cat = [&](int i) {
+        int slot = -1;
+        const int c = classify_one(bnew[i], e[i], y[i], C, &slot);
+        if (c == 2) return (slot >= 0 && first[slot] == i) ? 2 : 1;
+        return c;  // 0 inactive, 1 candidate, -1 none
+    };
+    const int nsw = block_compact(l, [&](int i) { return cat(i) == 2; }, [&](int p, int i) { SW[p] = i; }, s_scan);
+    const int nsc = block_compact(l, [&](int i) { return cat(i) == 1; }, [&](int p, int i) { SC[p] = i; }, s_scan);
+    const int nin = block_compact(l, [&](int i) { return cat(i) == 0; }, [&](int p, int i) { SIN[p] = i; }, s_scan);
+    if (threadIdx.x == 0) {
+        counts->nSW = nsw;
+        counts->nSC = nsc;
+        counts->nSIN = nin;
+    }
+}
+
+__global__ void fill_ws_kernel(int *SW, int nSW, int *SIN, int nSIN, const int *__restrict__ SC, int nSC,
+                               const int *__restrict__ perm, int space) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nSC; i += gridDim.x * blockDim.x) {
+        const int v = SC[perm ? perm[i] : i];
+        if (i < space) SW[nSW + i] = v;
+        else SIN[nSIN + (i - space)] = v;
+    }
+}
+
+}  // namespace
+
+extern "C" int irwls_sub_alloc(irwls_sub_ws *ws, int cap) {
+    memset(ws, 0, sizeof *ws);
+    ws->cap = cap;
+    ws->ldH = cap + 2;
+    const size_t nd = (size_t)cap + 2;
+    int rc = 0;
+    double **dbl[] = {&ws->a, &ws->e, &ws->beta, &ws->bnew, &ws->bsol, &ws->bbest, &ws->G13, &ws->rhs, &ws->GIN,
+                      &ws->y, &ws->dlt, &ws->scal};
+    for (double **p : dbl) rc |= irwls_dev_malloc((void **)p, nd * sizeof(double));
+    int **ints[] = {&ws->grp, &ws->S1, &ws->S3, &ws->lst, &ws->gl1, &ws->gl3, &ws->cnt, &ws->mapbuf};
+    for (int **p : ints) rc |= irwls_dev_malloc((void **)p, nd * sizeof(int));
+    rc |= irwls_dev_malloc((void **)&ws->H, nd * nd * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&ws->stats, sizeof(irwls_sub_stats));
+    rc |= irwls_dev_host_alloc((void **)&ws->h_stats, sizeof(irwls_sub_stats));
+    ws->map = ws->mapbuf;
+    return rc ? -3 : 0;
+}
+
+extern "C" void irwls_sub_release(irwls_sub_ws *ws) {
+    irwls_dev_sync();
+    void *ptrs[] = {ws->a, ws->e, ws->beta, ws->bnew, ws->bsol, ws->bbest, ws->G13, ws->rhs, ws->GIN, ws->y,
+                    ws->dlt, ws->scal, ws->grp, ws->S1, ws->S3, ws->lst, ws->gl1, ws->gl3, ws->cnt, ws->mapbuf,
+                    ws->H, ws->stats};
+    for (void *p : ptrs) irwls_dev_free(p);
+    irwls_dev_host_free(ws->h_stats);
+    memset(ws, 0, sizeof *ws);
+}
+
+extern "C" int irwls_sub_init(irwls_sub_ws *ws, const irwls_dev_set *X, double C) {
+    sub_init_kernel<<<1, CT, 0, irwls_stream()>>>(*ws, X->y, C);
+    IRWLS_LAUNCH_CHECK("sub_init");
+    return 0;
+}
+
+// G13 of the current S1/S3 lists (src/full-train.c:327-344). The reference
+// computes it at the end of an iteration for use in the next one; it is
+// issued here at the start of the next iteration, when n1/n3 are known.
+extern "C" int irwls_sub_g13(irwls_sub_ws *ws, const irwls_dev_set *X, int n1, int n3) {
+    if (n3 <= 0 || n1 <= 0) return 0;
+    return irwls_dev_kernel_rowsum(X, ws->gl1, n1, X, ws->gl3, n3, ws->rhs, X->y, X->y, 0, +1, nullptr, nullptr,
+                                   ws->G13);
+}
+
+extern "C" int irwls_sub_iterate(irwls_sub_ws *ws, const irwls_dev_set *X, double C, int n1, int n3) {
+    const int n = n1 + 1;
+    KView kv = kview(X);
+    if (n1 > 0) {
+        dim3 grid(ceil_div(n1, 64), n1);
+        const size_t smem = (size_t)X->ld * sizeof(double);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(build_H_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        build_H_kernel<<<grid, 64, smem, irwls_stream()>>>(*ws, kv, n1);
+        IRWLS_LAUNCH_CHECK("build_H");
+    }
+    build_border_kernel<<<ceil_div(n1 + 1, 256), 256, 0, irwls_stream()>>>(*ws, n1);
+    IRWLS_LAUNCH_CHECK("build_border");
+    if (irwls_dev_chol_solve(ws->H, n, ws->ldH, ws->rhs, ws->bsol)) return -2;
+    sub_update_kernel<<<1, CT, 0, irwls_stream()>>>(*ws, C, n1, n3);
+    IRWLS_LAUNCH_CHECK("sub_update");
+    // e_i -= k(i, j) (bnew_j - beta_j) over changed j, then the bias change
+    if (irwls_dev_kernel_rowsum_n(X, ws->map, ws->w, X, ws->lst, ws->cnt, ws->dlt, nullptr, nullptr, -1, ws->e,
+                                  ws->scal, ws->e))
+        return -2;
+    sub_groups_kernel<<<1, CT, 0, irwls_stream()>>>(*ws, C);
+    IRWLS_LAUNCH_CHECK("sub_groups");
+    return 0;
+}
+
+extern "C" int irwls_full_gin(const irwls_dev_set *X, const int *d_SW, int nSW, const int *d_SIN, int nSIN,
+                              const double *d_bnew, int *d_lst, double *d_cb, int *d_cnt, double *d_GIN) {
+    gin_prepare_kernel<<<1, CT, 0, irwls_stream()>>>(d_SIN, nSIN, d_bnew, d_lst, d_cb, d_cnt, d_GIN, nSW);
+    IRWLS_LAUNCH_CHECK("gin_prepare");
+    return irwls_dev_kernel_rowsum_n(X, d_SW, nSW, X, d_lst, d_cnt, d_cb, X->y, nullptr, +1, nullptr, nullptr,
+                                     d_GIN);
+}
+
+extern "C" int irwls_full_gather_ws(const int *d_SW, int nSW, const double *d_e, const double *d_beta, int l,
+                                    double *d_esub, double *d_bsub) {
+    gather_ws_kernel<<<ceil_div(nSW + 1, 256), 256, 0, irwls_stream()>>>(d_SW, nSW, d_e, d_beta, l, d_esub, d_bsub);
+    IRWLS_LAUNCH_CHECK("gather_ws");
+    return 0;
+}
+
+extern "C" int irwls_full_apply_ws(const int *d_SW, int nSW, const double *d_bt, const double *d_beta, int l,
+                                   double *d_bnew, int *d_lst, double *d_cb, int *d_cnt, double *d_dbias) {
+    if (irwls_dev_d2d(d_bnew, d_beta, (size_t)(l + 1) * sizeof(double))) return -2;
+    apply_ws_kernel<<<1, CT, 0, irwls_stream()>>>(d_SW, nSW, d_bt, d_beta, l, d_bnew, d_lst, d_cb, d_cnt, d_dbias);
+    IRWLS_LAUNCH_CHECK("apply_ws");
+    return 0;
+}
+
+extern "C" int irwls_full_norms(const double *d_beta, const double *d_bnew, int n, double *d_out2) {
+    norms_kernel<<<1, 32, 0, irwls_stream()>>>(d_beta, d_bnew, n, d_out2);
+    IRWLS_LAUNCH_CHECK("norms");
+    return 0;
+}
+
+extern "C" int irwls_full_classify(const double *d_bnew, const double *d_e, const double *d_y, int l, double C,
+                                   int *d_SW, int *d_SC, int *d_SIN, irwls_outer_counts *d_counts) {
+    classify_kernel<<<1, CT, 0, irwls_stream()>>>(d_bnew, d_e, d_y, l, C, d_SW, d_SC, d_SIN, d_counts);
+    IRWLS_LAUNCH_CHECK("classify");
+    return 0;
+}
+
+extern "C" int irwls_full_fill_ws(int *d_SW, int nSW, int *d_SIN, int nSIN, const int *d_SC, int nSC,
+                                  const int *d_perm, int space) {
+    if (nSC <= 0) return 0;
+    fill_ws_kernel<<<ceil_div(nSC, 256), 256, 0, irwls_stream()>>>(d_SW, nSW, d_SIN, nSIN, d_SC, nSC, d_perm, space);
+    IRWLS_LAUNCH_CHECK("fill_ws");
+    return 0;
+}
