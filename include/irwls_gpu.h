@@ -48,6 +48,19 @@ void irwls_profile_reset(void);
 void irwls_profile_read(int slot, double *ms, long long *launches);
 /* Kernel launches issued by the library since it was loaded. */
 long long irwls_kernel_launches(void);
+/* Iterations and final active-row count of the last IRWLSpar run. */
+void irwls_last_run_info(int *par_iterations, int *active_rows);
+/* Host-to-device and device-to-host bytes copied since the library was loaded. */
+void irwls_transfer_bytes(long long *h2d, long long *d2h);
+/* Overwrites a device buffer of `bytes` bytes (allocated on first use) so
+ * that the next timed step starts with a cold L2. */
+int irwls_l2_flush(size_t bytes);
+/* CUDA-event timer on the library's stream: start, then stop returns ms. */
+int irwls_timer_start(void);
+double irwls_timer_stop(void);
+/* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-chain
+ * kernel: the roofline denominator of the FP64 kernels. */
+double irwls_fp64_peak_tflops(int reps);
 
 #ifdef __cplusplus
 }

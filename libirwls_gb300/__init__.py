@@ -44,6 +44,12 @@ def load() -> C.CDLL:
         "irwls_profile_reset": (None, []),
         "irwls_profile_read": (None, [C.c_int, PD, C.POINTER(C.c_longlong)]),
         "irwls_kernel_launches": (C.c_longlong, []),
+        "irwls_transfer_bytes": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "irwls_l2_flush": (C.c_int, [C.c_size_t]),
+        "irwls_timer_start": (C.c_int, []),
+        "irwls_timer_stop": (C.c_double, []),
+        "irwls_fp64_peak_tflops": (C.c_double, [C.c_int]),
+        "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "storeModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
         "readModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
     }

@@ -112,6 +112,12 @@ done:
     return rc ? -1 : 0;
 }
 
+static int g_last_iters = 0, g_last_nact = 0;
+void irwls_last_run_info(int *par_iterations, int *active_rows) {
+    *par_iterations = g_last_iters;
+    *active_rows = g_last_nact;
+}
+
 /* IRWLSpar on a resident dataset; weights_out gets betaBest (m values). */
 int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties props, double *weights_out) {
     const int m = props.size;
@@ -181,6 +187,8 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
                 since_best += 1;
             }
         }
+        g_last_iters = iter;
+        g_last_nact = nact;
     }
     if (irwls_dev_d2h(weights_out, d_bbest, (size_t)m * sizeof(double)) || irwls_dev_sync()) goto fail;
     goto done;

@@ -93,13 +93,16 @@ extern "C" int irwls_dev_free(void *p) {
     if (p) cudaFree(p);
     return 0;
 }
+extern "C" void irwls_count_bytes(long long h2d, long long d2h);
 extern "C" int irwls_dev_h2d(void *d, const void *h, size_t bytes) {
     if (!bytes) return 0;
+    irwls_count_bytes((long long)bytes, 0);
     cudaError_t e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g_stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "H2D copy");
 }
 extern "C" int irwls_dev_d2h(void *h, const void *d, size_t bytes) {
     if (!bytes) return 0;
+    irwls_count_bytes(0, (long long)bytes);
     cudaError_t e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, g_stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "D2H copy");
 }
@@ -350,4 +353,86 @@ extern "C" int irwls_dev_chol_info(int *info) {
     if (irwls_dev_sync()) return -2;
     *info = flags[0];
     return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Benchmark support: transfer counters, L2 flush, stream timers and a probe of
+// the device's FP64 FMA throughput (the roofline denominator of the FP64
+// kernels: chains of independent DFMAs, no memory traffic).
+// ---------------------------------------------------------------------------
+static long long g_h2d = 0, g_d2h = 0;
+extern "C" void irwls_count_bytes(long long h2d, long long d2h) {
+    g_h2d += h2d;
+    g_d2h += d2h;
+}
+extern "C" void irwls_transfer_bytes(long long *h2d, long long *d2h) {
+    *h2d = g_h2d;
+    *d2h = g_d2h;
+}
+
+static void *g_flush = nullptr;
+extern "C" int irwls_l2_flush(size_t bytes) {
+    if (irwls_dev_init()) return -1;
+    if (!g_flush && irwls_dev_malloc(&g_flush, bytes)) return -3;
+    return irwls_dev_memset(g_flush, 0x5a, bytes);
+}
+
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+extern "C" int irwls_timer_start(void) {
+    if (irwls_dev_init()) return -1;
+    if (!g_t0) {
+        cudaEventCreate(&g_t0);
+        cudaEventCreate(&g_t1);
+    }
+    cudaEventRecord(g_t0, g_stream);
+    return 0;
+}
+extern "C" double irwls_timer_stop(void) {
+    cudaEventRecord(g_t1, g_stream);
+    cudaEventSynchronize(g_t1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g_t0, g_t1);
+    return ms;
+}
+
+namespace {
+__global__ void fp64_probe_kernel(double *out, int iters) {
+    double a[8];
+    for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-3 + k;
+    const double b = 0.999999, c = 1e-7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
+    double s = 0;
+    for (int k = 0; k < 8; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+// FP64 FMA throughput in TFLOP/s, best of `reps` timed launches.
+extern "C" double irwls_fp64_peak_tflops(int reps) {
+    if (irwls_dev_init()) return 0.0;
+    const int blocks = 4 * g_num_sms, threads = 256, iters = 20000;
+    double *d = nullptr;
+    if (irwls_dev_malloc((void **)&d, (size_t)blocks * threads * sizeof(double))) return 0.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 0.0;
+    fp64_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
+    for (int r = 0; r < reps; ++r) {
+        cudaEventRecord(e0, g_stream);
+        fp64_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
+        cudaEventRecord(e1, g_stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double tf = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+        if (tf > best) best = tf;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    return best;
 }

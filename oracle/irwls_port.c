@@ -23,6 +23,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "IOStructures.h"
 
@@ -782,3 +783,171 @@ static double *predict_rows(svm_dataset ds, model m, predictProperties props, in
 }
 double *softTest(svm_dataset ds, model m, predictProperties props) { return predict_rows(ds, m, props, 0); }
 double *test(svm_dataset ds, model m, predictProperties props) { return predict_rows(ds, m, props, 1); }
+
+/* ------------------------------------------------------------------------ */
+/* Timing hooks for the CPU baseline of the benchmark (not reference API).   */
+/* ------------------------------------------------------------------------ */
+
+static double now_s(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+/* Times `nsteps` SGMA steps at order s0 (the loop body of SGMA above:
+ * candidates drawn and scored, the best one's kernel column built); the
+ * first step is untimed. The
+ * starting centroids are the first s0 of a rand() permutation, their kernel
+ * columns and the Cholesky factor of K_CC + jitter are built untimed.
+ * Returns the mean seconds per step. */
+double port_sgma_step_seconds(svm_dataset ds, properties props, int s0, int nsteps) {
+    const int l = ds.l, NC = 64, m = s0 + nsteps;
+    properties pr = props;
+    pr.size = s0;
+    int *start = randomCentroids(ds, pr);
+    int *cent = (int *)malloc(m * sizeof(int));
+    memcpy(cent, start, s0 * sizeof(int));
+    free(start);
+    double *KSC = (double *)malloc((size_t)l * m * sizeof(double));
+    double *L = (double *)calloc((size_t)m * m, sizeof(double));
+    double *KC = (double *)calloc((size_t)s0 * s0, sizeof(double));
+#pragma omp parallel for schedule(static) if (props.Threads > 1)
+    for (int r = 0; r < l; r++)
+        for (int s = 0; s < s0; s++) KSC[(size_t)s * l + r] = kernelFunction(ds, r, cent[s], props);
+    for (int a = 0; a < s0; a++)
+        for (int b = 0; b < s0; b++) KC[(size_t)b * s0 + a] = kernelFunction(ds, cent[a], cent[b], props) + (a == b ? 1e-5 : 0.0);
+    {
+        char lo = 'L';
+        int n = s0, info = 0;
+        scipy_dpotrf_(&lo, &n, KC, &n, &info);
+        for (int c = 0; c < s0; c++)
+            for (int r = c; r < s0; r++) L[(size_t)c * s0 + r] = KC[(size_t)c * s0 + r];
+    }
+    free(KC);
+    double *KNC = (double *)malloc((size_t)NC * m * sizeof(double));
+    double *KSM = (double *)malloc((size_t)NC * l * sizeof(double));
+    double *Z = (double *)malloc((size_t)NC * m * sizeof(double));
+    double score[64], eta[64];
+    int cand[64];
+    double t0 = now_s();
+    for (int s = s0; s < s0 + nsteps; s++) {
+        if (s == s0 + 1) t0 = now_s();  /* the first step warms caches and threads, untimed */
+        for (int i = 0; i < NC; i++) {
+            const double want = (i % 2) * 2.0 - 1;
+            int pick = rand() % l;
+            while (ds.y[pick] != want) pick = rand() % l;
+            cand[i] = pick;
+        }
+#pragma omp parallel for schedule(static) if (props.Threads > 1)
+        for (int i = 0; i < NC; i++) {
+            double *ksm = KSM + (size_t)i * l, *knc = KNC + (size_t)i * m, *z = Z + (size_t)i * m;
+            for (int r = 0; r < l; r++) ksm[r] = kernelFunction(ds, cand[i], r, props);
+            for (int r = 0; r < s0; r++) {
+                double v = kernelFunction(ds, cand[i], cent[r], props);
+                knc[r] = v;
+                z[r] = v;
+            }
+            char lo = 'L', nn = 'N';
+            int ss = s0, one = 1, info = 0, ll = l;
+            double fone = 1.0, mone = -1.0;
+            /* every timed step works at order s0 (the factor is not grown), so
+               the mean is the cost of one SGMA step with s0 centroids */
+            scipy_dpotrs_(&lo, &ss, &one, L, &ss, z, &ss, &info);
+            double v = 1.0;
+            for (int r = 0; r < s0; r++) v = v - (knc[r] * z[r]);
+            eta[i] = v;
+            scipy_dgemm_(&nn, &nn, &ll, &one, &ss, &fone, KSC, &ll, z, &ss, &mone, ksm, &ll);
+            double acc = 0.0;
+            for (int r = 0; r < l; r++) acc += ksm[r] * ksm[r];
+            score[i] = (eta[i] > 0.0) ? (1.0 / eta[i]) * acc : 0.0;
+        }
+        int best = 0;
+        for (int i = 1; i < NC; i++)
+            if (score[i] > score[best]) best = i;
+        cent[s] = cand[best];
+#pragma omp parallel for schedule(static) if (props.Threads > 1)
+        for (int r = 0; r < l; r++) KSC[(size_t)s * l + r] = kernelFunction(ds, r, cent[s], props);
+    }
+    const double dt = (now_s() - t0) / (nsteps > 1 ? nsteps - 1 : 1);
+    free(cent); free(KSC); free(L); free(KNC); free(KSM); free(Z);
+    return dt;
+}
+
+/* Times IRWLSpar's pieces on the given centroids: out[0] = seconds of the
+ * kernel-matrix build (KC and K_nm), out[1] = seconds of the first iteration
+ * (Gram dgemm over all rows, solve, residual dgemm, weights), out[2] = mean
+ * seconds of iterations 2..iters (Gram over the active rows only). */
+void port_irwls_seconds(svm_dataset ds, int *idx, properties props, int iters, double *out) {
+    const int m = props.size, l = ds.l;
+    double *KC = (double *)calloc((size_t)m * m, sizeof(double));
+    double *KSC = (double *)calloc((size_t)l * m, sizeof(double));
+    double *KSCA = (double *)calloc((size_t)l * m, sizeof(double));
+    double *Da = (double *)calloc(l, sizeof(double));
+    double *Day = (double *)calloc(l, sizeof(double));
+    const double t0 = now_s();
+#pragma omp parallel for schedule(static) if (props.Threads > 1)
+    for (int i = 0; i < m; i++)
+        for (int j = 0; j < m; j++) KC[(size_t)i * m + j] = kernelFunction(ds, idx[i], idx[j], props) + (i == j ? 1e-5 : 0.0);
+    const double M = 10000.0;
+#pragma omp parallel for schedule(static) if (props.Threads > 1)
+    for (int i = 0; i < l; i++) {
+        Da[i] = M;
+        Day[i] = ds.y[i] * M;
+        for (int j = 0; j < m; j++) {
+            double kv = kernelFunction(ds, i, idx[j], props);
+            KSC[(size_t)i * m + j] = kv;
+            KSCA[(size_t)i * m + j] = kv;
+        }
+    }
+    out[0] = now_s() - t0;
+    double *K1 = (double *)calloc((size_t)m * m, sizeof(double));
+    double *K2 = (double *)calloc(m, sizeof(double));
+    double *beta = (double *)calloc(m, sizeof(double));
+    double *e = (double *)calloc(l, sizeof(double));
+    int *act = (int *)calloc(l, sizeof(int));
+    char nn = 'N', tt = 'T';
+    int one = 1, nsv = l;
+    double fone = 1.0, mone = -1.0, zero = 0.0;
+    const int parts = (m < props.Threads) ? m : props.Threads;
+    double t1 = now_s();
+    for (int it = 0; it < iters; it++) {
+        if (it == 1) {
+            out[1] = now_s() - t1;
+            t1 = now_s();
+        }
+        memcpy(K1, KC, (size_t)m * m * sizeof(double));
+#pragma omp parallel for schedule(static) if (parts > 1)
+        for (int p = 0; p < parts; p++) {
+            int c0 = (int)round(p * m / parts), c1 = (int)round((p + 1) * m / parts) - 1;
+            int len = c1 - c0 + 1, mm = m, ns = nsv;
+            if (len > 0) {
+                scipy_dgemm_(&nn, &nn, &len, &one, &ns, &fone, &KSCA[c0], &mm, Day, &ns, &zero, &K2[c0], &mm);
+                scipy_dgemm_(&nn, &tt, &len, &mm, &ns, &fone, &KSCA[c0], &mm, KSCA, &mm, &fone, &K1[c0], &mm);
+            }
+        }
+        port_linear_system(K1, m, K2, beta);
+        memcpy(e, ds.y, l * sizeof(double));
+#pragma omp parallel for schedule(static) if (parts > 1)
+        for (int p = 0; p < parts; p++) {
+            int r0 = (int)round(p * l / parts), r1 = (int)round((p + 1) * l / parts) - 1;
+            int len = r1 - r0 + 1, mm = m;
+            if (len > 0) scipy_dgemm_(&nn, &nn, &one, &len, &mm, &mone, beta, &one, &KSC[(size_t)r0 * m], &mm, &fone, &e[r0], &one);
+        }
+        for (int i = 0; i < l; i++) {
+            Da[i] = (e[i] * ds.y[i] < 0.0) ? 0.0 : 1.0 * props.C / (ds.y[i] * e[i]);
+            if (Da[i] > M) Da[i] = M;
+        }
+        nsv = 0;
+        for (int i = 0; i < l; i++)
+            if (Da[i] != 0.0) act[nsv++] = i;
+#pragma omp parallel for schedule(static) if (props.Threads > 1)
+        for (int i = 0; i < nsv; i++) {
+            const double s = sqrt(Da[act[i]]);
+            for (int j = 0; j < m; j++) KSCA[(size_t)i * m + j] = s * KSC[(size_t)act[i] * m + j];
+            Day[i] = sqrt(Da[act[i]]) * ds.y[act[i]];
+        }
+    }
+    if (iters > 1) out[2] = (now_s() - t1) / (iters - 1);
+    else out[1] = now_s() - t1;
+    free(KC); free(KSC); free(KSCA); free(Da); free(Day); free(K1); free(K2); free(beta); free(e); free(act);
+}
