@@ -26,6 +26,11 @@ One step = one complete training (SGMA + IRWLSpar) of that workload.
           and second iterations timed at m = 1000 (later iterations costed
           as the second), with the iteration count of the GPU run.
 
+`--workload full` measures the dense full-IRWLS workload instead (n = 4000
+train rows, d = 20, two Gaussian classes with 10% flipped labels, RBF gamma =
+0.05, C = 10, working set 500); its CPU baseline is the restatement's whole
+training on all host cores (about 1-3 s, no extrapolation).
+
 `--impl reference` runs only the CPU baseline measurement above (the reference
 sources cannot be built on the GPU host, so the restatement stands in for it)
 and prints its line with "impl": "reference".
@@ -65,6 +70,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full"])
     return ap.parse_args()
 
 
@@ -336,9 +342,149 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# dense full-IRWLS workload
+# ----------------------------------------------------------------------------
+FULL = dict(n=4000, d=20, seed=20240601, gamma=0.05, C=10.0, w=500)
+
+
+def full_workload():
+    from libirwls_gb300 import _abi, synth
+
+    X, y = synth.two_gaussians(FULL["n"], FULL["d"], FULL["seed"])
+    data = synth.from_dense(X, y, keep_zeros=True)
+    return _abi.build_dataset(data.indptr, data.indices, data.values, data.y)
+
+
+def full_props(threads=1):
+    from libirwls_gb300 import _abi
+
+    return _abi.make_properties(gamma=FULL["gamma"], C_=FULL["C"], working_set=FULL["w"], threads=threads)
+
+
+def full_config():
+    return {"workload": "full IRWLS, plain FP64: n=4000, d=20 dense (two Gaussian classes, means +-0.5, "
+                        "10%% labels flipped), RBF gamma=0.05, C=10, working set 500",
+            "n": FULL["n"], "d": FULL["d"], "gamma": FULL["gamma"], "C": FULL["C"], "working_set": FULL["w"],
+            "form": "plain FP64", "parallelism": "single GPU",
+            "l2": "flushed between timed steps (512 MiB overwrite); the training set (0.7 MB) fits in L2"}
+
+
+def full_cpu(hd):
+    from libirwls_gb300 import _abi
+
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    port = _abi.load_library(os.path.join(ROOT, "oracle", "_build", "libirwls_port.so"))
+    cores = os.cpu_count() or 1
+    libc = C.CDLL(None)
+    libc.srand(0)
+    t0 = time.perf_counter()
+    b = port.trainFULL(hd.struct, full_props(threads=cores))
+    dt = time.perf_counter() - t0
+    libc.free.argtypes = [C.c_void_p]
+    libc.free(C.cast(b, C.c_void_p))
+    return {"value": round(dt, 3), "unit": "s", "cores": cores, "kind": "port",
+            "sample": "whole training by the CPU restatement of the reference, %d OpenMP threads" % cores}
+
+
+def run_full(args):
+    import numpy as np
+
+    from libirwls_gb300 import load
+
+    hd = full_workload()
+    if args.impl == "reference":
+        vals = [full_cpu(hd)["value"] for _ in range(args.warmup + args.steps)][args.warmup:]
+        v = statistics.mean(vals)
+        base = full_cpu(hd)
+        base["value"] = round(v, 3)
+        print(json.dumps({"metric": METRIC, "value": round(v, 3), "unit": "s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": round(v * 1000, 1), "higher_is_better": False, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+                          "config": full_config(), "cpu_baseline": base,
+                          "e2e": {"value": round(v, 3), "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    lib = load()
+    if not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    libc = C.CDLL(None)
+    p = full_props()
+    res = lib.irwls_resident_upload(hd.struct, p, 0)
+    beta = np.zeros(hd.l + 1)
+
+    def step():
+        libc.srand(0)
+        if lib.irwls_resident_full(res, p, beta.ctypes.data_as(PD)) != 0:
+            raise SystemExit("training failed: " + lib.irwls_last_error_message().decode())
+
+    for _ in range(args.warmup):
+        step()
+    lib.irwls_profile_enable(1)
+    lib.irwls_profile_reset()
+    launches0 = lib.irwls_kernel_launches()
+    clocks = Clocks(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        lib.irwls_l2_flush(512 << 20)
+        lib.irwls_timer_start()
+        step()
+        times.append(lib.irwls_timer_stop() / 1000.0)
+    clk = clocks.stop()
+    launches = lib.irwls_kernel_launches() - launches0
+    shares = {}
+    for slot, name in ((2, "kernel_rowsum"), (3, "cholesky_solve")):
+        ms, n = C.c_double(), C.c_longlong()
+        lib.irwls_profile_read(slot, C.byref(ms), C.byref(n))
+        shares[name] = (ms.value / 1000.0 / args.steps, n.value // args.steps)
+    lib.irwls_profile_enable(0)
+    step_s = statistics.mean(times)
+    e2e = None
+    if not args.no_e2e:
+        h0, d0 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
+        e_times = []
+        for _ in range(args.steps):
+            lib.irwls_l2_flush(512 << 20)
+            t0 = time.perf_counter()
+            libc.srand(0)
+            lib.initMemory(1, FULL["w"] + 1)
+            bp = lib.trainFULL(hd.struct, p)
+            if not bp:
+                raise SystemExit("e2e training failed: " + lib.irwls_last_error_message().decode())
+            e_times.append(time.perf_counter() - t0)
+        h1, d1 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
+        e2e = {"value": round(statistics.mean(e_times), 3), "unit": "s",
+               "h2d_bytes_per_step": int((h1.value - h0.value) // args.steps),
+               "d2h_bytes_per_step": int((d1.value - d0.value) // args.steps)}
+    lib.irwls_resident_free(res)
+    chol_s, chol_n = shares["cholesky_solve"]
+    peak = lib.irwls_fp64_peak_tflops(5)
+    # the systems solved have order ~ working-set free count + 1; their flops
+    # (n^3/3 per factorization) are not recorded per call, so the roofline is
+    # reported for the kernel row sums, with 2 flops per term plus the kernel
+    # entry (3d + 2 FP64 operations and one exp, counted as 3d + 2)
+    roofline = {"bound": "latency", "kernel": "cholesky_solve (blocked panel/update/backsolve launches)",
+                "achieved": None, "peak": round(peak, 4), "unit": "TFLOP/s", "frac": None, "traffic": None,
+                "share_of_step": round(chol_s / step_s, 4), "launches_per_step": int(chol_n),
+                "rowsum_share_of_step": round(shares["kernel_rowsum"][0] / step_s, 4)}
+    base = None if args.no_cpu else full_cpu(hd)
+    print(json.dumps({"metric": METRIC, "value": round(step_s, 3), "unit": "s", "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1000, 1),
+                      "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic (seeded generator)", "config": full_config(), "e2e": e2e,
+                      "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": base,
+                      "clocks": clk}), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "full":
+        run_full(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -62,6 +62,32 @@ double irwls_timer_stop(void);
  * kernel: the roofline denominator of the FP64 kernels. */
 double irwls_fp64_peak_tflops(int reps);
 
+/* Cholesky factorization and solve of one system on the GPU that allocates
+ * no memory; no counterpart in the reference. For callers that cannot let a
+ * library allocate device memory mid-run: processes that gave the device's
+ * memory to their own pool allocator at start-up, or latency-sensitive code
+ * that must not run cudaMalloc/cudaFree (they can synchronize the device).
+ *
+ * d_M: column-major n x n matrix in device memory, leading dimension
+ * ld >= n + 1 (row n holds the right-hand side); overwritten by its lower
+ * Cholesky factor (a non-positive pivot is stored as LAPACK dpotrf leaves it).
+ * d_b: right-hand side (n doubles, device) copied into row n, or NULL if row n
+ * already holds it. d_x: solution (n doubles, device), or NULL to factor only.
+ * d_info: NULL, or a device int that receives the first failed pivot
+ * (1-based, 0 if none). stream: a cudaStream_t, or NULL for the default
+ * stream; the call only enqueues work on it.
+ *
+ * Limit: n <= 4096; larger orders are rejected (-11, see
+ * irwls_last_error_message). Scratch: one 1 MiB array in the library's
+ * device memory, held by every GPU that loads the library until the process
+ * exits. All calls share it and it keeps the last call's contents, so calls
+ * that overlap on the GPU (on different streams) race; serialize them. The
+ * first call on each device looks up the array's device address (with that
+ * device current); make that first call before any stream capture.
+ * Returns 0 on success. */
+int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double *d_b, double *d_x, int *d_info,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -268,3 +268,103 @@ extern "C" int irwls_dev_gemv(const double *d_A, const double *d_v, double *d_ou
     IRWLS_LAUNCH_CHECK("gemv");
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the Cholesky solve.
+//
+// Some callers cannot let a library allocate device memory while they run: a
+// serving process that reserved the device's memory for its own pool
+// allocator at start-up (a cudaMalloc in the middle of a request can fail, or
+// force the pool to give memory back), or a latency-sensitive caller for whom
+// cudaMalloc/cudaFree must not run because they can synchronize the whole
+// device. irwls_chol_solve_noalloc serves them: the caller passes the matrix,
+// the right-hand side and the output (all device memory the caller owns) and a
+// stream, and the call itself allocates nothing. Its only scratch is the
+// file-scope array below, which every GPU that loads this library holds until
+// the process exits.
+//
+// The scratch keeps the factored 32x32 diagonal blocks (one per panel) and
+// the pivot status word, which sizes it for matrices of order up to
+// IRWLS_NOALLOC_MAX_ORDER (4096: 1 MiB of blocks).
+// ---------------------------------------------------------------------------
+#define IRWLS_NOALLOC_MAX_ORDER 4096
+#define IRWLS_NOALLOC_PANELS (IRWLS_NOALLOC_MAX_ORDER / NB)
+
+static __device__ __align__(256) double g_noalloc_scratch[IRWLS_NOALLOC_PANELS * NB * NB + 32];
+
+#define IRWLS_NOALLOC_DEVICES 64
+static double *g_noalloc_addr[IRWLS_NOALLOC_DEVICES];  // device address of the array, per device
+
+extern "C" int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double *d_b, double *d_x, int *d_info,
+                                        void *stream) {
+    irwls_clear_error();
+    if (n <= 0) return 0;
+    if (n > IRWLS_NOALLOC_MAX_ORDER) {
+        irwls_set_error(-11, "irwls_chol_solve_noalloc: order %d exceeds its limit of %d", n, IRWLS_NOALLOC_MAX_ORDER);
+        return -11;
+    }
+    if (ld < n + 1) {
+        irwls_set_error(-6, "irwls_chol_solve_noalloc: leading dimension %d < n + 1 = %d", ld, n + 1);
+        return -6;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= IRWLS_NOALLOC_DEVICES) {
+        irwls_set_error(-2, "irwls_chol_solve_noalloc: no usable current device (%s)", cudaGetErrorString(e));
+        return -2;
+    }
+    // Set-up, once per device, with that device current: the host-side name
+    // of the array is not a device address, so ask the runtime for it.
+    if (!g_noalloc_addr[dev]) {
+        double *p = nullptr;
+        e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            irwls_set_error(-2, "irwls_chol_solve_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return -2;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    double *diag = g_noalloc_addr[dev];
+    int *flags = (int *)(diag + IRWLS_NOALLOC_PANELS * NB * NB);
+    cudaStream_t st = (cudaStream_t)stream;
+    // the pivot status must start at zero; the diagonal blocks are fully
+    // rewritten before they are read
+    if ((e = cudaMemsetAsync(flags, 0, sizeof(int), st)) != cudaSuccess) {
+        irwls_set_error(-2, "irwls_chol_solve_noalloc: %s", cudaGetErrorString(e));
+        return -2;
+    }
+    const int has_b = d_x != nullptr;
+    const int nrows = n + has_b;
+    if (d_b) {
+        e = cudaMemcpy2DAsync(d_M + n, (size_t)ld * sizeof(double), d_b, sizeof(double), sizeof(double), n,
+                              cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            irwls_set_error(-2, "irwls_chol_solve_noalloc: rhs copy: %s", cudaGetErrorString(e));
+            return -2;
+        }
+    }
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = min(NB, n - k0);
+        const int below = nrows - (k0 + nb);
+        const int grid = below > 0 ? ceil_div(below, 128) : 1;
+        chol_panel_kernel<<<grid, 128, 0, st>>>(d_M, n, ld, k0, nb, nrows, flags, diag + (size_t)(k0 / NB) * NB * NB);
+        IRWLS_LAUNCH_CHECK("chol_panel (noalloc)");
+        if (below > 0 && k0 + nb < n) {
+            dim3 g(ceil_div(n - (k0 + nb), 32), ceil_div(below, 32));
+            chol_update_kernel<<<g, 256, 0, st>>>(d_M, n, ld, k0, nb, nrows);
+            IRWLS_LAUNCH_CHECK("chol_update (noalloc)");
+        }
+    }
+    chol_store_diag_kernel<<<ceil_div(n, NB), 256, 0, st>>>(d_M, n, ld, diag);
+    IRWLS_LAUNCH_CHECK("chol_store_diag (noalloc)");
+    if (has_b) {
+        // order <= 4096: the backward sweep's vector fits the default 48 KiB
+        chol_backsolve_kernel<<<1, 256, (size_t)n * sizeof(double), st>>>(d_M, n, ld, d_x);
+        IRWLS_LAUNCH_CHECK("chol_backsolve (noalloc)");
+    }
+    if (d_info && (e = cudaMemcpyAsync(d_info, flags, sizeof(int), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) {
+        irwls_set_error(-2, "irwls_chol_solve_noalloc: %s", cudaGetErrorString(e));
+        return -2;
+    }
+    return 0;
+}
