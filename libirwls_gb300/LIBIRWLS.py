@@ -22,21 +22,21 @@ what the reference's extension returns.
 """
 from __future__ import annotations
 
-import ctypes as C
+import ctypes as ct
 
 import numpy as np
 
 from . import _abi, check, load as _load_lib
 
-_libc = C.CDLL(None)
-_libc.fopen.restype = C.c_void_p
-_libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
-_libc.fclose.argtypes = [C.c_void_p]
-_libc.free.argtypes = [C.c_void_p]
+_libc = ct.CDLL(None)
+_libc.fopen.restype = ct.c_void_p
+_libc.fopen.argtypes = [ct.c_char_p, ct.c_char_p]
+_libc.fclose.argtypes = [ct.c_void_p]
+_libc.free.argtypes = [ct.c_void_p]
 
-_capsule_get = C.pythonapi.PyCapsule_GetPointer
-_capsule_get.restype = C.c_void_p
-_capsule_get.argtypes = [C.py_object, C.c_char_p]
+_capsule_get = ct.pythonapi.PyCapsule_GetPointer
+_capsule_get.restype = ct.c_void_p
+_capsule_get.argtypes = [ct.py_object, ct.c_char_p]
 
 
 class Classifier:
@@ -67,7 +67,7 @@ def _model_of(classifier) -> _abi.Model:
     if isinstance(classifier, Classifier):
         return classifier.model
     ptr = _capsule_get(classifier, b"CLASSIFIER")
-    return C.cast(ptr, C.POINTER(_abi.Model)).contents
+    return ct.cast(ptr, ct.POINTER(_abi.Model)).contents
 
 
 def _arrays(data, labels):
@@ -96,7 +96,7 @@ def full_train(data, labels, gamma=1.0, C=1.0, threads=1, workingSet=500, eta=0.
         lib.initMemory(threads, workingSet + 1)
         beta = check(lib.trainFULL(ds, p), "full_train")
         mdl = lib.calculateFULLModel(p, ds, beta)
-        _libc.free(C.cast(beta, C.c_void_p))
+        _libc.free(ct.cast(beta, ct.c_void_p))
     finally:
         lib.freeDataset(ds)
     return Classifier(mdl)
@@ -116,8 +116,8 @@ def budgeted_train(data, labels, gamma=1.0, C=1.0, threads=1, size=10, algorithm
         cent = lib.randomCentroids(ds, p) if algorithm == 0 else check(lib.SGMA(ds, p), "budgeted_train (SGMA)")
         w = check(lib.IRWLSpar(ds, cent, p), "budgeted_train (IRWLS)")
         mdl = lib.calculateBudgetedModel(p, ds, cent, w)
-        _libc.free(C.cast(cent, C.c_void_p))
-        _libc.free(C.cast(w, C.c_void_p))
+        _libc.free(ct.cast(cent, ct.c_void_p))
+        _libc.free(ct.cast(w, ct.c_void_p))
     finally:
         lib.freeDataset(ds)
     return Classifier(mdl)
@@ -136,7 +136,7 @@ def predict(classifier, data, labels=None, threads=1, Soft=0, verbose=1):
         f = lib.softTest if Soft else lib.test
         out = check(f(ds, _model_of(classifier), pp), "predict")
         res = np.ctypeslib.as_array(out, shape=(X.shape[0],)).copy()
-        _libc.free(C.cast(out, C.c_void_p))
+        _libc.free(ct.cast(out, ct.c_void_p))
     finally:
         lib.freeDataset(ds)
     return res
@@ -149,9 +149,9 @@ def save(classifier, file):
     if not fp:
         raise OSError("cannot open %s" % file)
     try:
-        lib.storeModel(C.byref(_model_of(classifier)), C.c_void_p(fp))
+        lib.storeModel(ct.byref(_model_of(classifier)), ct.c_void_p(fp))
     finally:
-        _libc.fclose(C.c_void_p(fp))
+        _libc.fclose(ct.c_void_p(fp))
 
 
 def load(file):
@@ -162,11 +162,11 @@ def load(file):
         raise OSError("Input file with the trained model not found: %s" % file)
     mdl = _abi.Model()
     try:
-        lib.readModel(C.byref(mdl), C.c_void_p(fp))
+        lib.readModel(ct.byref(mdl), ct.c_void_p(fp))
     finally:
-        _libc.fclose(C.c_void_p(fp))
+        _libc.fclose(ct.c_void_p(fp))
     return Classifier(mdl)
 
 
 def C_double_p():
-    return C.POINTER(C.c_double)
+    return ct.POINTER(ct.c_double)

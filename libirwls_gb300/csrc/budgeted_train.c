@@ -128,11 +128,14 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
     double *d_KC = NULL, *d_KSC = NULL, *d_K1 = NULL, *d_part = NULL, *d_sd = NULL, *d_day = NULL, *d_e = NULL,
            *d_Da = NULL, *d_beta = NULL, *d_bnew = NULL, *d_bbest = NULL, *d_nrm = NULL, *h_nrm = NULL;
     const int ld = m + 1;
+    /* split-K chunks of the Gram update: about eight CTAs per SM over the
+       lower tiles, with at least 512 rows per chunk */
     const int sms = 152;
     const int tiles = ((m + 64) / 64) * ((m + 63) / 64 + 1) / 2;
-    int P = (2 * sms + tiles - 1) / tiles;
+    int P = (8 * sms + tiles - 1) / tiles;
+    if (P > l / 512) P = l / 512;
     if (P < 1) P = 1;
-    if (P > 16) P = 16;
+    if (P > 64) P = 64;
     rc |= irwls_dev_malloc((void **)&d_idx, (size_t)m * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_act, (size_t)l * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_nact, sizeof(int));

@@ -50,19 +50,26 @@ __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__re
         KN[(size_t)c * ldz + e] = kv;
     }
     __syncthreads();
-    // forward: L w = v
+    // forward: L w = v, 32-row blocks; the diagonal block is staged in Dg so
+    // the serial sweep of warp 0 reads shared memory
+    __shared__ double Dg[32][33];
     const int nblk = (s + 31) / 32;
     for (int b = 0; b < nblk; ++b) {
         const int r0 = b * 32, r1 = min(s, r0 + 32);
+        for (int t = tid; t < 32 * 32; t += blockDim.x) {
+            const int rr = t / 32, cc = t % 32;  // Dg[rr][cc] = L(r0 + rr, r0 + cc)
+            Dg[rr][cc] = (r0 + rr < r1 && r0 + cc < r1) ? L[(size_t)(r0 + rr) * ldL + r0 + cc] : 0.0;
+        }
+        __syncthreads();
         if (tid < 32) {
             const int r = r0 + tid;
             double x = (r < r1) ? v[r] : 0.0;
             for (int cc = r0; cc < r1; ++cc) {
                 double wc = 0.0;
-                if (r == cc) wc = x / L[(size_t)cc * ldL + cc];
+                if (r == cc) wc = x / Dg[cc - r0][cc - r0];
                 wc = __shfl_sync(0xffffffffu, wc, cc - r0);
                 if (r == cc) x = wc;
-                else if (r > cc && r < r1) x = fma(-L[(size_t)r * ldL + cc], wc, x);
+                else if (r > cc && r < r1) x = fma(-Dg[tid][cc - r0], wc, x);
             }
             if (r < r1) v[r] = x;
         }
@@ -70,6 +77,7 @@ __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__re
         for (int r = r1 + tid; r < s; r += blockDim.x) {
             double x = v[r];
             const double *row = L + (size_t)r * ldL;
+#pragma unroll 8
             for (int cc = r0; cc < r1; ++cc) x = fma(-row[cc], v[cc], x);
             v[r] = x;
         }
@@ -80,21 +88,27 @@ __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__re
     // backward: L^T z = w
     for (int b = nblk - 1; b >= 0; --b) {
         const int r0 = b * 32, r1 = min(s, r0 + 32);
+        for (int t = tid; t < 32 * 32; t += blockDim.x) {
+            const int rr = t / 32, cc = t % 32;
+            Dg[rr][cc] = (r0 + rr < r1 && r0 + cc < r1) ? L[(size_t)(r0 + rr) * ldL + r0 + cc] : 0.0;
+        }
+        __syncthreads();
         if (tid < 32) {
             const int r = r0 + tid;
             double x = (r < r1) ? v[r] : 0.0;
             for (int cc = r1 - 1; cc >= r0; --cc) {
                 double zc = 0.0;
-                if (r == cc) zc = x / L[(size_t)cc * ldL + cc];
+                if (r == cc) zc = x / Dg[cc - r0][cc - r0];
                 zc = __shfl_sync(0xffffffffu, zc, cc - r0);
                 if (r == cc) x = zc;
-                else if (r < cc) x = fma(-L[(size_t)cc * ldL + r], zc, x);
+                else if (r < cc) x = fma(-Dg[cc - r0][tid], zc, x);
             }
             if (r < r1) v[r] = x;
         }
         __syncthreads();
         for (int r = tid; r < r0; r += blockDim.x) {
             double x = v[r];
+#pragma unroll 8
             for (int cc = r0; cc < r1; ++cc) x = fma(-L[(size_t)cc * ldL + r], v[cc], x);
             v[r] = x;
         }
@@ -109,72 +123,95 @@ __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__re
     }
 }
 
-// acc[i][c] = sum_k KSC[k*l + i] Z[c*ldz + k]; r = acc - k(cand_c, x_i);
-// part[blk][c] = sum over the CTA's 128 rows of r^2.
-constexpr int GM = 128, GK = 16;
-__global__ void __launch_bounds__(256) sgma_gemm_kernel(KView X, int l, const int *__restrict__ cand, int s,
-                                                        const double *__restrict__ KSC, const double *__restrict__ Z,
-                                                        int ldz, double *__restrict__ part) {
-    __shared__ double As[2][GK][GM];
-    __shared__ double Bs[2][GK][NCAND + 1];
+// 8-byte asynchronous global->shared copy; src_bytes = 0 writes zeros.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// SGMA scores: for row tiles of GM rows and all 64 candidates,
+// acc[i][c] = sum_k KSC[k*l + i] Z[c*ldz + k], r = acc - k(cand_c, x_i), and
+// the sum of r^2 over the CTA's tiles goes to part[blockIdx.x][c].
+// Persistent: CTA b takes tiles b, b + gridDim.x, ... (a fixed order, so the
+// partial sums are deterministic); 32-row tiles keep the last round short.
+// K-steps of GK are double-buffered with cp.async.
+constexpr int GM = 32, GK = 16;
+__global__ void __launch_bounds__(256, 2) sgma_gemm_kernel(KView X, int l, const int *__restrict__ cand, int s,
+                                                           const double *__restrict__ KSC,
+                                                           const double *__restrict__ Z, int ldz,
+                                                           double *__restrict__ part) {
+    __shared__ __align__(16) double As[2][GK][GM];
+    __shared__ __align__(16) double Bs[2][GK][NCAND + 1];
     __shared__ double red[16][NCAND + 1];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;  // tx: candidate group, ty: row group
-    const int i0 = blockIdx.x * GM;
-    double acc[8][4];
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
-
-    auto load = [&](int buf, int k0) {
-        // A: GK x GM, coalesced along rows of a KSC column
-        for (int t = tid; t < GK * GM; t += 256) {
-            const int kk = t / GM, r = t % GM;
-            const int k = k0 + kk, i = i0 + r;
-            As[buf][kk][r] = (k < s && i < l) ? KSC[(size_t)k * l + i] : 0.0;
-        }
-        for (int t = tid; t < GK * NCAND; t += 256) {
-            const int c = t / GK, kk = t % GK;
-            const int k = k0 + kk;
-            Bs[buf][kk][c] = (k < s) ? Z[(size_t)c * ldz + k] : 0.0;
-        }
-    };
+    const int ntiles = (l + GM - 1) / GM;
     const int nk = (s + GK - 1) / GK;
-    if (nk > 0) load(0, 0);
-    __syncthreads();
-    for (int kt = 0; kt < nk; ++kt) {
-        const int buf = kt & 1;
-        if (kt + 1 < nk) load(buf ^ 1, (kt + 1) * GK);
-#pragma unroll
-        for (int kk = 0; kk < GK; ++kk) {
-            double av[8], bv[4];
-#pragma unroll
-            for (int a = 0; a < 8; ++a) av[a] = As[buf][kk][ty + 16 * a];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) bv[b] = Bs[buf][kk][tx + 16 * b];
-#pragma unroll
-            for (int a = 0; a < 8; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
-        }
-        __syncthreads();
-    }
-    // epilogue: subtract the candidate kernel value, square, reduce
     double ps[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int i0 = tile * GM;
+        double acc[2][4];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const int c = tx + 16 * b;
-        const int gc = cand[c];
-        const double *arow = X.X + (size_t)gc * X.ld;
-        const double qa = X.q[gc];
+        for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            const int i = i0 + ty + 16 * a;
-            if (i < l) {
-                const double kv = kentry(X, arow, qa, i);
-                const double r = acc[a][b] - kv;
-                ps[b] = fma(r, r, ps[b]);
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+        auto load = [&](int buf, int k0) {
+            for (int t = tid; t < GK * GM; t += 256) {
+                const int kk = t / GM, r = t % GM;
+                const int k = k0 + kk, i = i0 + r;
+                const bool ok = (k < s && i < l);
+                cp_async8(&As[buf][kk][r], ok ? (const void *)(KSC + (size_t)k * l + i) : (const void *)KSC,
+                          ok ? 8 : 0);
+            }
+            for (int t = tid; t < GK * NCAND; t += 256) {
+                const int c = t / GK, kk = t % GK;
+                const int k = k0 + kk;
+                const bool ok = k < s;
+                cp_async8(&Bs[buf][kk][c], ok ? (const void *)(Z + (size_t)c * ldz + k) : (const void *)Z,
+                          ok ? 8 : 0);
+            }
+            cp_async_commit();
+        };
+        if (nk > 0) load(0, 0);
+        for (int kt = 0; kt < nk; ++kt) {
+            const int buf = kt & 1;
+            if (kt + 1 < nk) {
+                load(buf ^ 1, (kt + 1) * GK);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();
+#pragma unroll
+            for (int kk = 0; kk < GK; ++kk) {
+                double av[2], bv[4];
+#pragma unroll
+                for (int a = 0; a < 2; ++a) av[a] = As[buf][kk][ty + 16 * a];
+#pragma unroll
+                for (int b = 0; b < 4; ++b) bv[b] = Bs[buf][kk][tx + 16 * b];
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+            }
+            __syncthreads();
+        }
+        // epilogue: subtract the candidate kernel value, square, accumulate
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int gc = cand[tx + 16 * b];
+            const double *arow = X.X + (size_t)gc * X.ld;
+            const double qa = X.q[gc];
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const int i = i0 + ty + 16 * a;
+                if (i < l) {
+                    const double r = acc[a][b] - kentry(X, arow, qa, i);
+                    ps[b] = fma(r, r, ps[b]);
+                }
             }
         }
     }
@@ -261,7 +298,9 @@ __global__ void add_diag_kernel(double *KC, int m, double v) {
 // Partial Gram tiles. A' row p = [sd_p * KSC[act_p, :], day_p] (m + 1 values).
 // Tile (bi, bj), bi >= bj, of the lower triangle of A'^T A' restricted to
 // columns < m; chunk z of the active rows. part layout: [P][m+1 rows][m cols]
-// row-major by output row.
+// row-major by output row. Row chunks of TK are copied with cp.async into a
+// double buffer, then scaled in place (each thread scales the values it
+// copied) so that the products use fl(sd * KSC) as the reference does.
 constexpr int TT = 64, TK = 16;
 __global__ void __launch_bounds__(256) gram_kernel(const double *__restrict__ KSC, int m, const int *__restrict__ act,
                                                    int nact, const double *__restrict__ sd,
@@ -271,38 +310,70 @@ __global__ void __launch_bounds__(256) gram_kernel(const double *__restrict__ KS
     if (bi < bj) return;
     const int r0 = bi * TT, c0 = bj * TT;  // output rows (0..m), output cols (0..m-1)
     const int p0 = z * chunk, p1 = min(nact, p0 + chunk);
-    __shared__ double Ai[TK][TT + 1];
-    __shared__ double Aj[TK][TT + 1];
+    __shared__ __align__(16) double Ai[2][TK][TT + 1];
+    __shared__ __align__(16) double Aj[2][TK][TT + 1];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     double acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
-    for (int p = p0; p < p1; p += TK) {
+    auto load = [&](int buf, int p) {
         for (int t = tid; t < TK * TT; t += 256) {
             const int kk = t / TT, cc = t % TT;
             const int pp = p + kk;
-            double vi = 0.0, vj = 0.0;
+            const int ci = r0 + cc, cj = c0 + cc;
+            const double *si = KSC, *sj = KSC;
+            int ni = 0, nj = 0;
             if (pp < p1) {
-                const int g = act[pp];
-                const double s = sd[pp];
-                const double *row = KSC + (size_t)g * m;
-                const int ci = r0 + cc, cj = c0 + cc;
-                vi = (ci < m) ? __dmul_rn(s, row[ci]) : ((ci == m) ? day[pp] : 0.0);
-                vj = (cj < m) ? __dmul_rn(s, row[cj]) : 0.0;
+                const double *row = KSC + (size_t)act[pp] * m;
+                if (ci < m) {
+                    si = row + ci;
+                    ni = 8;
+                } else if (ci == m) {
+                    si = day + pp;
+                    ni = 8;
+                }
+                if (cj < m) {
+                    sj = row + cj;
+                    nj = 8;
+                }
             }
-            Ai[kk][cc] = vi;
-            Aj[kk][cc] = vj;
+            cp_async8(&Ai[buf][kk][cc], si, ni);
+            cp_async8(&Aj[buf][kk][cc], sj, nj);
         }
+        cp_async_commit();
+    };
+    auto scale = [&](int buf, int p) {
+        for (int t = tid; t < TK * TT; t += 256) {
+            const int kk = t / TT, cc = t % TT;
+            const int pp = p + kk;
+            if (pp < p1) {
+                const double sc = sd[pp];
+                if (r0 + cc < m) Ai[buf][kk][cc] = __dmul_rn(sc, Ai[buf][kk][cc]);
+                if (c0 + cc < m) Aj[buf][kk][cc] = __dmul_rn(sc, Aj[buf][kk][cc]);
+            }
+        }
+    };
+    if (p0 < p1) load(0, p0);
+    int it = 0;
+    for (int p = p0; p < p1; p += TK, ++it) {
+        const int buf = it & 1;
+        if (p + TK < p1) {
+            load(buf ^ 1, p + TK);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        scale(buf, p);
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < TK; ++kk) {
             double ai[4], aj[4];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) ai[a] = Ai[kk][ty + 16 * a];
+            for (int a = 0; a < 4; ++a) ai[a] = Ai[buf][kk][ty + 16 * a];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) aj[b] = Aj[kk][tx + 16 * b];
+            for (int b = 0; b < 4; ++b) aj[b] = Aj[buf][kk][tx + 16 * b];
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -414,23 +485,40 @@ __global__ void first_weights_kernel(const double *__restrict__ y, int l, double
     }
 }
 
-__global__ void delta_kernel(const double *__restrict__ bnew, double *beta, int m, double *out2) {
-    if (threadIdx.x || blockIdx.x) return;
-    double dW = 0.0, nW = 0.0;
-    for (int i = 0; i < m; ++i) {
+// dW = |bnew - beta|^2, nW = |bnew|^2 (chunked, fixed order), beta <- bnew.
+__global__ void __launch_bounds__(CT) delta_kernel(const double *__restrict__ bnew, double *beta, int m,
+                                                   double *out2) {
+    __shared__ double red[33];
+    const int ch = (m + CT - 1) / CT;
+    const int b = threadIdx.x * ch, e = min(m, b + ch);
+    double vd = 0.0, vn = 0.0;
+    for (int i = b; i < e; ++i) {
         const double d = __dsub_rn(bnew[i], beta[i]);
-        dW = __dadd_rn(dW, __dmul_rn(d, d));
-        nW = __dadd_rn(nW, __dmul_rn(bnew[i], bnew[i]));
-        beta[i] = bnew[i];
+        vd = __dadd_rn(vd, __dmul_rn(d, d));
+        vn = __dadd_rn(vn, __dmul_rn(bnew[i], bnew[i]));
     }
-    out2[0] = dW;
-    out2[1] = nW;
+    const double dW = block_sum<CT>(vd, red);
+    const double nW = block_sum<CT>(vn, red);
+    __syncthreads();
+    for (int i = b; i < e; ++i) beta[i] = bnew[i];
+    if (threadIdx.x == 0) {
+        out2[0] = dW;
+        out2[1] = nW;
+    }
 }
 
 }  // namespace
 
 extern "C" int irwls_dev_kernel_block_t(const irwls_dev_set *A, const int *d_ia, int nA, const irwls_dev_set *B,
                                         const int *d_ib, int nB, double *d_out, long long ld_out, int trans);
+
+// CTAs of the persistent score GEMM: two per SM (its launch bound), at most
+// one per tile.
+static int sgma_gemm_grid(int l) {
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    const int ntiles = ceil_div(l, GM);
+    return ntiles < 2 * sms ? ntiles : 2 * sms;
+}
 
 extern "C" int irwls_sgma_first(const irwls_dev_set *X, int l, int *d_cent, double *d_L, int ldL, double *d_KSC) {
     // centroid 0 = row l (the positive class mean), set by the caller in d_cent
@@ -459,17 +547,18 @@ extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand
                                                           d_eta);
     IRWLS_LAUNCH_CHECK("sgma_cand");
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
-    sgma_gemm_kernel<<<ceil_div(l, GM), 256, 0, irwls_stream()>>>(kview(X), l, d_cand, s, d_KSC, d_Z, ldz, d_part);
+    sgma_gemm_kernel<<<sgma_gemm_grid(l), 256, 0, irwls_stream()>>>(kview(X), l, d_cand, s, d_KSC, d_Z, ldz,
+                                                                     d_part);
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_GEMM);
     IRWLS_LAUNCH_CHECK("sgma_gemm");
     return 0;
 }
 
-extern "C" int irwls_sgma_partials(int l) { return ceil_div(l, GM); }
+extern "C" int irwls_sgma_partials(int l) { return sgma_gemm_grid(l); }
 
 extern "C" int irwls_sgma_select(const double *d_part, int l, const double *d_eta, const int *d_cand, int s,
                                  int *d_cent, int *d_best, double *d_bestval) {
-    sgma_select_kernel<<<1, NCAND, 0, irwls_stream()>>>(d_part, ceil_div(l, GM), d_eta, d_cand, s, d_cent, d_best,
+    sgma_select_kernel<<<1, NCAND, 0, irwls_stream()>>>(d_part, sgma_gemm_grid(l), d_eta, d_cand, s, d_cent, d_best,
                                                         d_bestval);
     IRWLS_LAUNCH_CHECK("sgma_select");
     return 0;
@@ -534,7 +623,7 @@ extern "C" int irwls_par_weights(const double *d_Da, const double *d_y, int l, i
 }
 
 extern "C" int irwls_par_delta(const double *d_bnew, double *d_beta, int m, double *d_out2) {
-    delta_kernel<<<1, 32, 0, irwls_stream()>>>(d_bnew, d_beta, m, d_out2);
+    delta_kernel<<<1, CT, 0, irwls_stream()>>>(d_bnew, d_beta, m, d_out2);
     IRWLS_LAUNCH_CHECK("delta");
     return 0;
 }

@@ -24,30 +24,19 @@ namespace {
 
 constexpr int NB = 32;
 
-// Every CTA reads the (updated) diagonal block from M and factors it; CTA 0
-// stores the factor in Dout, not in M, because other CTAs of the same launch
-// may still be reading the block from M. The stored blocks are copied into M
-// after the last panel (chol_store_diag_kernel).
-__global__ void __launch_bounds__(128) chol_panel_kernel(double *__restrict__ M, int n, int ld, int k0, int nb,
-                                                         int nrows, int *__restrict__ flags,
-                                                         double *__restrict__ Dout) {
-    __shared__ double D[NB][NB + 1];
-    __shared__ int failed_at;
+// Factors the nb x nb diagonal block at (k0, k0) held in D (shared, NB x NB,
+// lower part valid), with LAPACK dpotrf's failed-pivot behaviour, and forms
+// the inverse of the lower factor in Di. Uses the whole CTA; ends synced.
+__device__ void factor_invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], int nb, int k0, int *flags,
+                                    int *failed_at) {
     const int tid = threadIdx.x;
-    for (int t = tid; t < NB * NB; t += blockDim.x) {
-        const int r = t / NB, c = t % NB;
-        D[r][c] = (r < nb && c <= r) ? M[(size_t)(k0 + c) * ld + k0 + r] : (r == c ? 1.0 : 0.0);
-    }
-    if (tid == 0) failed_at = -1;
+    if (tid == 0) *failed_at = -1;
     __syncthreads();
     for (int c = 0; c < nb; ++c) {
         if (tid == 0) {
             const double s = D[c][c];
-            if (s > 0.0) {
-                D[c][c] = sqrt(s);
-            } else if (failed_at < 0) {
-                failed_at = c;  // stored unsquare-rooted, as dpotrf leaves it
-            }
+            if (s > 0.0) D[c][c] = sqrt(s);
+            else if (*failed_at < 0) *failed_at = c;  // stored without its root, as dpotrf leaves it
         }
         __syncthreads();
         const double piv = D[c][c];
@@ -60,58 +49,87 @@ __global__ void __launch_bounds__(128) chol_panel_kernel(double *__restrict__ M,
         }
         __syncthreads();
     }
-    if (blockIdx.x == 0) {
-        for (int t = tid; t < NB * NB; t += blockDim.x) Dout[t] = D[t / NB][t % NB];
-        if (tid == 0 && failed_at >= 0) atomicCAS(flags, 0, k0 + failed_at + 1);
-    }
-    // rows below the block (and the right-hand-side row n when present)
-    const int i = k0 + nb + blockIdx.x * blockDim.x + tid;
-    if (i >= nrows) return;
-    double x[NB];
-#pragma unroll
-    for (int c = 0; c < NB; ++c) x[c] = (c < nb) ? M[(size_t)(k0 + c) * ld + i] : 0.0;
-#pragma unroll
-    for (int c = 0; c < NB; ++c) {
-        if (c < nb) {
-            double v = x[c];
-#pragma unroll
-            for (int t = 0; t < c; ++t) v = fma(-x[t], D[c][t], v);
-            x[c] = v / D[c][c];
+    // inverse of the lower factor, one column per thread
+    if (tid < NB) {
+        const int j = tid;
+        for (int r = 0; r < NB; ++r) Di[r][j] = 0.0;
+        if (j < nb) {
+            Di[j][j] = 1.0 / D[j][j];
+            for (int c = j + 1; c < nb; ++c) {
+                double acc = 0.0;
+                for (int t = j; t < c; ++t) acc = fma(D[c][t], Di[t][j], acc);
+                Di[c][j] = -acc / D[c][c];
+            }
         }
     }
-#pragma unroll
-    for (int c = 0; c < NB; ++c)
-        if (c < nb) M[(size_t)(k0 + c) * ld + i] = x[c];
+    __syncthreads();
+    if (tid == 0 && *failed_at >= 0) atomicCAS(flags, 0, k0 + *failed_at + 1);
 }
 
-__global__ void chol_store_diag_kernel(double *__restrict__ M, int n, int ld, const double *__restrict__ Dall) {
-    const int k0 = blockIdx.x * NB;
-    const int nb = min(NB, n - k0);
-    const double *D = Dall + (size_t)blockIdx.x * NB * NB;
-    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
-        const int r = t / nb, c = t % nb;
-        if (c <= r) M[(size_t)(k0 + c) * ld + k0 + r] = D[r * NB + c];
+__device__ void store_block(double *M, int ld, int k0, int nb, double (*D)[NB + 1], double (*Di)[NB + 1],
+                            double *Dinv) {
+    for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+        const int r = t / NB, c = t % NB;
+        if (r < nb && c <= r) M[(size_t)(k0 + c) * ld + k0 + r] = D[r][c];
+        Dinv[t] = Di[r][c];
     }
 }
 
-__global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(t / n), r = (int)(t % n);
-        if (r < c) M[(size_t)c * ld + r] = 0.0;
+// First diagonal block (the others are factored by the trailing update of
+// the previous panel).
+__global__ void __launch_bounds__(256) chol_factor0_kernel(double *__restrict__ M, int n, int ld,
+                                                           int *__restrict__ flags, double *__restrict__ Dinv) {
+    __shared__ double D[NB][NB + 1], Di[NB][NB + 1];
+    __shared__ int failed_at;
+    const int nb = min(NB, n);
+    for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+        const int r = t / NB, c = t % NB;
+        D[r][c] = (r < nb && c <= r) ? M[(size_t)c * ld + r] : 0.0;
+    }
+    __syncthreads();
+    factor_invert_block(D, Di, nb, 0, flags, &failed_at);
+    store_block(M, ld, 0, nb, D, Di, Dinv);
+}
+
+// Panel solve: rows i >= k0 + nb (and the right-hand-side row n when present)
+// get L[i, k0:k0+nb] = A[i, k0:k0+nb] D^-T, an independent 32-term dot per
+// output. 8 rows per CTA, one output per thread.
+__global__ void __launch_bounds__(256) chol_trsm_kernel(double *__restrict__ M, int ld, int k0, int nb, int nrows,
+                                                        const double *__restrict__ Dinv) {
+    __shared__ double Di[NB][NB + 1];
+    __shared__ double A[8][NB + 1];
+    const int tid = threadIdx.x;
+    const int i0 = k0 + nb + blockIdx.x * 8;
+    for (int t = tid; t < NB * NB; t += 256) Di[t / NB][t % NB] = Dinv[t];
+    {
+        const int c = tid / 8, r = tid % 8;  // 256 = 32 columns x 8 rows
+        const int i = i0 + r;
+        A[r][c] = (c < nb && i < nrows) ? M[(size_t)(k0 + c) * ld + i] : 0.0;
+    }
+    __syncthreads();
+    const int c = tid / 8, r = tid % 8;
+    const int i = i0 + r;
+    if (c < nb && i < nrows) {
+        double x = 0.0;
+        for (int t = 0; t <= c; ++t) x = fma(Di[c][t], A[r][t], x);
+        M[(size_t)(k0 + c) * ld + i] = x;
     }
 }
 
 // Trailing update of the lower part: M[i][j] -= sum_t L[i][t] L[j][t] over the
 // panel columns t, for k1 <= j <= i < nrows, j < n. One 32x32 tile per CTA.
+// The CTA of tile (0, 0) then factors and inverts that tile, which is the
+// next panel's diagonal block.
 __global__ void __launch_bounds__(256) chol_update_kernel(double *__restrict__ M, int n, int ld, int k0, int nb,
-                                                          int nrows) {
+                                                          int nrows, int *__restrict__ flags,
+                                                          double *__restrict__ Dinv_next) {
     const int bj = blockIdx.x, bi = blockIdx.y;
     if (bi < bj) return;
     const int k1 = k0 + nb;
     const int r0 = k1 + bi * 32, c0 = k1 + bj * 32;
     __shared__ double Li[32][NB + 1];
     __shared__ double Lj[32][NB + 1];
+    __shared__ int failed_at;
     const int tid = threadIdx.x;
     for (int t = tid; t < 32 * NB; t += 256) {
         const int r = t % 32, k = t / 32;
@@ -130,42 +148,97 @@ __global__ void __launch_bounds__(256) chol_update_kernel(double *__restrict__ M
         double *p = M + (size_t)gj * ld + gi;
         *p = *p - acc;
     }
+    if (bi != 0 || bj != 0) return;
+    // next diagonal block: reuse Li / Lj as D / Di
+    __syncthreads();
+    const int nb2 = min(NB, n - k1);
+    for (int t = tid; t < NB * NB; t += 256) {
+        const int rr = t / NB, c = t % NB;
+        Li[rr][c] = (rr < nb2 && c <= rr) ? M[(size_t)(k1 + c) * ld + k1 + rr] : 0.0;
+    }
+    __syncthreads();
+    factor_invert_block(Li, Lj, nb2, k1, flags, &failed_at);
+    store_block(M, ld, k1, nb2, Li, Lj, Dinv_next);
 }
 
-// Backward sweep L^T x = z with z in row n of M; one CTA, z kept in shared
-// memory, 32-row blocks from the bottom: warp 0 solves the diagonal block,
-// then all threads update the rows above it.
+// Backward sweep L^T x = z, z in row n of M; one CTA, z in shared memory,
+// 32-row blocks from the bottom: x_b = D_b^-T y_b (parallel dots with the
+// stored inverse), then the rows above are updated.
 __global__ void __launch_bounds__(256) chol_backsolve_kernel(const double *__restrict__ M, int n, int ld,
+                                                             const double *__restrict__ Dinv,
                                                              double *__restrict__ x) {
     extern __shared__ double z[];
+    __shared__ double Di[NB][NB + 1];
+    __shared__ double yb[NB];
     const int tid = threadIdx.x;
     for (int c = tid; c < n; c += blockDim.x) z[c] = M[(size_t)c * ld + n];
-    __syncthreads();
-    const int nblk = (n + 31) / 32;
+    const int nblk = (n + NB - 1) / NB;
     for (int b = nblk - 1; b >= 0; --b) {
-        const int r0 = b * 32, r1 = min(n, r0 + 32);
-        if (tid < 32) {
-            const int r = r0 + tid;
-            double v = (r < r1) ? z[r] : 0.0;
-            for (int c = r1 - 1; c >= r0; --c) {
-                double xc = 0.0;
-                if (r == c) xc = v / M[(size_t)c * ld + c];
-                xc = __shfl_sync(0xffffffffu, xc, c - r0);
-                if (r == c) v = xc;
-                else if (r < c) v = fma(-M[(size_t)r * ld + c], xc, v);
-            }
-            if (r < r1) z[r] = v;
+        const int r0 = b * NB, r1 = min(n, r0 + NB);
+        for (int t = tid; t < NB * NB; t += blockDim.x) Di[t / NB][t % NB] = Dinv[(size_t)b * NB * NB + t];
+        __syncthreads();
+        if (tid < NB) yb[tid] = (r0 + tid < r1) ? z[r0 + tid] : 0.0;
+        __syncthreads();
+        if (tid < r1 - r0) {
+            double v = 0.0;
+            for (int c = tid; c < r1 - r0; ++c) v = fma(Di[c][tid], yb[c], v);
+            z[r0 + tid] = v;
         }
         __syncthreads();
         for (int r = tid; r < r0; r += blockDim.x) {
             double v = z[r];
             const double *col = M + (size_t)r * ld;
+#pragma unroll 8
             for (int c = r0; c < r1; ++c) v = fma(-col[c], z[c], v);
             z[r] = v;
         }
         __syncthreads();
     }
     for (int c = tid; c < n; c += blockDim.x) x[c] = z[c];
+}
+
+__global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(t / n), r = (int)(t % n);
+        if (r < c) M[(size_t)c * ld + r] = 0.0;
+    }
+}
+
+// Enqueues the whole factorization (and the solve when has_b) on `st`, with
+// Dinv holding ceil(n/32) blocks of 32x32 doubles.
+int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Dinv, cudaStream_t st) {
+    const int has_b = d_x != nullptr;
+    const int nrows = n + has_b;
+    chol_factor0_kernel<<<1, 256, 0, st>>>(d_M, n, ld, flags, Dinv);
+    IRWLS_LAUNCH_CHECK("chol_factor0");
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = min(NB, n - k0);
+        const int below = nrows - (k0 + nb);
+        if (below <= 0) break;
+        chol_trsm_kernel<<<ceil_div(below, 8), 256, 0, st>>>(d_M, ld, k0, nb, nrows,
+                                                             Dinv + (size_t)(k0 / NB) * NB * NB);
+        IRWLS_LAUNCH_CHECK("chol_trsm");
+        if (k0 + nb < n) {
+            dim3 g(ceil_div(n - (k0 + nb), 32), ceil_div(below, 32));
+            chol_update_kernel<<<g, 256, 0, st>>>(d_M, n, ld, k0, nb, nrows, flags,
+                                                  Dinv + (size_t)(k0 / NB + 1) * NB * NB);
+            IRWLS_LAUNCH_CHECK("chol_update");
+        }
+    }
+    if (has_b) {
+        const size_t smem = (size_t)n * sizeof(double);
+        if (smem > 48 * 1024) {
+            if (smem > 160 * 1024) {
+                irwls_set_error(-6, "system of order %d exceeds the backward-solve tile", n);
+                return -6;
+            }
+            cudaFuncSetAttribute(chol_backsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        chol_backsolve_kernel<<<1, 256, smem, st>>>(d_M, n, ld, Dinv, d_x);
+        IRWLS_LAUNCH_CHECK("chol_backsolve");
+    }
+    return 0;
 }
 
 double *g_diag = nullptr;  // factored diagonal blocks, grow-only
@@ -189,8 +262,6 @@ extern "C" int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_
     }
     int *flags = irwls_dev_flags();
     if (irwls_dev_memset(flags, 0, sizeof(int))) return -2;
-    const int has_b = d_x != nullptr;  // the right-hand side is (or is copied into) row n
-    const int nrows = n + has_b;
     if (d_b) {
         // b becomes row n: M[c*ld + n] = b[c]
         cudaError_t e = cudaMemcpy2DAsync(d_M + n, (size_t)ld * sizeof(double), d_b, sizeof(double), sizeof(double), n,
@@ -213,33 +284,8 @@ extern "C" int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_
         g_diag_bytes = dbytes;
     }
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_CHOL);
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        const int nb = min(NB, n - k0);
-        const int below = nrows - (k0 + nb);
-        const int grid = below > 0 ? ceil_div(below, 128) : 1;
-        chol_panel_kernel<<<grid, 128, 0, irwls_stream()>>>(d_M, n, ld, k0, nb, nrows, flags,
-                                                             g_diag + (size_t)(k0 / NB) * NB * NB);
-        IRWLS_LAUNCH_CHECK("chol_panel");
-        if (below > 0 && k0 + nb < n) {
-            dim3 g(ceil_div(n - (k0 + nb), 32), ceil_div(below, 32));
-            chol_update_kernel<<<g, 256, 0, irwls_stream()>>>(d_M, n, ld, k0, nb, nrows);
-            IRWLS_LAUNCH_CHECK("chol_update");
-        }
-    }
-    chol_store_diag_kernel<<<npanel, 256, 0, irwls_stream()>>>(d_M, n, ld, g_diag);
-    IRWLS_LAUNCH_CHECK("chol_store_diag");
-    if (has_b) {
-        const size_t smem = (size_t)n * sizeof(double);
-        if (smem > 48 * 1024) {
-            if (smem > 200 * 1024) {
-                irwls_set_error(-6, "system of order %d exceeds the backward-solve tile", n);
-                return -6;
-            }
-            cudaFuncSetAttribute(chol_backsolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        }
-        chol_backsolve_kernel<<<1, 256, smem, irwls_stream()>>>(d_M, n, ld, d_x);
-        IRWLS_LAUNCH_CHECK("chol_backsolve");
-    }
+    int rc = chol_enqueue(d_M, n, ld, d_x, flags, g_diag, irwls_stream());
+    if (rc) return rc;
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_CHOL);
     return 0;
 }
@@ -283,7 +329,7 @@ extern "C" int irwls_dev_gemv(const double *d_A, const double *d_v, double *d_ou
 // file-scope array below, which every GPU that loads this library holds until
 // the process exits.
 //
-// The scratch keeps the factored 32x32 diagonal blocks (one per panel) and
+// The scratch keeps the inverted 32x32 diagonal blocks (one per panel) and
 // the pivot status word, which sizes it for matrices of order up to
 // IRWLS_NOALLOC_MAX_ORDER (4096: 1 MiB of blocks).
 // ---------------------------------------------------------------------------
@@ -333,8 +379,6 @@ extern "C" int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double
         irwls_set_error(-2, "irwls_chol_solve_noalloc: %s", cudaGetErrorString(e));
         return -2;
     }
-    const int has_b = d_x != nullptr;
-    const int nrows = n + has_b;
     if (d_b) {
         e = cudaMemcpy2DAsync(d_M + n, (size_t)ld * sizeof(double), d_b, sizeof(double), sizeof(double), n,
                               cudaMemcpyDeviceToDevice, st);
@@ -343,25 +387,9 @@ extern "C" int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double
             return -2;
         }
     }
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        const int nb = min(NB, n - k0);
-        const int below = nrows - (k0 + nb);
-        const int grid = below > 0 ? ceil_div(below, 128) : 1;
-        chol_panel_kernel<<<grid, 128, 0, st>>>(d_M, n, ld, k0, nb, nrows, flags, diag + (size_t)(k0 / NB) * NB * NB);
-        IRWLS_LAUNCH_CHECK("chol_panel (noalloc)");
-        if (below > 0 && k0 + nb < n) {
-            dim3 g(ceil_div(n - (k0 + nb), 32), ceil_div(below, 32));
-            chol_update_kernel<<<g, 256, 0, st>>>(d_M, n, ld, k0, nb, nrows);
-            IRWLS_LAUNCH_CHECK("chol_update (noalloc)");
-        }
-    }
-    chol_store_diag_kernel<<<ceil_div(n, NB), 256, 0, st>>>(d_M, n, ld, diag);
-    IRWLS_LAUNCH_CHECK("chol_store_diag (noalloc)");
-    if (has_b) {
-        // order <= 4096: the backward sweep's vector fits the default 48 KiB
-        chol_backsolve_kernel<<<1, 256, (size_t)n * sizeof(double), st>>>(d_M, n, ld, d_x);
-        IRWLS_LAUNCH_CHECK("chol_backsolve (noalloc)");
-    }
+    // order <= 4096: the backward sweep's vector fits the default 48 KiB
+    const int rc = chol_enqueue(d_M, n, ld, d_x, flags, diag, st);
+    if (rc) return rc;
     if (d_info && (e = cudaMemcpyAsync(d_info, flags, sizeof(int), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) {
         irwls_set_error(-2, "irwls_chol_solve_noalloc: %s", cudaGetErrorString(e));
         return -2;

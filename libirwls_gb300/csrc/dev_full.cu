@@ -49,6 +49,51 @@ __device__ int block_compact(int n, Pred pred, Emit emit, int *s_scan) {
     return total;
 }
 
+// Deterministic CTA-wide sum of f(i), i < n: each thread adds its contiguous
+// chunk left to right, then a fixed tree combines the threads. The result is
+// returned to every thread.
+template <class F>
+__device__ double block_sum_ordered(int n, F f, double *red) {
+    const int ch = (n + CT - 1) / CT;
+    const int b = threadIdx.x * ch, e = min(n, b + ch);
+    double v = 0.0;
+    for (int i = b; i < e; ++i) v = __dadd_rn(v, f(i));
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = red[lane];
+        for (int o = 16; o > 0; o >>= 1) t = __dadd_rn(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    const double r = red[32];
+    __syncthreads();
+    return r;
+}
+
+template <class F, class Op>
+__device__ double block_reduce(int n, F f, Op op, double init, double *red) {
+    double v = init;
+    for (int i = threadIdx.x; i < n; i += CT) v = op(v, f(i));
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = red[lane];
+        for (int o = 16; o > 0; o >>= 1) t = op(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    const double r = red[32];
+    __syncthreads();
+    return r;
+}
+
 // --- inner IRWLS -----------------------------------------------------------
 
 // a_i and groups at entry (src/full-train.c:131-155).
@@ -125,18 +170,17 @@ __global__ void __launch_bounds__(CT) sub_update_kernel(irwls_sub_ws ws, double 
     for (int i = threadIdx.x; i < n3; i += CT) ws.bnew[ws.S3[i]] = __dmul_rn(C, ws.y[ws.S3[i]]);
     if (threadIdx.x == 0) ws.bnew[w] = ws.bsol[n1];
     __syncthreads();
+    __shared__ double red[33];
+    const double bmax = block_reduce(n1, [&](int i) { return ws.bsol[i]; },
+                                     [](double a, double b) { return b > a ? b : a; }, 0.0, red);
+    const double bmin = block_reduce(n1, [&](int i) { return ws.bsol[i]; },
+                                     [](double a, double b) { return b < a ? b : a; }, 0.0, red);
+    const double dW = block_sum_ordered(w + 1, [&](int i) {
+        const double d = __dsub_rn(ws.bnew[i], ws.beta[i]);
+        return __dmul_rn(d, d);
+    }, red);
+    const double nW = block_sum_ordered(w + 1, [&](int i) { return __dmul_rn(ws.beta[i], ws.beta[i]); }, red);
     if (threadIdx.x == 0) {
-        double bmax = 0.0, bmin = 0.0, dW = 0.0, nW = 0.0;
-        for (int i = 0; i < n1; ++i) {
-            const double b = ws.bsol[i];
-            if (b > bmax) bmax = b;
-            if (b < bmin) bmin = b;
-        }
-        for (int i = 0; i <= w; ++i) {
-            const double d = __dsub_rn(ws.bnew[i], ws.beta[i]);
-            dW = __dadd_rn(dW, __dmul_rn(d, d));
-            nW = __dadd_rn(nW, __dmul_rn(ws.beta[i], ws.beta[i]));
-        }
         ws.stats->bmax = bmax;
         ws.stats->bmin = bmin;
         ws.stats->dW = dW;
@@ -190,12 +234,10 @@ __global__ void __launch_bounds__(CT) sub_groups_kernel(irwls_sub_ws ws, double 
                                  s_scan);
     for (int i = threadIdx.x; i <= n1; i += CT) ws.G13[i] = 0.0;
     __syncthreads();
+    __shared__ double red[33];
+    const double g13 = block_sum_ordered(n3, [&](int o) { return __dmul_rn(ws.rhs[o], ws.y[ws.S3[o]]); }, red);
     if (threadIdx.x == 0) {
-        if (n3 > 0) {
-            double g = 0.0;
-            for (int o = 0; o < n3; ++o) g = __dadd_rn(g, __dmul_rn(ws.rhs[o], ws.y[ws.S3[o]]));
-            ws.G13[n1] = g;
-        }
+        if (n3 > 0) ws.G13[n1] = g13;
         ws.stats->nS1 = n1;
         ws.stats->nS3 = n3;
     }
@@ -215,10 +257,10 @@ __global__ void __launch_bounds__(CT) gin_prepare_kernel(const int *__restrict__
                                     cb[p] = bnew[SIN[o]];
                                 },
                                 s_scan);
+    __shared__ double red[33];
+    const double g = block_sum_ordered(nSIN, [&](int o) { return bnew[SIN[o]]; }, red);
     if (threadIdx.x == 0) {
         cnt[0] = n;
-        double g = 0.0;
-        for (int o = 0; o < nSIN; ++o) g = __dadd_rn(g, bnew[SIN[o]]);
         GIN[nSW] = g;
     }
 }
@@ -257,16 +299,18 @@ __global__ void __launch_bounds__(CT) apply_ws_kernel(const int *__restrict__ SW
     if (threadIdx.x == 0) cnt[0] = n;
 }
 
-__global__ void norms_kernel(const double *__restrict__ beta, const double *__restrict__ bnew, int n, double *out2) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double dW = 0.0, nW = 0.0;
-    for (int i = 0; i < n; ++i) {
+__global__ void __launch_bounds__(CT) norms_kernel(const double *__restrict__ beta, const double *__restrict__ bnew,
+                                                   int n, double *out2) {
+    __shared__ double red[33];
+    const double dW = block_sum_ordered(n, [&](int i) {
         const double d = __dsub_rn(beta[i], bnew[i]);
-        dW = __dadd_rn(dW, __dmul_rn(d, d));
-        nW = __dadd_rn(nW, __dmul_rn(beta[i], beta[i]));
+        return __dmul_rn(d, d);
+    }, red);
+    const double nW = block_sum_ordered(n, [&](int i) { return __dmul_rn(beta[i], beta[i]); }, red);
+    if (threadIdx.x == 0) {
+        out2[0] = dW;
+        out2[1] = nW;
     }
-    out2[0] = dW;
-    out2[1] = nW;
 }
 
 // Classification of every sample after an outer iteration
@@ -428,7 +472,7 @@ extern "C" int irwls_full_apply_ws(const int *d_SW, int nSW, const double *d_bt,
 }
 
 extern "C" int irwls_full_norms(const double *d_beta, const double *d_bnew, int n, double *d_out2) {
-    norms_kernel<<<1, 32, 0, irwls_stream()>>>(d_beta, d_bnew, n, d_out2);
+    norms_kernel<<<1, CT, 0, irwls_stream()>>>(d_beta, d_bnew, n, d_out2);
     IRWLS_LAUNCH_CHECK("norms");
     return 0;
 }
