@@ -50,6 +50,8 @@ def load() -> C.CDLL:
         "irwls_timer_stop": (C.c_double, []),
         "irwls_fp64_peak_tflops": (C.c_double, [C.c_int]),
         "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "irwls_tc_status": (C.c_int, []),
+        "irwls_dev_sync": (C.c_int, []),
         "storeModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
         "readModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
     }

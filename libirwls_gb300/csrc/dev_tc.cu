@@ -1,0 +1,326 @@
+// dev_tc.cu -- split-BF16 GEMM on the 5th-generation tensor cores (tcgen05,
+// sm_103a) for the precision form of the solvers.
+//
+//   C (M x N) = A (M x K) . B (N x K)^T,   A = Ahi + Alo, B = Bhi + Blo (bf16)
+//   C ~= Ahi.Bhi + Ahi.Blo + Alo.Bhi      accumulated in FP32 in tensor memory
+//
+// An FP32 value x is split as hi = bf16(x), lo = bf16(x - hi): the pair
+// carries 16 significant bits, and the dropped lo.lo product is 2^-16 of the
+// product, so each term of the dot product has a relative error of about
+// 1.5e-5; the accumulation itself is FP32.
+//
+// Operands are K-major (each row's K values contiguous) bf16 arrays in global
+// memory with leading dimension ld (a multiple of 8 elements) and K padded
+// with zeros to a multiple of 64. A CTA of 128 threads computes a 128 x BN
+// tile (BN = 64 or 128): every K stage of 64 is copied with cp.async into the
+// canonical K-major no-swizzle shared layout (8-row x 16-byte core matrices;
+// LBO = 128 B between K-neighbouring core matrices, SBO = 1024 B between row
+// groups), then thread 0 issues 4 x 3 tcgen05.mma (K = 16 each) and commits
+// them to the stage's mbarrier. Two stages are in flight. The accumulator is
+// a 128-lane x BN-column FP32 block of tensor memory; warp w reads lanes
+// 32w..32w+31 with tcgen05.ld.
+//
+// Every mbarrier wait is bounded: if it runs out, the kernel records the
+// failure in the device flag word 1, skips the rest of its work, and still
+// releases its tensor memory.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "dev_common.cuh"
+
+namespace {
+
+constexpr int TC_BM = 128, TC_BK = 64;
+constexpr int TC_THREADS = 128;
+constexpr long long TC_WAIT_LIMIT = 1LL << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    const uint32_t lbo = 128, sbo = 1024;
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // tcgen05 descriptor version; no swizzle, base offset 0
+    return d;
+}
+
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    // D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16 (bits 10-12 = 1), K-major A
+    // and B, N >> 3 at bit 17, M >> 4 at bit 24
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void *gmem, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(gmem), "r"(src_bytes));
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (long long it = 0; it < TC_WAIT_LIMIT && !done; ++it) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity));
+    }
+    return done != 0;
+}
+
+// Shared memory of one K stage: A hi/lo (128 rows) and B hi/lo (BN rows).
+template <int BN>
+struct TcStage {
+    static constexpr int A_BYTES = TC_BM * TC_BK * 2;
+    static constexpr int B_BYTES = BN * TC_BK * 2;
+    static constexpr int BYTES = 2 * A_BYTES + 2 * B_BYTES;
+};
+
+// Copies K stage `ks` of the CTA's rows into stage buffer `sb` (cp.async).
+template <int BN>
+__device__ __forceinline__ void tc_load_stage(unsigned char *sb, const __nv_bfloat16 *Ahi, const __nv_bfloat16 *Alo,
+                                              int lda, int m0, int M, const __nv_bfloat16 *Bhi,
+                                              const __nv_bfloat16 *Blo, int ldb, int n0, int N, int ks) {
+    const int k0 = ks * TC_BK;
+    const uint32_t base = smem_u32(sb);
+    // A: 2 x 128 rows x 8 chunks of 16 B
+    for (int t = threadIdx.x; t < 2 * TC_BM * 8; t += TC_THREADS) {
+        const int which = t / (TC_BM * 8), rem = t % (TC_BM * 8);
+        const int r = rem / 8, c = rem % 8;
+        const int gr = m0 + r;
+        const __nv_bfloat16 *src = (which ? Alo : Ahi) + (size_t)(gr < M ? gr : 0) * lda + k0 + c * 8;
+        const uint32_t dst = base + which * TcStage<BN>::A_BYTES + (r / 8) * 1024 + c * 128 + (r % 8) * 16;
+        cp_async16(dst, src, gr < M ? 16 : 0);
+    }
+    for (int t = threadIdx.x; t < 2 * BN * 8; t += TC_THREADS) {
+        const int which = t / (BN * 8), rem = t % (BN * 8);
+        const int r = rem / 8, c = rem % 8;
+        const int gr = n0 + r;
+        const __nv_bfloat16 *src = (which ? Blo : Bhi) + (size_t)(gr < N ? gr : 0) * ldb + k0 + c * 8;
+        const uint32_t dst =
+            base + 2 * TcStage<BN>::A_BYTES + which * TcStage<BN>::B_BYTES + (r / 8) * 1024 + c * 128 + (r % 8) * 16;
+        cp_async16(dst, src, gr < N ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+}
+
+// Issues the 12 MMAs of one K stage (thread 0 only).
+template <int BN>
+__device__ __forceinline__ void tc_mma_stage(unsigned char *sb, uint32_t tmem, bool first) {
+    const uint32_t base = smem_u32(sb);
+    const uint32_t aHi = base, aLo = base + TcStage<BN>::A_BYTES;
+    const uint32_t bHi = base + 2 * TcStage<BN>::A_BYTES, bLo = bHi + TcStage<BN>::B_BYTES;
+    constexpr uint32_t idesc = tc_idesc(TC_BM, BN);
+#pragma unroll
+    for (int kk = 0; kk < TC_BK / 16; ++kk) {
+        const uint32_t off = kk * 256;  // 16 elements = 2 core matrices along K
+        mma_bf16(tmem, tc_desc(aHi + off), tc_desc(bHi + off), idesc, (first && kk == 0) ? 0u : 1u);
+        mma_bf16(tmem, tc_desc(aHi + off), tc_desc(bLo + off), idesc, 1u);
+        mma_bf16(tmem, tc_desc(aLo + off), tc_desc(bHi + off), idesc, 1u);
+    }
+}
+
+// The main loop shared by the kernels below: accumulates the CTA's
+// 128 x BN tile over K stages [ks0, ks1) into tensor memory. Returns false if
+// a wait ran out.
+template <int BN>
+__device__ bool tc_mainloop(unsigned char *smem, uint64_t *mbar, uint32_t tmem, const __nv_bfloat16 *Ahi,
+                            const __nv_bfloat16 *Alo, int lda, int m0, int M, const __nv_bfloat16 *Bhi,
+                            const __nv_bfloat16 *Blo, int ldb, int n0, int N, int ks0, int ks1) {
+    constexpr int SB = TcStage<BN>::BYTES;
+    const int nst = ks1 - ks0;
+    bool ok = true;
+    if (nst <= 0) return true;
+    tc_load_stage<BN>(smem, Ahi, Alo, lda, m0, M, Bhi, Blo, ldb, n0, N, ks0);
+    for (int i = 0; i < nst; ++i) {
+        const int buf = i & 1;
+        if (i + 1 < nst) {
+            // the other buffer was last read by the MMAs of stage i - 1
+            if (i >= 1 && !mbar_wait(smem_u32(&mbar[buf ^ 1]), ((i - 1) >> 1) & 1)) ok = false;
+            tc_load_stage<BN>(smem + (buf ^ 1) * SB, Ahi, Alo, lda, m0, M, Bhi, Blo, ldb, n0, N, ks0 + i + 1);
+            asm volatile("cp.async.wait_group 1;\n" ::);
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::);
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::);
+        __syncthreads();
+        if (threadIdx.x == 0 && ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            tc_mma_stage<BN>(smem + buf * SB, tmem, i == 0);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&mbar[buf])));
+        }
+        __syncthreads();
+        if (!ok) break;
+    }
+    // the last stage's commit covers all earlier MMAs
+    const int last = nst - 1;
+    if (ok && !mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1)) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    return ok;
+}
+
+template <int BN>
+__device__ __forceinline__ void tc_setup(uint64_t *mbar, uint32_t *tmem_slot) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+}
+
+template <int BN>
+__device__ __forceinline__ void tc_teardown(uint32_t tmem) {
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+// Reads 8 accumulator columns of this thread's row (lane 32w + laneid).
+__device__ __forceinline__ void tc_ld8(uint32_t tmem, int c0, float *v) {
+    const int w = threadIdx.x >> 5;
+    uint32_t r[8];
+    const uint32_t addr = tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)c0;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// C tiles to global memory (FP32). grid: (ceil(N / BN), ceil(M / 128), splits);
+// split z accumulates K stages [z*per, (z+1)*per) into C + z * zstride.
+template <int BN>
+__global__ void __launch_bounds__(TC_THREADS) tc_gemm_store_kernel(const __nv_bfloat16 *Ahi, const __nv_bfloat16 *Alo,
+                                                                   int lda, int M, const __nv_bfloat16 *Bhi,
+                                                                   const __nv_bfloat16 *Blo, int ldb, int N, int kst,
+                                                                   int per, float *C, int ldc, long long zstride,
+                                                                   int lower_only, int *flags) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    const int n0 = blockIdx.x * BN, m0 = blockIdx.y * TC_BM, z = blockIdx.z;
+    if (lower_only && n0 >= m0 + TC_BM) return;  // whole tile above the diagonal
+    // align the dynamic buffer to 1024 bytes
+    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
+    tc_setup<BN>(mbar, &tmem_slot);
+    const uint32_t tmem = tmem_slot;
+    const int ks0 = z * per, ks1 = min(kst, ks0 + per);
+    const bool ok = tc_mainloop<BN>(smem, mbar, tmem, Ahi, Alo, lda, m0, M, Bhi, Blo, ldb, n0, N, ks0, ks1);
+    if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
+    const int row = m0 + threadIdx.x;
+    float *out = C + z * zstride;
+    if (ok) {
+        for (int c0 = 0; c0 < BN; c0 += 8) {
+            float v[8];
+            if (ks1 > ks0) tc_ld8(tmem, c0, v);
+            else
+                for (int j = 0; j < 8; ++j) v[j] = 0.f;
+            if (row < M)
+                for (int j = 0; j < 8; ++j)
+                    if (n0 + c0 + j < N) out[(size_t)row * ldc + n0 + c0 + j] = v[j];
+        }
+    }
+    tc_teardown<BN>(tmem);
+}
+
+// hi/lo split of an FP32 (or FP64) matrix into two bf16 matrices.
+template <class T>
+__global__ void split_bf16_kernel(const T *__restrict__ X, long long rows, int cols, int ldx, __nv_bfloat16 *hi,
+                                  __nv_bfloat16 *lo, int ldo) {
+    const long long total = rows * (long long)ldo;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long r = t / ldo;
+        const int c = (int)(t % ldo);
+        const float x = (c < cols) ? (float)X[r * ldx + c] : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        hi[t] = h;
+        lo[t] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+}
+
+}  // namespace
+
+extern "C" size_t irwls_tc_smem_bytes(int bn) {
+    return (bn == 64 ? 2 * TcStage<64>::BYTES : 2 * TcStage<128>::BYTES) + 1024;
+}
+
+// C (M x N, FP32, row-major ldc) = A B^T from split operands; `splits` K
+// partitions write to C + z * zstride. K must be a multiple of 64 (zero pad).
+extern "C" int irwls_tc_gemm(const void *Ahi, const void *Alo, int lda, int M, const void *Bhi, const void *Blo,
+                             int ldb, int N, int K, float *C, int ldc, int splits, long long zstride,
+                             int lower_only, int bn) {
+    if (K % TC_BK || lda % 8 || ldb % 8) {
+        irwls_set_error(-12, "tensor-core GEMM needs K %% 64 == 0 and leading dimensions %% 8 == 0");
+        return -12;
+    }
+    const int kst = K / TC_BK;
+    if (splits < 1) splits = 1;
+    const int per = (kst + splits - 1) / splits;
+    int *flags = irwls_dev_flags();
+    const size_t smem = irwls_tc_smem_bytes(bn);
+    if (bn == 64) {
+        cudaFuncSetAttribute(tc_gemm_store_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        dim3 grid(ceil_div(N, 64), ceil_div(M, TC_BM), splits);
+        tc_gemm_store_kernel<64><<<grid, TC_THREADS, smem, irwls_stream()>>>(
+            (const __nv_bfloat16 *)Ahi, (const __nv_bfloat16 *)Alo, lda, M, (const __nv_bfloat16 *)Bhi,
+            (const __nv_bfloat16 *)Blo, ldb, N, kst, per, C, ldc, zstride, lower_only, flags);
+    } else {
+        cudaFuncSetAttribute(tc_gemm_store_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        dim3 grid(ceil_div(N, 128), ceil_div(M, TC_BM), splits);
+        tc_gemm_store_kernel<128><<<grid, TC_THREADS, smem, irwls_stream()>>>(
+            (const __nv_bfloat16 *)Ahi, (const __nv_bfloat16 *)Alo, lda, M, (const __nv_bfloat16 *)Bhi,
+            (const __nv_bfloat16 *)Blo, ldb, N, kst, per, C, ldc, zstride, lower_only, flags);
+    }
+    IRWLS_LAUNCH_CHECK("tc_gemm");
+    return 0;
+}
+
+extern "C" int irwls_split_bf16_f64(const double *X, long long rows, int cols, int ldx, void *hi, void *lo, int ldo) {
+    const long long total = rows * (long long)ldo;
+    const int blocks = (int)((total + 255) / 256 < 65535 ? (total + 255) / 256 : 65535);
+    split_bf16_kernel<double><<<blocks, 256, 0, irwls_stream()>>>(X, rows, cols, ldx, (__nv_bfloat16 *)hi,
+                                                                  (__nv_bfloat16 *)lo, ldo);
+    IRWLS_LAUNCH_CHECK("split_bf16");
+    return 0;
+}
+
+extern "C" int irwls_split_bf16_f32(const float *X, long long rows, int cols, int ldx, void *hi, void *lo, int ldo) {
+    const long long total = rows * (long long)ldo;
+    const int blocks = (int)((total + 255) / 256 < 65535 ? (total + 255) / 256 : 65535);
+    split_bf16_kernel<float><<<blocks, 256, 0, irwls_stream()>>>(X, rows, cols, ldx, (__nv_bfloat16 *)hi,
+                                                                 (__nv_bfloat16 *)lo, ldo);
+    IRWLS_LAUNCH_CHECK("split_bf16");
+    return 0;
+}
+
+// Reads (and clears) the tensor-core wait-failure flag.
+extern "C" int irwls_tc_status(void) {
+    int flags[8];
+    cudaMemcpyAsync(flags, irwls_dev_flags(), sizeof flags, cudaMemcpyDeviceToHost, irwls_stream());
+    cudaStreamSynchronize(irwls_stream());
+    if (flags[1]) {
+        int zero = 0;
+        cudaMemcpyAsync(irwls_dev_flags() + 1, &zero, sizeof zero, cudaMemcpyHostToDevice, irwls_stream());
+        cudaStreamSynchronize(irwls_stream());
+        return 1;
+    }
+    return 0;
+}
