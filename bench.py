@@ -54,7 +54,7 @@ METRIC = "train s at ≤1e-4 rel dual-obj err: mixed/batched/learned vs plain FP
 N_ROWS, BUDGET, GAMMA, COST, SEED = 200_000, 1000, 0.1, 100.0, 20240602
 # IRWLSpar iteration count of this seeded workload, measured by the GPU run;
 # the reference arm (which runs no GPU work) extrapolates with it.
-PAR_ITERS_MEASURED = 44
+PAR_ITERS_MEASURED = 42
 
 PD = C.POINTER(C.c_double)
 PI = C.POINTER(C.c_int)
@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
     ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full"])
+    ap.add_argument("--no-mixed", action="store_true", help="skip the precision-form measurement")
     return ap.parse_args()
 
 
@@ -327,6 +328,7 @@ def run_ours(args):
         e2e = {"value": round(statistics.mean(e_times), 3), "unit": "s",
                "h2d_bytes_per_step": int((h1.value - h0.value) // args.steps),
                "d2h_bytes_per_step": int((d1.value - d0.value) // args.steps)}
+    mixed = None if args.no_mixed else measure_mixed(lib, libc, res, hd, p, args, cent, w, step_s)
     lib.irwls_resident_free(res)
 
     if rank != 0:
@@ -338,8 +340,83 @@ def run_ours(args):
             "data": "synthetic (seeded generator)",
             "config": config(args, {"par_iterations": iters.value, "active_rows_final": nact.value}),
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": base,
-            "clocks": clk}
+            "clocks": clk, "mixed": mixed}
     print(json.dumps(line), flush=True)
+
+
+def primal_objective(hd, cent, w, gamma, cost, f):
+    """Budgeted primal 1/2 w^T (K_mm + 1e-5 I) w + C sum_i max(0, 1 - y_i f_i)
+    in FP64 on the host (f = K_nm w from the library's prediction path)."""
+    import numpy as np
+
+    from libirwls_gb300 import _abi
+
+    rows, y, q = _abi.dataset_rows(hd.struct, hd.n_rows)
+    d = max(int(r[0].max()) for r in rows if len(r[0])) + 1
+    Xc = np.zeros((len(cent), d))
+    for k, c in enumerate(cent):
+        Xc[k, rows[c][0]] = rows[c][1]
+    qc = q[cent]
+    Kmm = np.exp(-gamma * (qc[:, None] + qc[None, :] - 2.0 * Xc @ Xc.T)) + 1e-5 * np.eye(len(cent))
+    return float(0.5 * w @ Kmm @ w + cost * np.maximum(0.0, 1.0 - y[:hd.l] * f).sum())
+
+
+def measure_mixed(lib, libc, res, hd, p, args, cent_plain, w_plain, plain_s):
+    """Precision form (split-BF16 tensor-core SGMA scores) on the same resident
+    workload: train seconds, centroid agreement with the plain run, relative
+    primal-objective difference and held-out accuracy change."""
+    import numpy as np
+
+    from libirwls_gb300 import _abi, synth
+
+    cent = np.zeros(args.budget, np.int32)
+    w = np.zeros(args.budget)
+    lib.irwls_set_precision(1)
+    for _ in range(args.warmup):
+        libc.srand(1)
+        lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD))
+    lib.irwls_profile_enable(1)
+    lib.irwls_profile_reset()
+    times = []
+    for _ in range(args.steps):
+        lib.irwls_l2_flush(512 << 20)
+        lib.irwls_timer_start()
+        libc.srand(1)
+        rc = lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD))
+        times.append(lib.irwls_timer_stop() / 1000.0)
+        if rc != 0:
+            raise SystemExit("mixed training failed: " + lib.irwls_last_error_message().decode())
+    ms_g, n_g = C.c_double(), C.c_longlong()
+    lib.irwls_profile_read(0, C.byref(ms_g), C.byref(n_g))
+    ms_gram, n_gram = C.c_double(), C.c_longlong()
+    lib.irwls_profile_read(1, C.byref(ms_gram), C.byref(n_gram))
+    lib.irwls_profile_enable(0)
+    lib.irwls_set_precision(0)
+    te = synth.budgeted_test_set(20000)
+    ht = _abi.build_dataset(te.indptr, te.indices, te.values, te.y, with_means=False)
+    out = {}
+    for name, c, ww in (("plain", cent_plain, w_plain), ("mixed", cent, w)):
+        c = np.ascontiguousarray(c, dtype=np.int32)
+        ww = np.ascontiguousarray(ww)
+        mdl = lib.calculateBudgetedModel(p, hd.struct, c.ctypes.data_as(PI), ww.ctypes.data_as(PD))
+        soft = np.ctypeslib.as_array(lib.softTest(hd.struct, mdl, _abi.make_predict_properties(soft=1)),
+                                     shape=(hd.l,)).copy()
+        pred = np.ctypeslib.as_array(lib.test(ht.struct, mdl, _abi.make_predict_properties(soft=0)),
+                                     shape=(ht.l,)).copy()
+        out[name] = (primal_objective(hd, c, ww, GAMMA, COST, soft), float((pred == te.y).mean()))
+    value = statistics.mean(times)
+    flops = sum(3 * 2.0 * args.rows * s * 64 for s in range(2, args.budget))
+    gemm_s = ms_g.value / 1000.0 / max(args.steps, 1)
+    return {"form": "split-BF16 tcgen05 SGMA scores (Q = K_nm L^-T formulation), FP64 factor/solves/IRWLSpar",
+            "value": round(value, 3), "unit": "s", "speedup_vs_plain_fp64": round(plain_s / value, 2),
+            "centroids_identical": int((cent == cent_plain).sum()), "budget": args.budget,
+            "primal_rel_err": abs(out["mixed"][0] - out["plain"][0]) / abs(out["plain"][0]),
+            "test_acc_plain": out["plain"][1], "test_acc_mixed": out["mixed"][1],
+            "test_acc_change": out["mixed"][1] - out["plain"][1],
+            "score_gemm": {"kernel": "sgma_tc_score_kernel",
+                           "tflops_3_products": round(flops / gemm_s / 1e12, 2) if gemm_s > 0 else None,
+                           "share_of_step": round(gemm_s / value, 4)},
+            "gram_fp64_share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / value, 4)}
 
 
 # ----------------------------------------------------------------------------

@@ -21,6 +21,18 @@ const char *irwls_last_error_message(void);
  * device every training or prediction call fails with an error. */
 int irwls_gpu_available(void);
 
+/* Arithmetic of SGMA centroid selection:
+ * IRWLS_PRECISION_FP64 (default): FP64 throughout, reference parity;
+ * IRWLS_PRECISION_MIXED: the precision form -- candidate scores computed as
+ * split-BF16 tensor-core products (FP32 accumulation) on the Nystrom
+ * features of the current centroids, with the K_mm factorization and its
+ * solves in FP64. It can pick a different centroid where two candidates
+ * score within about 1e-5 of each other; IRWLSpar stays FP64 in both forms.
+ * The environment variable IRWLS_PRECISION=mixed selects it at start-up. */
+enum { IRWLS_PRECISION_FP64 = 0, IRWLS_PRECISION_MIXED = 1 };
+void irwls_set_precision(int mode);
+int irwls_get_precision(void);
+
 /* A training set uploaded to the GPU once (rows l + 2 when the class-mean
  * rows exist), for repeated training without host-to-device traffic. */
 typedef struct irwls_resident irwls_resident;

@@ -51,6 +51,8 @@ def load() -> C.CDLL:
         "irwls_fp64_peak_tflops": (C.c_double, [C.c_int]),
         "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "irwls_tc_status": (C.c_int, []),
+        "irwls_set_precision": (None, [C.c_int]),
+        "irwls_get_precision": (C.c_int, []),
         "irwls_dev_sync": (C.c_int, []),
         "storeModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),
         "readModel": (None, [C.POINTER(_abi.Model), C.c_void_p]),

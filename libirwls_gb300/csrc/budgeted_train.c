@@ -32,9 +32,11 @@ int *randomCentroids(svm_dataset dataset, properties props) {
     return c;
 }
 
+int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properties props, int *cent_out);
+
 /* Candidate draws of every SGMA step s >= 2 (src/budgeted-train.c:157-167):
  * candidate i must carry label (i % 2) * 2 - 1. */
-static int *draw_candidates(const svm_dataset *ds, int m) {
+int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m) {
     int have_pos = 0, have_neg = 0;
     for (int i = 0; i < ds->l && !(have_pos && have_neg); i++) {
         if (ds->y[i] == 1.0) have_pos = 1;
@@ -59,7 +61,8 @@ static int *draw_candidates(const svm_dataset *ds, int m) {
 int irwls_sgma_dev(const irwls_dev_set *X, const svm_dataset *ds, properties props, int *cent_out) {
     const int m = props.size, l = ds->l;
     if (m <= 0) return 0;
-    int *cand = draw_candidates(ds, m);
+    if (irwls_get_precision() == IRWLS_PRECISION_MIXED) return irwls_sgma_mixed_dev(X, ds, props, cent_out);
+    int *cand = irwls_draw_sgma_candidates(ds, m);
     if (!cand) return -1;
     int rc = 0;
     int *d_cand = NULL, *d_cent = NULL, *d_best = NULL;
@@ -116,6 +119,10 @@ static int g_last_iters = 0, g_last_nact = 0;
 void irwls_last_run_info(int *par_iterations, int *active_rows) {
     *par_iterations = g_last_iters;
     *active_rows = g_last_nact;
+}
+void irwls_record_run_info(int par_iterations, int active_rows) {
+    g_last_iters = par_iterations;
+    g_last_nact = active_rows;
 }
 
 /* IRWLSpar on a resident dataset; weights_out gets betaBest (m values). */

@@ -30,12 +30,14 @@ constexpr int CT = 1024;
 
 // Per candidate: KNC row, forward then backward substitution with L, eta.
 // smem: v[s] (working vector), A row of the candidate (ld doubles).
+// mode 0: forward and backward substitution, eta = 1 - k.z (the reference's
+// form); mode 1 (precision form): forward substitution only, eta = 1 - |w|^2.
 __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__restrict__ cand,
                                                         const int *__restrict__ cent, int s,
                                                         const double *__restrict__ L, int ldL,
                                                         double *__restrict__ W, double *__restrict__ Z,
                                                         double *__restrict__ KN, int ldz,
-                                                        double *__restrict__ eta) {
+                                                        double *__restrict__ eta, int mode) {
     extern __shared__ double sm[];
     double *v = sm;
     double *sA = sm + s;
@@ -85,6 +87,14 @@ __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__re
     }
     for (int e = tid; e < s; e += blockDim.x) W[(size_t)c * ldz + e] = v[e];
     __syncthreads();
+    if (mode == 1) {
+        if (tid == 0) {
+            double val = 1.0;
+            for (int e = 0; e < s; ++e) val = __dsub_rn(val, __dmul_rn(v[e], v[e]));
+            eta[c] = val;
+        }
+        return;
+    }
     // backward: L^T z = w
     for (int b = nblk - 1; b >= 0; --b) {
         const int r0 = b * 32, r1 = min(s, r0 + 32);
@@ -544,7 +554,7 @@ extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand
     }
     if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     sgma_cand_kernel<<<NCAND, 256, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_L, ldL, d_W, d_Z, d_KN, ldz,
-                                                          d_eta);
+                                                          d_eta, 0);
     IRWLS_LAUNCH_CHECK("sgma_cand");
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
     sgma_gemm_kernel<<<sgma_gemm_grid(l), 256, 0, irwls_stream()>>>(kview(X), l, d_cand, s, d_KSC, d_Z, ldz,
@@ -555,6 +565,40 @@ extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand
 }
 
 extern "C" int irwls_sgma_partials(int l) { return sgma_gemm_grid(l); }
+
+// Precision form: candidate kernel rows, forward substitution, eta = 1 - |w|^2.
+extern "C" int irwls_sgma_cand_forward(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s,
+                                       const double *d_L, int ldL, double *d_W, double *d_KN, int ldz, double *d_eta) {
+    const size_t smem = ((size_t)s + X->ld) * sizeof(double);
+    if (smem > 200 * 1024) {
+        irwls_set_error(-7, "SGMA budget %d with feature width %d exceeds the substitution tile", s, X->width);
+        return -7;
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sgma_cand_kernel<<<NCAND, 256, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_L, ldL, d_W, nullptr, d_KN,
+                                                          ldz, d_eta, 1);
+    IRWLS_LAUNCH_CHECK("sgma_cand_forward");
+    return 0;
+}
+
+extern "C" int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, const int *d_cand, int s,
+                                   int *d_cent, int *d_best, double *d_bestval) {
+    sgma_select_kernel<<<1, NCAND, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval);
+    IRWLS_LAUNCH_CHECK("sgma_select");
+    return 0;
+}
+
+// Row s of the SGMA factor only (no K_nm column).
+extern "C" int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W,
+                                 int ldz, double *d_L, int ldL) {
+    const size_t smem = (size_t)X->ld * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL);
+    IRWLS_LAUNCH_CHECK("sgma_factor");
+    return 0;
+}
+
+
 
 extern "C" int irwls_sgma_select(const double *d_part, int l, const double *d_eta, const int *d_cand, int s,
                                  int *d_cent, int *d_best, double *d_bestval) {

@@ -26,6 +26,8 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "dev_common.cuh"
 
 namespace {
@@ -149,19 +151,20 @@ __device__ bool tc_mainloop(unsigned char *smem, uint64_t *mbar, uint32_t tmem, 
             asm volatile("cp.async.wait_group 0;\n" ::);
         }
         asm volatile("fence.proxy.async.shared::cta;\n" ::);
-        __syncthreads();
-        if (threadIdx.x == 0 && ok) {
+        ok = __syncthreads_and(ok);  // CTA-uniform: every thread takes the same branch below
+        if (!ok) break;
+        if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
             tc_mma_stage<BN>(smem + buf * SB, tmem, i == 0);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 smem_u32(&mbar[buf])));
         }
-        __syncthreads();
-        if (!ok) break;
     }
+    asm volatile("cp.async.wait_group 0;\n" ::);
     // the last stage's commit covers all earlier MMAs
     const int last = nst - 1;
     if (ok && !mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1)) ok = false;
+    ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
     return ok;
 }
@@ -322,5 +325,154 @@ extern "C" int irwls_tc_status(void) {
         cudaStreamSynchronize(irwls_stream());
         return 1;
     }
+    return 0;
+}
+
+// ===========================================================================
+// Precision form of SGMA.
+//
+// SGMA works on Q = K_nm L^-T (row i = the Nystrom features of sample i, all
+// of norm <= 1) instead of K_nm: for a candidate c with w = L^-1 k_C(c),
+// K_nm z = Q w, eta = 1 - |w|^2, and the residual is r = Q w - k(c, .). Q and
+// w are bounded, which is what makes the split-BF16 product accurate here
+// (the reference's K_nm z form multiplies K_nm by z = K_CC^-1 k_C, whose
+// entries are large and cancel). Q is kept in FP32 (master copy) and as bf16
+// hi/lo for the tensor cores; a new centroid adds the column
+// q_s = (k(., c_s) - Q l2) / L3 with l2 = L^-1 k_C(c_s), L3 the new pivot.
+// ===========================================================================
+
+namespace {
+
+// FP32 kernel entry: A row held densely (FP32), B row from the device set.
+__device__ __forceinline__ float kentry_f32(const KView &B, const float *a, float qa, int jb) {
+    if (B.mode == IRWLS_K_RAW_RBF) {
+        const double *b = B.X + (size_t)jb * B.ld;
+        float s = 0.f;
+        for (int t = 0; t < B.width; ++t) {
+            const float d = a[t] - (float)b[t];
+            s = fmaf(d, d, s);
+        }
+        return __expf((float)B.ng * s);
+    }
+    float s = 0.f;
+    const int p0 = B.rp[jb], p1 = B.rp[jb + 1];
+    for (int p = p0; p < p1; ++p) s = fmaf((float)B.cv[p], a[B.ci[p]], s);
+    if (B.mode == IRWLS_K_LINEAR) return s;
+    const float d2 = fmaxf((float)(qa + B.q[jb]) - 2.f * s, 0.f);
+    return __expf((float)B.ng * d2);
+}
+
+// SGMA scores in the precision form: R = Q W^T on the tensor cores (rows of
+// the CTA's 128-row tile x 64 candidates), r = R - k(cand, row) in FP32, and
+// the per-candidate sums of r^2 over the tile (in FP64) to part[tile][64].
+__global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KView X, int l, const int *__restrict__ cand,
+                                                                   const __nv_bfloat16 *Qhi, const __nv_bfloat16 *Qlo,
+                                                                   int ldq, const __nv_bfloat16 *Whi,
+                                                                   const __nv_bfloat16 *Wlo, int kst,
+                                                                   double *__restrict__ part, int *flags) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ float qc[64];
+    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
+    float *ca = (float *)(smem + 2 * TcStage<64>::BYTES);  // 64 candidate rows, FP32, X.ld each
+    const int m0 = blockIdx.x * TC_BM;
+    for (int t = threadIdx.x; t < 64 * X.ld; t += TC_THREADS) {
+        const int c = t / X.ld, k = t % X.ld;
+        ca[t] = (float)X.X[(size_t)cand[c] * X.ld + k];
+    }
+    if (threadIdx.x < 64) qc[threadIdx.x] = (float)X.q[cand[threadIdx.x]];
+    tc_setup<64>(mbar, &tmem_slot);
+    const uint32_t tmem = tmem_slot;
+    const bool ok = tc_mainloop<64>(smem, mbar, tmem, Qhi, Qlo, ldq, m0, l, Whi, Wlo, ldq, 0, 64, 0, kst);
+    if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
+    // residual squares of this thread's row into the (now free) stage buffer
+    float *sr = (float *)smem;  // [128][65]
+    const int row = m0 + threadIdx.x;
+    for (int c0 = 0; c0 < 64; c0 += 8) {
+        float v[8];
+        if (ok) tc_ld8(tmem, c0, v);
+        else
+            for (int j = 0; j < 8; ++j) v[j] = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = c0 + j;
+            float r2 = 0.f;
+            if (row < l && ok) {
+                const float r = v[j] - kentry_f32(X, ca + (size_t)c * X.ld, qc[c], row);
+                r2 = r * r;
+            }
+            sr[threadIdx.x * 65 + c] = r2;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        double acc = 0.0;
+        for (int r = 0; r < TC_BM; ++r) acc += (double)sr[r * 65 + threadIdx.x];
+        part[(size_t)blockIdx.x * 64 + threadIdx.x] = acc;
+    }
+    tc_teardown<64>(tmem);
+}
+
+// New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, one warp
+// per row; the centroid row is staged in shared memory for the FP64 kernel
+// entry.
+__global__ void q_column_kernel(KView X, int l, const int *__restrict__ cent, int s, const double *__restrict__ L,
+                                int ldL, float *Qf, __nv_bfloat16 *Qhi, __nv_bfloat16 *Qlo, int ldq) {
+    extern __shared__ double sc[];
+    const int gc = cent[s];
+    for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sc[t] = X.X[(size_t)gc * X.ld + t];
+    __syncthreads();
+    const double qa = X.q[gc];
+    const double *l2 = L + (size_t)s * ldL;  // row s of L: l2 then the pivot L3
+    const double L3 = l2[s];
+    const int lane = threadIdx.x & 31;
+    const int warps = blockDim.x >> 5;
+    for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += gridDim.x * warps) {
+        const float *qrow = Qf + (size_t)i * ldq;
+        float acc = 0.f;
+        for (int j = lane; j < s; j += 32) acc = fmaf(qrow[j], (float)l2[j], acc);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double kv = kentry(X, sc, qa, i);
+            const float q = (float)((kv - (double)acc) / L3);
+            Qf[(size_t)i * ldq + s] = q;
+            const __nv_bfloat16 h = __float2bfloat16_rn(q);
+            Qhi[(size_t)i * ldq + s] = h;
+            Qlo[(size_t)i * ldq + s] = __float2bfloat16_rn(q - __bfloat162float(h));
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, int l, const int *d_cand, const void *Qhi, const void *Qlo,
+                                   int ldq, const void *Whi, const void *Wlo, int s, double *d_part) {
+    const int kst = (s + TC_BK - 1) / TC_BK;
+    const size_t smem = 2 * TcStage<64>::BYTES + 1024 + (size_t)64 * X->ld * sizeof(float);
+    if (smem > 220 * 1024) {
+        irwls_set_error(-12, "feature width %d too wide for the precision-form SGMA tile", X->width);
+        return -12;
+    }
+    cudaFuncSetAttribute(sgma_tc_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
+    sgma_tc_score_kernel<<<ceil_div(l, TC_BM), TC_THREADS, smem, irwls_stream()>>>(
+        kview(X), l, d_cand, (const __nv_bfloat16 *)Qhi, (const __nv_bfloat16 *)Qlo, ldq,
+        (const __nv_bfloat16 *)Whi, (const __nv_bfloat16 *)Wlo, kst, d_part, irwls_dev_flags());
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_GEMM);
+    IRWLS_LAUNCH_CHECK("sgma_tc_score");
+    return 0;
+}
+
+extern "C" int irwls_sgma_tc_partials(int l) { return ceil_div(l, TC_BM); }
+
+extern "C" int irwls_q_column(const irwls_dev_set *X, int l, const int *d_cent, int s, const double *d_L, int ldL,
+                              float *Qf, void *Qhi, void *Qlo, int ldq) {
+    const size_t smem = (size_t)X->ld * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int blocks = std::min(ceil_div(l, 8), 16 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
+    q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kview(X), l, d_cent, s, d_L, ldL, Qf,
+                                                            (__nv_bfloat16 *)Qhi, (__nv_bfloat16 *)Qlo, ldq);
+    IRWLS_LAUNCH_CHECK("q_column");
     return 0;
 }

@@ -1,0 +1,128 @@
+/*
+ * mixed.c -- host orchestration of the precision form of budgeted IRWLS
+ * (same loops, exit tests and random draws as budgeted_train.c):
+ *   SGMA: candidate kernel rows, factor L of K_CC + jitter and its forward
+ *         solves in FP64; scores from Q w on the tensor cores in split BF16
+ *         (Q = K_nm L^-T, kept in FP32 and as bf16 hi/lo), candidate kernel
+ *         rows of the score epilogue in FP32.
+ *   IRWLSpar stays FP64: its system K1 = KC + K_nm^T D_a K_nm carries weights
+ *   up to 1e4 against a 1e-5 jitter, so its condition number reaches ~1e13,
+ *   and a Gram accumulated from 16-bit-mantissa products (relative error
+ *   ~1e-5) turns it indefinite; measured on 200000 rows and 1000 centroids,
+ *   that variant's primal objective was off by a factor of 4e6.
+ * Selected with irwls_set_precision(IRWLS_PRECISION_MIXED) or the
+ * environment variable IRWLS_PRECISION=mixed; plain FP64 is the default.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "irwls_dev.h"
+#include "irwls_gpu.h"
+
+int irwls_sgma_cand_forward(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s, const double *d_L,
+                            int ldL, double *d_W, double *d_KN, int ldz, double *d_eta);
+int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, const int *d_cand, int s, int *d_cent,
+                        int *d_best, double *d_bestval);
+int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W, int ldz,
+                      double *d_L, int ldL);
+int irwls_sgma_tc_score(const irwls_dev_set *X, int l, const int *d_cand, const void *Qhi, const void *Qlo, int ldq,
+                        const void *Whi, const void *Wlo, int s, double *d_part);
+int irwls_sgma_tc_partials(int l);
+int irwls_q_column(const irwls_dev_set *X, int l, const int *d_cent, int s, const double *d_L, int ldL, float *Qf,
+                   void *Qhi, void *Qlo, int ldq);
+int irwls_split_bf16_f64(const double *X, long long rows, int cols, int ldx, void *hi, void *lo, int ldo);
+int irwls_tc_status(void);
+int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m);
+void irwls_record_run_info(int par_iterations, int active_rows);
+
+static int g_precision = -1;
+
+void irwls_set_precision(int mode) { g_precision = mode; }
+
+int irwls_get_precision(void) {
+    if (g_precision < 0) {
+        const char *e = getenv("IRWLS_PRECISION");
+        g_precision = (e && strcmp(e, "mixed") == 0) ? IRWLS_PRECISION_MIXED : IRWLS_PRECISION_FP64;
+    }
+    return g_precision;
+}
+
+static int round_up(int x, int a) { return (x + a - 1) / a * a; }
+
+int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properties props, int *cent_out) {
+    const int m = props.size, l = ds->l;
+    if (m <= 0) return 0;
+    int *cand = irwls_draw_sgma_candidates(ds, m);
+    if (!cand) return -1;
+    const int ldq = round_up(m, 64), ldL = m, ldz = m;
+    const int nblk = irwls_sgma_tc_partials(l);
+    int rc = 0;
+    int *d_cand = NULL, *d_cent = NULL, *d_best = NULL;
+    double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_part = NULL, *d_val = NULL;
+    float *Qf = NULL;
+    void *Qhi = NULL, *Qlo = NULL, *Whi = NULL, *Wlo = NULL;
+    rc |= irwls_dev_malloc((void **)&d_cand, (size_t)m * 64 * sizeof(int));
+    rc |= irwls_dev_malloc((void **)&d_cent, (size_t)m * sizeof(int));
+    rc |= irwls_dev_malloc((void **)&d_best, sizeof(int));
+    rc |= irwls_dev_malloc((void **)&d_L, (size_t)m * ldL * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_W, (size_t)64 * ldz * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_KN, (size_t)64 * ldz * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_eta, 64 * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_part, (size_t)nblk * 64 * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_val, (size_t)m * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&Qf, (size_t)l * ldq * sizeof(float));
+    rc |= irwls_dev_malloc(&Qhi, (size_t)l * ldq * 2);
+    rc |= irwls_dev_malloc(&Qlo, (size_t)l * ldq * 2);
+    rc |= irwls_dev_malloc(&Whi, (size_t)64 * ldq * 2);
+    rc |= irwls_dev_malloc(&Wlo, (size_t)64 * ldq * 2);
+    if (rc) goto done;
+    {
+        int first[2] = {l, l + 1};
+        rc |= irwls_dev_h2d(d_cand, cand, (size_t)m * 64 * sizeof(int));
+        rc |= irwls_dev_h2d(d_cent, first, (m > 1 ? 2 : 1) * sizeof(int));
+        rc |= irwls_dev_memset(d_L, 0, (size_t)m * ldL * sizeof(double));
+        rc |= irwls_dev_memset(d_W, 0, (size_t)64 * ldz * sizeof(double));
+        rc |= irwls_dev_memset(Qf, 0, (size_t)l * ldq * sizeof(float));
+        rc |= irwls_dev_memset(Qhi, 0, (size_t)l * ldq * 2);
+        rc |= irwls_dev_memset(Qlo, 0, (size_t)l * ldq * 2);
+        rc |= irwls_sgma_factor(X, 0, d_cent, d_best, d_W, ldz, d_L, ldL);
+        rc |= irwls_q_column(X, l, d_cent, 0, d_L, ldL, Qf, Qhi, Qlo, ldq);
+        if (m > 1) {
+            rc |= irwls_sgma_factor(X, 1, d_cent, d_best, d_W, ldz, d_L, ldL);
+            rc |= irwls_q_column(X, l, d_cent, 1, d_L, ldL, Qf, Qhi, Qlo, ldq);
+        }
+        for (int s = 2; s < m && !rc; s++) {
+            rc |= irwls_sgma_cand_forward(X, d_cand + (size_t)s * 64, d_cent, s, d_L, ldL, d_W, d_KN, ldz, d_eta);
+            rc |= irwls_split_bf16_f64(d_W, 64, s, ldz, Whi, Wlo, ldq);
+            rc |= irwls_sgma_tc_score(X, l, d_cand + (size_t)s * 64, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
+            rc |= irwls_sgma_select_n(d_part, nblk, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
+            rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
+            rc |= irwls_q_column(X, l, d_cent, s, d_L, ldL, Qf, Qhi, Qlo, ldq);
+        }
+        if (rc) goto done;
+        double *val = (double *)malloc((size_t)m * sizeof(double));
+        rc |= irwls_dev_d2h(cent_out, d_cent, (size_t)m * sizeof(int));
+        rc |= irwls_dev_d2h(val, d_val, (size_t)m * sizeof(double));
+        rc |= irwls_dev_sync();
+        if (!rc && irwls_tc_status()) {
+            irwls_set_error(-13, "a tensor-core pipeline wait ran out");
+            rc = -13;
+        }
+        if (!rc && props.verbose == 1) {
+            for (int s = 0; s < m; s++) {
+                if (s == 0) printf("Best Error Descent %f, Average of positive data is centroid %d\n", 1.0, s);
+                if (s == 1) printf("Best Error Descent %f, Average of negative data is centroid %d\n", 1.0, s);
+                if (s > 1) printf("Best Error Descent %f, Data with index %d is centroid %d\n", val[s], cent_out[s], s);
+            }
+        }
+        free(val);
+    }
+done:
+    free(cand);
+    {
+        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qhi, Qlo, Whi, Wlo};
+        for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
+    }
+    return rc ? -1 : 0;
+}

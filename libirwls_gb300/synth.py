@@ -64,10 +64,13 @@ def full_dense_workload(n_train=4000, n_test=1000, d=20, seed=20240601):
     return tr, te
 
 
-def mixed_onehot(n: int, seed: int, n_cont=10, groups=(4, 40), hidden=16, flip=0.05):
+def mixed_onehot(n: int, seed: int, n_cont=10, groups=(4, 40), hidden=16, flip=0.05, label_seed=None):
     """n_cont N(0,1) features plus one-hot groups; labels from the sign of a
     seeded random 2-layer tanh network, with a fraction ``flip`` flipped.
-    Zeros are omitted, so the reader flags the set as sparse."""
+    Zeros are omitted, so the reader flags the set as sparse. The network is
+    drawn from ``label_seed`` when given (so that a test set drawn with
+    another ``seed`` shares the training set's labelling function), else from
+    the same stream as the rows."""
     rng = np.random.default_rng(seed)
     d = n_cont + sum(groups)
     X = np.zeros((n, d))
@@ -76,17 +79,23 @@ def mixed_onehot(n: int, seed: int, n_cont=10, groups=(4, 40), hidden=16, flip=0
     for g in groups:
         X[np.arange(n), off + rng.integers(0, g, n)] = 1.0
         off += g
-    W1 = rng.standard_normal((d, hidden)) / np.sqrt(d)
-    w2 = rng.standard_normal(hidden)
+    frng = rng if label_seed is None else np.random.default_rng(label_seed)
+    W1 = frng.standard_normal((d, hidden)) / np.sqrt(d)
+    w2 = frng.standard_normal(hidden)
     s = np.tanh(X @ W1 * 2.0) @ w2
-    y = np.where(s >= np.median(s), 1.0, -1.0)
+    y = np.where(s >= (np.median(s) if label_seed is None else 0.0), 1.0, -1.0)
     y = np.where(rng.random(n) < flip, -y, y)
     return from_dense(X, y, keep_zeros=False)
 
 
-def budgeted_workload(n=200_000, seed=20240602):
+def budgeted_workload(n=200_000, seed=20240602, label_seed=20240603):
     """Budgeted-IRWLS workload: 10 continuous + one-hot(4) + one-hot(40)."""
-    return mixed_onehot(n, seed)
+    return mixed_onehot(n, seed, label_seed=label_seed)
+
+
+def budgeted_test_set(n=20_000, seed=20240604, label_seed=20240603):
+    """Held-out rows labelled by the same network as budgeted_workload()."""
+    return mixed_onehot(n, seed, label_seed=label_seed)
 
 
 def write_libsvm(path: str, data: Sparse, labeled: bool = True) -> None:
