@@ -303,7 +303,9 @@ def run_ours(args):
                                "MEASURED_PEAKS.json has no FP64 figure",
                 "launches_per_step": int(n_g.value // max(args.steps, 1)),
                 "share_of_step": round(gemm_s / step_s, 4),
-                "gram_share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / step_s, 4)}
+                "gram_share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / step_s, 4),
+                "gram_tflops": gram_rate(lib, ms_gram.value, args.steps),
+                "breakdown_s": profile_breakdown(lib, args.steps)}
 
     # end to end through the reference-facing API with host buffers
     e2e = None
@@ -342,6 +344,28 @@ def run_ours(args):
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": base,
             "clocks": clk, "mixed": mixed}
     print(json.dumps(line), flush=True)
+
+
+PROFILE_SLOTS = {"sgma_scores": 0, "sgma_candidate_solves": 5, "sgma_select_and_factor": 6, "irwls_gram": 1,
+                 "irwls_cholesky": 3}
+
+
+def profile_breakdown(lib, steps):
+    """Seconds per step of each profiled stage (CUDA events on the library's
+    stream around the stage's launches)."""
+    out = {}
+    for name, slot in PROFILE_SLOTS.items():
+        ms, n = C.c_double(), C.c_longlong()
+        lib.irwls_profile_read(slot, C.byref(ms), C.byref(n))
+        out[name] = round(ms.value / 1000.0 / max(steps, 1), 4)
+    return out
+
+
+def gram_rate(lib, ms_total, steps):
+    """Algorithmic TFLOP/s of the IRWLSpar Gram updates of the last training
+    (active_rows * (m + 1) * m per iteration over the profiled kernel time)."""
+    per_step_s = ms_total / 1000.0 / max(steps, 1)
+    return round(lib.irwls_last_gram_flops() / per_step_s / 1e12, 3) if per_step_s > 0 else None
 
 
 def primal_objective(hd, cent, w, gamma, cost, f):
@@ -390,6 +414,7 @@ def measure_mixed(lib, libc, res, hd, p, args, cent_plain, w_plain, plain_s):
     lib.irwls_profile_read(0, C.byref(ms_g), C.byref(n_g))
     ms_gram, n_gram = C.c_double(), C.c_longlong()
     lib.irwls_profile_read(1, C.byref(ms_gram), C.byref(n_gram))
+    breakdown = profile_breakdown(lib, args.steps)
     lib.irwls_profile_enable(0)
     lib.irwls_set_precision(0)
     te = synth.budgeted_test_set(20000)
@@ -407,7 +432,8 @@ def measure_mixed(lib, libc, res, hd, p, args, cent_plain, w_plain, plain_s):
     value = statistics.mean(times)
     flops = sum(3 * 2.0 * args.rows * s * 64 for s in range(2, args.budget))
     gemm_s = ms_g.value / 1000.0 / max(args.steps, 1)
-    return {"form": "split-BF16 tcgen05 SGMA scores (Q = K_nm L^-T formulation), FP64 factor/solves/IRWLSpar",
+    return {"form": "SGMA scores in split BF16 on tcgen05 (Q = K_nm L^-T formulation); IRWLSpar Gram in "
+                    "double-float FP32 pairs; FP64 factors, solves, residuals and convergence tests",
             "value": round(value, 3), "unit": "s", "speedup_vs_plain_fp64": round(plain_s / value, 2),
             "centroids_identical": int((cent == cent_plain).sum()), "budget": args.budget,
             "primal_rel_err": abs(out["mixed"][0] - out["plain"][0]) / abs(out["plain"][0]),
@@ -416,7 +442,10 @@ def measure_mixed(lib, libc, res, hd, p, args, cent_plain, w_plain, plain_s):
             "score_gemm": {"kernel": "sgma_tc_score_kernel",
                            "tflops_3_products": round(flops / gemm_s / 1e12, 2) if gemm_s > 0 else None,
                            "share_of_step": round(gemm_s / value, 4)},
-            "gram_fp64_share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / value, 4)}
+            "breakdown_s": breakdown,
+            "gram": {"kernel": "df_pack_kernel + gram_df_kernel",
+                     "tflops_fp64_equivalent": gram_rate(lib, ms_gram.value, args.steps),
+                     "share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / value, 4)}}
 
 
 # ----------------------------------------------------------------------------

@@ -50,6 +50,7 @@ def load() -> C.CDLL:
         "irwls_timer_stop": (C.c_double, []),
         "irwls_fp64_peak_tflops": (C.c_double, [C.c_int]),
         "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "irwls_last_gram_flops": (C.c_double, []),
         "irwls_tc_status": (C.c_int, []),
         "irwls_set_precision": (None, [C.c_int]),
         "irwls_get_precision": (C.c_int, []),

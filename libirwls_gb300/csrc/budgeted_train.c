@@ -91,8 +91,10 @@ int irwls_sgma_dev(const irwls_dev_set *X, const svm_dataset *ds, properties pro
         for (int s = 2; s < m && !rc; s++) {
             rc |= irwls_sgma_score(X, l, d_cand + (size_t)s * 64, 64, d_cent, s, d_L, ldL, d_KSC, d_W, d_Z, d_KN,
                                    ldz, d_eta, d_part);
+            irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
             rc |= irwls_sgma_select(d_part, l, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
             rc |= irwls_sgma_extend(X, l, s, d_cent, d_best, d_W, ldz, d_L, ldL, d_KSC);
+            irwls_prof_end(IRWLS_PROF_SGMA_UPDATE);
         }
         if (rc) goto done;
         double *val = (double *)malloc((size_t)m * sizeof(double));
@@ -116,10 +118,12 @@ done:
 }
 
 static int g_last_iters = 0, g_last_nact = 0;
+static double g_gram_flops = 0.0;
 void irwls_last_run_info(int *par_iterations, int *active_rows) {
     *par_iterations = g_last_iters;
     *active_rows = g_last_nact;
 }
+double irwls_last_gram_flops(void) { return g_gram_flops; }
 void irwls_record_run_info(int par_iterations, int active_rows) {
     g_last_iters = par_iterations;
     g_last_nact = active_rows;
@@ -143,6 +147,18 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
     if (P > l / 512) P = l / 512;
     if (P < 1) P = 1;
     if (P > 64) P = 64;
+    /* precision form: double-float Gram over FP32 pairs of the active rows;
+       finer split-K (chunks of at least 256 rows) since each product costs
+       twelve FP32 instructions instead of one FP64 FMA */
+    const int mixed = irwls_get_precision() == IRWLS_PRECISION_MIXED;
+    void *d_A = NULL;
+    if (mixed) {
+        P = (24 * sms + tiles - 1) / tiles;
+        if (P > l / 256) P = l / 256;
+        if (P < 1) P = 1;
+        if (P > 128) P = 128;
+        rc |= irwls_dev_malloc(&d_A, (size_t)l * irwls_par_df_lda(m) * 2 * sizeof(float));
+    }
     rc |= irwls_dev_malloc((void **)&d_idx, (size_t)m * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_act, (size_t)l * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_nact, sizeof(int));
@@ -171,10 +187,14 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
     if (rc) goto done;
     {
         int iter = 0, since_best = 0, nact = l;
+        g_gram_flops = 0.0;
         double dW = 1e9, nW = 1.0, old = 0.0, best = 1e9;
         while ((iter < 500) && (dW / nW > 1e-6) && (since_best < 5)) {
             /* K1 = KC + KSCA^T KSCA (lower) and K2 = KSCA^T Day in row m (:401-416) */
-            if (irwls_par_gram(d_KSC, m, d_act, nact, d_sd, d_day, d_KC, d_K1, ld, d_part, P)) goto fail;
+            if (mixed ? irwls_par_gram_df(d_KSC, m, d_act, nact, d_sd, d_day, d_KC, d_K1, ld, d_part, P, d_A)
+                      : irwls_par_gram(d_KSC, m, d_act, nact, d_sd, d_day, d_KC, d_K1, ld, d_part, P))
+                goto fail;
+            g_gram_flops += (double)nact * (m + 1) * m;
             if (irwls_dev_chol_solve(d_K1, m, ld, NULL, d_bnew)) goto fail;
             if (irwls_par_delta(d_bnew, d_beta, m, d_nrm)) goto fail;
             if (irwls_par_residual(d_KSC, l, m, d_beta, X->y, C, M, d_e, d_Da)) goto fail;
@@ -207,7 +227,7 @@ fail:
 done:
     {
         void *bufs[] = {d_idx, d_act, d_nact, d_KC, d_KSC, d_K1, d_part, d_sd, d_day, d_e, d_Da, d_beta, d_bnew,
-                        d_bbest, d_nrm};
+                        d_bbest, d_nrm, d_A};
         for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
         irwls_dev_host_free(h_nact);
         irwls_dev_host_free(h_nrm);

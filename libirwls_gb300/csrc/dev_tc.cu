@@ -343,29 +343,84 @@ extern "C" int irwls_tc_status(void) {
 
 namespace {
 
-// FP32 kernel entry: A row held densely (FP32), B row from the device set.
-__device__ __forceinline__ float kentry_f32(const KView &B, const float *a, float qa, int jb) {
+// FP32 mirror of a device set (dense rows, CSR values, norms), made once per
+// precision-form run so that no kernel of that form converts from FP64 per
+// entry: conversions and adds in FP64 run on this part's narrow FP64 pipe.
+struct KViewF {
+    int mode, width, ld;
+    float ng;
+    const float *__restrict__ X;
+    const int *__restrict__ rp;
+    const int *__restrict__ ci;
+    const float *__restrict__ cv;
+    const float *__restrict__ q;
+};
+
+struct F32Mirror {
+    float *X, *cv, *q;
+};
+
+static inline KViewF kviewf(const irwls_dev_set *s, const F32Mirror *f) {
+    KViewF v;
+    v.mode = s->mode;
+    v.width = s->width;
+    v.ld = s->ld;
+    v.ng = (float)s->neg_gamma;
+    v.X = f->X;
+    v.rp = s->rp;
+    v.ci = s->ci;
+    v.cv = f->cv;
+    v.q = f->q;
+    return v;
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ in, long long n, float *__restrict__ out) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[t] = __double2float_rn(in[t]);
+}
+
+// Kernel values of one row of the set against 8 A rows held densely in FP32
+// (A row j at a + j * lda), each entry of the row read once.
+__device__ __forceinline__ void kentry8_f32(const KViewF &B, const float *a, int lda, const float *qa, int jb,
+                                            float out[8]) {
+    float acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
     if (B.mode == IRWLS_K_RAW_RBF) {
-        const double *b = B.X + (size_t)jb * B.ld;
-        float s = 0.f;
+        const float *b = B.X + (size_t)jb * B.ld;
         for (int t = 0; t < B.width; ++t) {
-            const float d = a[t] - (float)b[t];
-            s = fmaf(d, d, s);
+            const float bt = b[t];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float d = a[j * lda + t] - bt;
+                acc[j] = fmaf(d, d, acc[j]);
+            }
         }
-        return __expf((float)B.ng * s);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * acc[j]);
+        return;
     }
-    float s = 0.f;
     const int p0 = B.rp[jb], p1 = B.rp[jb + 1];
-    for (int p = p0; p < p1; ++p) s = fmaf((float)B.cv[p], a[B.ci[p]], s);
-    if (B.mode == IRWLS_K_LINEAR) return s;
-    const float d2 = fmaxf((float)(qa + B.q[jb]) - 2.f * s, 0.f);
-    return __expf((float)B.ng * d2);
+    for (int p = p0; p < p1; ++p) {
+        const float v = B.cv[p];
+        const int c = B.ci[p];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, a[j * lda + c], acc[j]);
+    }
+    if (B.mode == IRWLS_K_LINEAR) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out[j] = acc[j];
+        return;
+    }
+    const float qb = B.q[jb];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
 }
 
 // SGMA scores in the precision form: R = Q W^T on the tensor cores (rows of
 // the CTA's 128-row tile x 64 candidates), r = R - k(cand, row) in FP32, and
 // the per-candidate sums of r^2 over the tile (in FP64) to part[tile][64].
-__global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KView X, int l, const int *__restrict__ cand,
+__global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int l, const int *__restrict__ cand,
                                                                    const __nv_bfloat16 *Qhi, const __nv_bfloat16 *Qlo,
                                                                    int ldq, const __nv_bfloat16 *Whi,
                                                                    const __nv_bfloat16 *Wlo, int kst,
@@ -379,9 +434,9 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KView X, int 
     const int m0 = blockIdx.x * TC_BM;
     for (int t = threadIdx.x; t < 64 * X.ld; t += TC_THREADS) {
         const int c = t / X.ld, k = t % X.ld;
-        ca[t] = (float)X.X[(size_t)cand[c] * X.ld + k];
+        ca[t] = X.X[(size_t)cand[c] * X.ld + k];
     }
-    if (threadIdx.x < 64) qc[threadIdx.x] = (float)X.q[cand[threadIdx.x]];
+    if (threadIdx.x < 64) qc[threadIdx.x] = X.q[cand[threadIdx.x]];
     tc_setup<64>(mbar, &tmem_slot);
     const uint32_t tmem = tmem_slot;
     const bool ok = tc_mainloop<64>(smem, mbar, tmem, Qhi, Qlo, ldq, m0, l, Whi, Wlo, ldq, 0, 64, 0, kst);
@@ -390,19 +445,19 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KView X, int 
     float *sr = (float *)smem;  // [128][65]
     const int row = m0 + threadIdx.x;
     for (int c0 = 0; c0 < 64; c0 += 8) {
-        float v[8];
+        float v[8], kv[8];
         if (ok) tc_ld8(tmem, c0, v);
         else
             for (int j = 0; j < 8; ++j) v[j] = 0.f;
+        if (row < l && ok) kentry8_f32(X, ca + (size_t)c0 * X.ld, X.ld, qc + c0, row, kv);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int c = c0 + j;
             float r2 = 0.f;
             if (row < l && ok) {
-                const float r = v[j] - kentry_f32(X, ca + (size_t)c * X.ld, qc[c], row);
+                const float r = v[j] - kv[j];
                 r2 = r * r;
             }
-            sr[threadIdx.x * 65 + c] = r2;
+            sr[threadIdx.x * 65 + c0 + j] = r2;
         }
     }
     __syncthreads();
@@ -415,27 +470,55 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KView X, int 
 }
 
 // New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, one warp
-// per row; the centroid row is staged in shared memory for the FP64 kernel
-// entry.
-__global__ void q_column_kernel(KView X, int l, const int *__restrict__ cent, int s, const double *__restrict__ L,
-                                int ldL, float *Qf, __nv_bfloat16 *Qhi, __nv_bfloat16 *Qlo, int ldq) {
-    extern __shared__ double sc[];
+// per row. lrow holds l2 (s floats) then 1 / L3, written by the factor step;
+// Q's columns >= s are still zero, so the dot runs over whole 128-column
+// pieces. The kernel entry is split over the warp's lanes.
+__global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
+                                                       const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qhi,
+                                                       __nv_bfloat16 *Qlo, int ldq) {
+    extern __shared__ float qsm[];
+    const int s4 = (s + 127) / 128 * 128;  // <= ldq
+    float *l2 = qsm;                       // s4 floats, zero past s
+    float *sc = qsm + s4;                  // centroid row, X.ld floats
     const int gc = cent[s];
+    for (int t = threadIdx.x; t < s4; t += blockDim.x) l2[t] = t < s ? lrow[t] : 0.f;
     for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sc[t] = X.X[(size_t)gc * X.ld + t];
     __syncthreads();
-    const double qa = X.q[gc];
-    const double *l2 = L + (size_t)s * ldL;  // row s of L: l2 then the pivot L3
-    const double L3 = l2[s];
+    const float inv_l3 = lrow[s];
+    const float qa = X.q[gc];
     const int lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
     for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += gridDim.x * warps) {
-        const float *qrow = Qf + (size_t)i * ldq;
+        const float4 *qrow = (const float4 *)(Qf + (size_t)i * ldq);
         float acc = 0.f;
-        for (int j = lane; j < s; j += 32) acc = fmaf(qrow[j], (float)l2[j], acc);
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        for (int j4 = lane; j4 < s4 / 4; j4 += 32) {
+            const float4 qv = qrow[j4];
+            const float4 lv = *(const float4 *)(l2 + 4 * j4);
+            acc = fmaf(qv.x, lv.x, acc);
+            acc = fmaf(qv.y, lv.y, acc);
+            acc = fmaf(qv.z, lv.z, acc);
+            acc = fmaf(qv.w, lv.w, acc);
+        }
+        float kd = 0.f;
+        if (X.mode == IRWLS_K_RAW_RBF) {
+            const float *b = X.X + (size_t)i * X.ld;
+            for (int t = lane; t < X.width; t += 32) {
+                const float d = sc[t] - b[t];
+                kd = fmaf(d, d, kd);
+            }
+        } else {
+            for (int p = X.rp[i] + lane; p < X.rp[i + 1]; p += 32) kd = fmaf(X.cv[p], sc[X.ci[p]], kd);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            kd += __shfl_xor_sync(0xffffffffu, kd, o);
+        }
         if (lane == 0) {
-            const double kv = kentry(X, sc, qa, i);
-            const float q = (float)((kv - (double)acc) / L3);
+            float kv;
+            if (X.mode == IRWLS_K_RAW_RBF) kv = __expf(X.ng * kd);
+            else if (X.mode == IRWLS_K_LINEAR) kv = kd;
+            else kv = __expf(X.ng * fmaxf(qa + X.q[i] - 2.f * kd, 0.f));
+            const float q = (kv - acc) * inv_l3;
             Qf[(size_t)i * ldq + s] = q;
             const __nv_bfloat16 h = __float2bfloat16_rn(q);
             Qhi[(size_t)i * ldq + s] = h;
@@ -444,10 +527,56 @@ __global__ void q_column_kernel(KView X, int l, const int *__restrict__ cent, in
     }
 }
 
+// Row s of L as FP32 (l2, then 1 / L3) for q_column_kernel.
+__global__ void l_row_f32_kernel(const double *__restrict__ L, int ldL, int s, float *__restrict__ lrow) {
+    for (int t = threadIdx.x; t < s; t += blockDim.x) lrow[t] = __double2float_rn(L[(size_t)s * ldL + t]);
+    if (threadIdx.x == 0) lrow[s] = __double2float_rn(__drcp_rn(L[(size_t)s * ldL + s]));
+}
+
 }  // namespace
 
-extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, int l, const int *d_cand, const void *Qhi, const void *Qlo,
-                                   int ldq, const void *Whi, const void *Wlo, int s, double *d_part) {
+extern "C" void *irwls_f32_mirror(const irwls_dev_set *X) {
+    F32Mirror *f = (F32Mirror *)calloc(1, sizeof(F32Mirror));
+    if (!f) return nullptr;
+    const long long nx = (long long)X->n_rows * X->ld;
+    int rc = 0;
+    rc |= irwls_dev_malloc((void **)&f->X, (size_t)(nx > 0 ? nx : 1) * sizeof(float));
+    rc |= irwls_dev_malloc((void **)&f->cv, (size_t)(X->nnz > 0 ? X->nnz : 1) * sizeof(float));
+    rc |= irwls_dev_malloc((void **)&f->q, (size_t)(X->n_rows > 0 ? X->n_rows : 1) * sizeof(float));
+    if (!rc) {
+        const int g = 4 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148);
+        const double *src[3] = {X->X, X->cv, X->q};
+        float *dst[3] = {f->X, f->cv, f->q};
+        const long long cnt[3] = {nx, X->nnz, X->n_rows};
+        for (int k = 0; k < 3; ++k)
+            if (cnt[k] > 0) {
+                to_f32_kernel<<<g, 256, 0, irwls_stream()>>>(src[k], cnt[k], dst[k]);
+                irwls_count_launch(1);
+            }
+        if (cudaPeekAtLastError() != cudaSuccess) rc = -1;
+    }
+    if (rc) {
+        irwls_dev_free(f->X);
+        irwls_dev_free(f->cv);
+        irwls_dev_free(f->q);
+        free(f);
+        irwls_set_error(-3, "cannot create the FP32 copy of the dataset");
+        return nullptr;
+    }
+    return f;
+}
+
+extern "C" void irwls_f32_mirror_free(void *h) {
+    F32Mirror *f = (F32Mirror *)h;
+    if (!f) return;
+    irwls_dev_free(f->X);
+    irwls_dev_free(f->cv);
+    irwls_dev_free(f->q);
+    free(f);
+}
+
+extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
+                                   const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, double *d_part) {
     const int kst = (s + TC_BK - 1) / TC_BK;
     const size_t smem = 2 * TcStage<64>::BYTES + 1024 + (size_t)64 * X->ld * sizeof(float);
     if (smem > 220 * 1024) {
@@ -457,7 +586,7 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, int l, const int *d_c
     cudaFuncSetAttribute(sgma_tc_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
     sgma_tc_score_kernel<<<ceil_div(l, TC_BM), TC_THREADS, smem, irwls_stream()>>>(
-        kview(X), l, d_cand, (const __nv_bfloat16 *)Qhi, (const __nv_bfloat16 *)Qlo, ldq,
+        kviewf(X, (const F32Mirror *)F), l, d_cand, (const __nv_bfloat16 *)Qhi, (const __nv_bfloat16 *)Qlo, ldq,
         (const __nv_bfloat16 *)Whi, (const __nv_bfloat16 *)Wlo, kst, d_part, irwls_dev_flags());
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_GEMM);
     IRWLS_LAUNCH_CHECK("sgma_tc_score");
@@ -466,12 +595,20 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, int l, const int *d_c
 
 extern "C" int irwls_sgma_tc_partials(int l) { return ceil_div(l, TC_BM); }
 
-extern "C" int irwls_q_column(const irwls_dev_set *X, int l, const int *d_cent, int s, const double *d_L, int ldL,
-                              float *Qf, void *Qhi, void *Qlo, int ldq) {
-    const size_t smem = (size_t)X->ld * sizeof(double);
+// lrow: scratch of at least s + 1 floats.
+extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const double *d_L,
+                              int ldL, float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq) {
+    const int s4 = (s + 127) / 128 * 128;
+    if (s4 > ldq) {
+        irwls_set_error(-12, "Q leading dimension %d below the padded order %d", ldq, s4);
+        return -12;
+    }
+    l_row_f32_kernel<<<1, 256, 0, irwls_stream()>>>(d_L, ldL, s, lrow);
+    IRWLS_LAUNCH_CHECK("l_row_f32");
+    const size_t smem = ((size_t)s4 + X->ld) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int blocks = std::min(ceil_div(l, 8), 16 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
-    q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kview(X), l, d_cent, s, d_L, ldL, Qf,
+    const int blocks = std::min(ceil_div(l, 8), 8 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
+    q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
                                                             (__nv_bfloat16 *)Qhi, (__nv_bfloat16 *)Qlo, ldq);
     IRWLS_LAUNCH_CHECK("q_column");
     return 0;

@@ -171,6 +171,13 @@ int irwls_par_first(const double *d_y, int l, double M, int *d_act, double *d_sd
 size_t irwls_par_gram_part_bytes(int m, int P);
 int irwls_par_gram(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                    const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P);
+/* Precision form of the Gram: A' packed as FP32 hi/lo pairs (d_A holds
+   nact x irwls_par_df_lda(m) pairs), double-float products and sums, FP64
+   reduction of the P partials. */
+int irwls_par_df_lda(int m);
+int irwls_par_gram_df(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
+                      const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P,
+                      void *d_A);
 int irwls_par_residual(const double *d_KSC, int l, int m, const double *d_beta, const double *d_y, double C,
                        double M, double *d_e, double *d_Da);
 int irwls_par_weights(const double *d_Da, const double *d_y, int l, int *d_act, double *d_sd, double *d_day,
@@ -195,7 +202,7 @@ int irwls_prof_collect(void);
 void irwls_prof_read(int slot, double *ms, long long *launches);
 void irwls_prof_reset(void);
 enum { IRWLS_PROF_SGMA_GEMM = 0, IRWLS_PROF_GRAM = 1, IRWLS_PROF_ROWSUM = 2, IRWLS_PROF_CHOL = 3,
-       IRWLS_PROF_PREDICT = 4, IRWLS_PROF_SLOTS = 8 };
+       IRWLS_PROF_PREDICT = 4, IRWLS_PROF_SGMA_CAND = 5, IRWLS_PROF_SGMA_UPDATE = 6, IRWLS_PROF_SLOTS = 8 };
 long long irwls_launch_count(void);
 void irwls_count_launch(int n);
 

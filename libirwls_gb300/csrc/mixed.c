@@ -5,11 +5,14 @@
  *         solves in FP64; scores from Q w on the tensor cores in split BF16
  *         (Q = K_nm L^-T, kept in FP32 and as bf16 hi/lo), candidate kernel
  *         rows of the score epilogue in FP32.
- *   IRWLSpar stays FP64: its system K1 = KC + K_nm^T D_a K_nm carries weights
- *   up to 1e4 against a 1e-5 jitter, so its condition number reaches ~1e13,
- *   and a Gram accumulated from 16-bit-mantissa products (relative error
- *   ~1e-5) turns it indefinite; measured on 200000 rows and 1000 centroids,
- *   that variant's primal objective was off by a factor of 4e6.
+ *   IRWLSpar (budgeted_train.c, irwls_par_dev) accumulates its Gram in
+ *   double-float FP32 pairs; its factor, solves, residuals and convergence
+ *   test stay FP64. Its system K1 = KC + K_nm^T D_a K_nm carries weights up
+ *   to 1e4 against a 1e-5 jitter, so its condition number reaches ~1e13: a
+ *   Gram accumulated from 16-bit-mantissa products (relative error ~1e-5)
+ *   turns it indefinite (measured on 200000 rows and 1000 centroids, that
+ *   variant's primal objective was off by a factor of 4e6), while the
+ *   double-float Gram's ~1e-14 relative error keeps it definite.
  * Selected with irwls_set_precision(IRWLS_PRECISION_MIXED) or the
  * environment variable IRWLS_PRECISION=mixed; plain FP64 is the default.
  */
@@ -26,11 +29,13 @@ int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, con
                         int *d_best, double *d_bestval);
 int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W, int ldz,
                       double *d_L, int ldL);
-int irwls_sgma_tc_score(const irwls_dev_set *X, int l, const int *d_cand, const void *Qhi, const void *Qlo, int ldq,
-                        const void *Whi, const void *Wlo, int s, double *d_part);
+int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
+                        const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, double *d_part);
 int irwls_sgma_tc_partials(int l);
-int irwls_q_column(const irwls_dev_set *X, int l, const int *d_cent, int s, const double *d_L, int ldL, float *Qf,
-                   void *Qhi, void *Qlo, int ldq);
+int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const double *d_L, int ldL,
+                   float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq);
+void *irwls_f32_mirror(const irwls_dev_set *X);
+void irwls_f32_mirror_free(void *h);
 int irwls_split_bf16_f64(const double *X, long long rows, int cols, int ldx, void *hi, void *lo, int ldo);
 int irwls_tc_status(void);
 int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m);
@@ -55,13 +60,18 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     if (m <= 0) return 0;
     int *cand = irwls_draw_sgma_candidates(ds, m);
     if (!cand) return -1;
-    const int ldq = round_up(m, 64), ldL = m, ldz = m;
+    const int ldq = round_up(m, 128), ldL = m, ldz = m;
     const int nblk = irwls_sgma_tc_partials(l);
     int rc = 0;
     int *d_cand = NULL, *d_cent = NULL, *d_best = NULL;
     double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_part = NULL, *d_val = NULL;
-    float *Qf = NULL;
+    float *Qf = NULL, *lrow = NULL;
     void *Qhi = NULL, *Qlo = NULL, *Whi = NULL, *Wlo = NULL;
+    void *F = irwls_f32_mirror(X);
+    if (!F) {
+        free(cand);
+        return -1;
+    }
     rc |= irwls_dev_malloc((void **)&d_cand, (size_t)m * 64 * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_cent, (size_t)m * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_best, sizeof(int));
@@ -76,6 +86,7 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     rc |= irwls_dev_malloc(&Qlo, (size_t)l * ldq * 2);
     rc |= irwls_dev_malloc(&Whi, (size_t)64 * ldq * 2);
     rc |= irwls_dev_malloc(&Wlo, (size_t)64 * ldq * 2);
+    rc |= irwls_dev_malloc((void **)&lrow, (size_t)(m + 1) * sizeof(float));
     if (rc) goto done;
     {
         int first[2] = {l, l + 1};
@@ -87,18 +98,22 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
         rc |= irwls_dev_memset(Qhi, 0, (size_t)l * ldq * 2);
         rc |= irwls_dev_memset(Qlo, 0, (size_t)l * ldq * 2);
         rc |= irwls_sgma_factor(X, 0, d_cent, d_best, d_W, ldz, d_L, ldL);
-        rc |= irwls_q_column(X, l, d_cent, 0, d_L, ldL, Qf, Qhi, Qlo, ldq);
+        rc |= irwls_q_column(X, F, l, d_cent, 0, d_L, ldL, lrow, Qf, Qhi, Qlo, ldq);
         if (m > 1) {
             rc |= irwls_sgma_factor(X, 1, d_cent, d_best, d_W, ldz, d_L, ldL);
-            rc |= irwls_q_column(X, l, d_cent, 1, d_L, ldL, Qf, Qhi, Qlo, ldq);
+            rc |= irwls_q_column(X, F, l, d_cent, 1, d_L, ldL, lrow, Qf, Qhi, Qlo, ldq);
         }
         for (int s = 2; s < m && !rc; s++) {
             rc |= irwls_sgma_cand_forward(X, d_cand + (size_t)s * 64, d_cent, s, d_L, ldL, d_W, d_KN, ldz, d_eta);
+            irwls_prof_begin(IRWLS_PROF_SGMA_CAND);
             rc |= irwls_split_bf16_f64(d_W, 64, s, ldz, Whi, Wlo, ldq);
-            rc |= irwls_sgma_tc_score(X, l, d_cand + (size_t)s * 64, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
+            irwls_prof_end(IRWLS_PROF_SGMA_CAND);
+            rc |= irwls_sgma_tc_score(X, F, l, d_cand + (size_t)s * 64, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
+            irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
             rc |= irwls_sgma_select_n(d_part, nblk, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
-            rc |= irwls_q_column(X, l, d_cent, s, d_L, ldL, Qf, Qhi, Qlo, ldq);
+            rc |= irwls_q_column(X, F, l, d_cent, s, d_L, ldL, lrow, Qf, Qhi, Qlo, ldq);
+            irwls_prof_end(IRWLS_PROF_SGMA_UPDATE);
         }
         if (rc) goto done;
         double *val = (double *)malloc((size_t)m * sizeof(double));
@@ -121,8 +136,9 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
 done:
     free(cand);
     {
-        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qhi, Qlo, Whi, Wlo};
+        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qhi, Qlo, Whi, Wlo, lrow};
         for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
+        irwls_f32_mirror_free(F);
     }
     return rc ? -1 : 0;
 }

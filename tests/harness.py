@@ -107,3 +107,24 @@ def dual_objective(hd, beta, gamma, kernel):
         K = np.exp(-gamma * np.maximum(sq[:, None] + sq[None, :] - 2 * Xs @ Xs.T, 0.0))
     bs = b[sv]
     return float((y[sv] * bs).sum() - 0.5 * bs @ K @ bs)
+
+
+def budget_primal(hd, cent, w, gamma, cost, kernel):
+    """Budgeted primal 1/2 w^T (K_mm + 1e-5 I) w + C sum_i max(0, 1 - y_i f_i),
+    f = K_nm w over the training rows, in FP64 on the host (centroid indices
+    may name the class-mean rows l and l+1)."""
+    rows, y, q = _abi.dataset_rows(hd.struct, hd.n_rows)
+    d = max([int(r[0].max()) for r in rows if len(r[0])] + [0]) + 1
+    X = np.zeros((hd.n_rows, d))
+    for i, (ix, v) in enumerate(rows):
+        X[i, ix] = v
+    Xc = X[np.asarray(cent)]
+    if kernel == 0:
+        Kmm, Knm = Xc @ Xc.T, X[:hd.l] @ Xc.T
+    else:
+        qc = q[np.asarray(cent)]
+        Kmm = np.exp(-gamma * (qc[:, None] + qc[None, :] - 2.0 * Xc @ Xc.T))
+        Knm = np.exp(-gamma * (q[:hd.l, None] + qc[None, :] - 2.0 * X[:hd.l] @ Xc.T))
+    w = np.asarray(w)
+    f = Knm @ w
+    return float(0.5 * w @ (Kmm + 1e-5 * np.eye(len(w))) @ w + cost * np.maximum(0.0, 1.0 - y[:hd.l] * f).sum())

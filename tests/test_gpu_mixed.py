@@ -1,11 +1,16 @@
-"""Precision form of SGMA (irwls_set_precision(IRWLS_PRECISION_MIXED)): the
-candidate scores come from split-BF16 tensor-core products on the Nystrom
-features Q = K_nm L^-T, with the factor, its solves and IRWLSpar in FP64.
+"""Precision form of budgeted IRWLS (irwls_set_precision(IRWLS_PRECISION_MIXED)).
 
-Its scores differ from the FP64 form by about 1e-5 relative, so it may pick a
+SGMA: the candidate scores come from split-BF16 tensor-core products on the
+Nystrom features Q = K_nm L^-T, with the factor and its solves in FP64. Its
+scores differ from the FP64 form by about 1e-5 relative, so it may pick a
 different centroid where two candidates score within that margin; on the
-seeded reference cases below every step's argmax agrees with the reference,
-and the weights then meet the plain form's bars."""
+seeded reference cases below every step's argmax agrees with the reference.
+
+IRWLSpar: the Gram K1 = KC + A'^T A' is accumulated in double-float (FP32
+pairs, about 48 significant bits) instead of FP64; the factor, solves,
+residual and convergence test stay FP64. Its weights therefore differ from
+the reference's by the solve's sensitivity to that rounding; the bar is the
+objective the weights reach and the labels they predict."""
 import numpy as np
 import pytest
 
@@ -14,20 +19,36 @@ from libirwls_gb300 import load
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"budget_cfg2_reduced": 1e-8, "budget_linear": 5e-5}
+# Relative primal-objective difference allowed against the reference (the
+# precision form's contract is 1e-4). Measured: 1e-12 and below on the RBF
+# cases, 1.0e-7 on the rank-deficient linear-kernel case, 9e-7 on the
+# 200000-row benchmark workload against the FP64 form.
+PRIMAL_TOL = {"budget_linear": 1e-5}
 
 
-@pytest.mark.parametrize("case", ["budget_sgma", "budget_sgma_dense", "budget_linear", "budget_cfg2_reduced"])
-def test_mixed_sgma_matches_reference(case):
+@pytest.mark.parametrize("case", ["budget_sgma", "budget_sgma_dense", "budget_random", "budget_linear",
+                                  "budget_cfg2_reduced"])
+def test_mixed_budgeted_matches_reference(case):
     lib = load()
     g = H.golden(case)
     p = H.params(g)
-    tr, _ = H.datasets(g)
+    tr, te = H.datasets(g)
     lib.irwls_set_precision(1)
     try:
-        cent, w, _, _, _ = H.run_budget(lib, tr, p)
+        cent, w, cptr, wptr, prop = H.run_budget(lib, tr, p)
     finally:
         lib.irwls_set_precision(0)
     assert lib.irwls_tc_status() == 0
     assert np.array_equal(cent, g["centroids"])
-    assert H.rel_err(w, g["weights"]) < TOL.get(case, H.REL_TOL)
+    ref = H.budget_primal(tr, g["centroids"], g["weights"], p["gamma"], p["C"], p["kernel"])
+    got = H.budget_primal(tr, cent, w, p["gamma"], p["C"], p["kernel"])
+    print("%s: weights rel err %.3g, primal rel err %.3g" % (case, H.rel_err(w, g["weights"]),
+                                                             abs(got - ref) / abs(ref)))
+    assert abs(got - ref) <= PRIMAL_TOL.get(case, 1e-6) * abs(ref)
+    mdl = lib.calculateBudgetedModel(prop, tr.struct, cptr, wptr)
+    try:
+        labels = H.predict(lib, te, mdl, 0)
+    finally:
+        lib.freeModel(mdl)
+    agree = float((labels == g["hard"]).mean())
+    assert agree >= 0.999
