@@ -13,6 +13,7 @@
 // over active rows is a split-K SYRK on the lower triangle; the right-hand
 // side K2 = sum_i a_i (sqrt(Da_i) y_i) is computed as the extra row m of the
 // same product, which is exactly where the Cholesky solver wants it.
+#include <cuda_bf16.h>
 #include <math.h>
 
 #include <algorithm>
@@ -30,14 +31,12 @@ constexpr int CT = 1024;
 
 // Per candidate: KNC row, forward then backward substitution with L, eta.
 // smem: v[s] (working vector), A row of the candidate (ld doubles).
-// mode 0: forward and backward substitution, eta = 1 - k.z (the reference's
-// form); mode 1 (precision form): forward substitution only, eta = 1 - |w|^2.
 __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__restrict__ cand,
                                                         const int *__restrict__ cent, int s,
                                                         const double *__restrict__ L, int ldL,
                                                         double *__restrict__ W, double *__restrict__ Z,
                                                         double *__restrict__ KN, int ldz,
-                                                        double *__restrict__ eta, int mode) {
+                                                        double *__restrict__ eta) {
     extern __shared__ double sm[];
     double *v = sm;
     double *sA = sm + s;
@@ -87,14 +86,6 @@ __global__ void __launch_bounds__(256) sgma_cand_kernel(KView X, const int *__re
     }
     for (int e = tid; e < s; e += blockDim.x) W[(size_t)c * ldz + e] = v[e];
     __syncthreads();
-    if (mode == 1) {
-        if (tid == 0) {
-            double val = 1.0;
-            for (int e = 0; e < s; ++e) val = __dsub_rn(val, __dmul_rn(v[e], v[e]));
-            eta[c] = val;
-        }
-        return;
-    }
     // backward: L^T z = w
     for (int b = nblk - 1; b >= 0; --b) {
         const int r0 = b * 32, r1 = min(s, r0 + 32);
@@ -141,6 +132,164 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem, int src_
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// ---- precision form: candidate solves through the explicit inverse factor ----
+//
+// The reference keeps L^-1 beside L (invKC, src/budgeted-train.c:241-279); the
+// precision form does the same so that the 64 candidate solves of a step,
+// W = K_CN L^-T (FP64), are one split-K GEMM over all SMs instead of 64
+// dependent substitutions. Linv is row-major (ldi), zero above the diagonal.
+
+// KN[c][t] = k(cand_c, cent_t) for t < s, FP64 (the reference's kernel).
+__global__ void __launch_bounds__(128) cand_rows_kernel(KView X, const int *__restrict__ cand,
+                                                        const int *__restrict__ cent, int s, double *__restrict__ KN,
+                                                        int ldz) {
+    extern __shared__ double sa[];
+    const int c = blockIdx.y, gc = cand[c];
+    for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sa[t] = X.X[(size_t)gc * X.ld + t];
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < s) KN[(size_t)c * ldz + t] = kentry(X, sa, X.q[gc], cent[t]);
+}
+
+// Partial W^T over one chunk of WT columns of Linv: item (eb, tc) covers rows
+// e in [32 eb, 32 eb + 32) and t in [WT tc, WT tc + WT) (t <= e only, Linv is
+// zero above); part[(tc * 64 + c) * ldp + e]. Rows of Linv and KN stream
+// through a cp.async double buffer of WK columns.
+constexpr int WE = 32, WT = 128, WK = 16;
+__global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ Linv, int ldi,
+                                                     const double *__restrict__ KN, int ldz, int s,
+                                                     double *__restrict__ part, int ldp) {
+    const int eb = blockIdx.x, tc = blockIdx.y;
+    const int e0 = eb * WE, t0 = tc * WT;
+    if (t0 > e0 + WE - 1) return;
+    const int t1 = min(min(t0 + WT, e0 + WE), s);
+    __shared__ __align__(16) double Ls[2][WE][WK + 1];
+    __shared__ __align__(16) double Ks[2][NCAND][WK + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    double acc[2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    auto load = [&](int buf, int t) {
+        for (int u = tid; u < (WE + NCAND) * WK; u += 256) {
+            const int r = u / WK, k = u % WK;
+            const int tt = t + k;
+            if (r < WE) {
+                const int e = e0 + r;
+                const bool ok = e < s && tt < t1;
+                cp_async8(&Ls[buf][r][k], ok ? (const void *)(Linv + (size_t)e * ldi + tt) : (const void *)Linv,
+                          ok ? 8 : 0);
+            } else {
+                const int c = r - WE;
+                const bool ok = tt < t1;
+                cp_async8(&Ks[buf][c][k], ok ? (const void *)(KN + (size_t)c * ldz + tt) : (const void *)KN,
+                          ok ? 8 : 0);
+            }
+        }
+        cp_async_commit();
+    };
+    if (t0 < t1) load(0, t0);
+    int it = 0;
+    for (int t = t0; t < t1; t += WK, ++it) {
+        const int buf = it & 1;
+        if (t + WK < t1) {
+            load(buf ^ 1, t + WK);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < WK; ++k) {
+            const double l0 = Ls[buf][ty][k], l1 = Ls[buf][ty + 16][k];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const double kv = Ks[buf][tx + 16 * b][k];
+                acc[0][b] = fma(l0, kv, acc[0][b]);
+                acc[1][b] = fma(l1, kv, acc[1][b]);
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const int e = e0 + ty + 16 * a;
+        if (e >= s) continue;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) part[((size_t)tc * NCAND + tx + 16 * b) * ldp + e] = acc[a][b];
+    }
+}
+
+// Per candidate c: w_e = sum of the chunks of row e in chunk order, W (FP64),
+// eta = 1 - |w|^2 (fixed-order block reduction), and w as bf16 hi/lo of its
+// FP32 rounding (zero up to the padded width kpad).
+__global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict__ part, int ldp, int s,
+                                                       double *__restrict__ W, int ldz, __nv_bfloat16 *Whi,
+                                                       __nv_bfloat16 *Wlo, int ldq, int kpad,
+                                                       double *__restrict__ eta) {
+    __shared__ double red[256];
+    const int c = blockIdx.x;
+    double ss = 0.0;
+    for (int e = threadIdx.x; e < kpad; e += blockDim.x) {
+        float xf = 0.f;
+        if (e < s) {
+            const int ntc = (e / WE * WE + WE - 1) / WT + 1;
+            double w = 0.0;
+            for (int tc = 0; tc < ntc; ++tc) w += part[((size_t)tc * NCAND + c) * ldp + e];
+            W[(size_t)c * ldz + e] = w;
+            ss = fma(w, w, ss);
+            xf = (float)w;
+        }
+        const __nv_bfloat16 h = __float2bfloat16_rn(xf);
+        Whi[(size_t)c * ldq + e] = h;
+        Wlo[(size_t)c * ldq + e] = __float2bfloat16_rn(xf - __bfloat162float(h));
+    }
+    red[threadIdx.x] = ss;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) eta[c] = 1.0 - red[0];
+}
+
+// New row s of Linv from row s of L (l2, pivot L3):
+//   Linv[s][t] = -(sum_{t <= e < s} l2_e Linv[e][t]) / L3,  Linv[s][s] = 1 / L3.
+// Stage 1: partial sums over e-chunks of LE rows, part2[chunk][t].
+constexpr int LE = 64;
+__global__ void __launch_bounds__(128) linv_partial_kernel(const double *__restrict__ L, int ldL,
+                                                           const double *__restrict__ Linv, int ldi, int s,
+                                                           double *__restrict__ part2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e0 = blockIdx.y * LE, e1 = min(s, e0 + LE);
+    if (t >= s) return;
+    const double *l2 = L + (size_t)s * ldL;
+    double acc = 0.0;
+    for (int e = max(e0, t); e < e1; ++e) acc = fma(l2[e], Linv[(size_t)e * ldi + t], acc);
+    part2[(size_t)blockIdx.y * s + t] = acc;
+}
+
+// Stage 2 (one CTA): the row of Linv in chunk order, and row s of L as FP32
+// (l2, then 1 / L3) for the Q column update.
+__global__ void __launch_bounds__(256) linv_finish_kernel(const double *__restrict__ L, int ldL,
+                                                          double *__restrict__ Linv, int ldi, int s,
+                                                          const double *__restrict__ part2, int nch,
+                                                          float *__restrict__ lrow) {
+    const double L3 = L[(size_t)s * ldL + s];
+    for (int t = threadIdx.x; t < s; t += blockDim.x) {
+        double acc = 0.0;
+        for (int ch = t / LE; ch < nch; ++ch) acc += part2[(size_t)ch * s + t];
+        Linv[(size_t)s * ldi + t] = -acc / L3;
+        lrow[t] = __double2float_rn(L[(size_t)s * ldL + t]);
+    }
+    if (threadIdx.x == 0) {
+        const double inv = 1.0 / L3;
+        Linv[(size_t)s * ldi + s] = inv;
+        lrow[s] = __double2float_rn(inv);
+    }
+}
 
 // SGMA scores: for row tiles of GM rows and all 64 candidates,
 // acc[i][c] = sum_k KSC[k*l + i] Z[c*ldz + k], r = acc - k(cand_c, x_i), and
@@ -673,7 +822,7 @@ extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand
     if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_CAND);
     sgma_cand_kernel<<<NCAND, 256, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_L, ldL, d_W, d_Z, d_KN, ldz,
-                                                          d_eta, 0);
+                                                          d_eta);
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_CAND);
     IRWLS_LAUNCH_CHECK("sgma_cand");
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
@@ -686,27 +835,53 @@ extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand
 
 extern "C" int irwls_sgma_partials(int l) { return sgma_gemm_grid(l); }
 
-// Precision form: candidate kernel rows, forward substitution, eta = 1 - |w|^2.
-extern "C" int irwls_sgma_cand_forward(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s,
-                                       const double *d_L, int ldL, double *d_W, double *d_KN, int ldz, double *d_eta) {
-    const size_t smem = ((size_t)s + X->ld) * sizeof(double);
-    if (smem > 200 * 1024) {
-        irwls_set_error(-7, "SGMA budget %d with feature width %d exceeds the substitution tile", s, X->width);
-        return -7;
-    }
-    if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_cand_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_CAND);
-    sgma_cand_kernel<<<NCAND, 256, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_L, ldL, d_W, nullptr, d_KN,
-                                                          ldz, d_eta, 1);
-    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_CAND);
-    IRWLS_LAUNCH_CHECK("sgma_cand_forward");
-    return 0;
-}
-
 extern "C" int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, const int *d_cand, int s,
                                    int *d_cent, int *d_best, double *d_bestval) {
     sgma_select_kernel<<<1, NCAND, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval);
     IRWLS_LAUNCH_CHECK("sgma_select");
+    return 0;
+}
+
+// Precision form: W = K_CN L^-T for the 64 candidates of step s, eta and the
+// bf16 split of W. wpart: irwls_sgma_wpart_count(m) doubles.
+extern "C" size_t irwls_sgma_wpart_count(int m) { return ((size_t)m / WT + 2) * NCAND * (size_t)(m > 0 ? m : 1); }
+extern "C" size_t irwls_sgma_lpart_count(int m) { return ((size_t)ceil_div(m, LE) + 1) * (size_t)(m > 0 ? m : 1); }
+
+extern "C" int irwls_sgma_cand_inv(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s,
+                                   const double *d_Linv, int ldi, double *d_KN, int ldz, double *d_wpart, int ldp,
+                                   double *d_W, void *Whi, void *Wlo, int ldq, double *d_eta) {
+    if (s < 1) return 0;
+    const size_t smem = (size_t)X->ld * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(cand_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int kpad = ceil_div(s, 64) * 64;
+    if (kpad > ldq) {
+        irwls_set_error(-12, "candidate width %d exceeds the split leading dimension %d", kpad, ldq);
+        return -12;
+    }
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_CAND);
+    cand_rows_kernel<<<dim3(ceil_div(s, 128), NCAND), 128, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_KN,
+                                                                                 ldz);
+    IRWLS_LAUNCH_CHECK("cand_rows");
+    w_gemm_kernel<<<dim3(ceil_div(s, WE), ceil_div(s, WT)), 256, 0, irwls_stream()>>>(d_Linv, ldi, d_KN, ldz, s,
+                                                                                    d_wpart, ldp);
+    IRWLS_LAUNCH_CHECK("w_gemm");
+    w_finish_kernel<<<NCAND, 256, 0, irwls_stream()>>>(d_wpart, ldp, s, d_W, ldz, (__nv_bfloat16 *)Whi,
+                                                       (__nv_bfloat16 *)Wlo, ldq, kpad, d_eta);
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_CAND);
+    IRWLS_LAUNCH_CHECK("w_finish");
+    return 0;
+}
+
+// Row s of Linv from row s of L, and row s of L in FP32 (l2, 1 / L3) into lrow.
+extern "C" int irwls_sgma_linv_update(const double *d_L, int ldL, double *d_Linv, int ldi, int s, double *d_lpart,
+                                      float *d_lrow) {
+    const int nch = ceil_div(s, LE);
+    if (s > 0) {
+        linv_partial_kernel<<<dim3(ceil_div(s, 128), nch), 128, 0, irwls_stream()>>>(d_L, ldL, d_Linv, ldi, s, d_lpart);
+        IRWLS_LAUNCH_CHECK("linv_partial");
+    }
+    linv_finish_kernel<<<1, 256, 0, irwls_stream()>>>(d_L, ldL, d_Linv, ldi, s, d_lpart, nch, d_lrow);
+    IRWLS_LAUNCH_CHECK("linv_finish");
     return 0;
 }
 

@@ -527,11 +527,6 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
     }
 }
 
-// Row s of L as FP32 (l2, then 1 / L3) for q_column_kernel.
-__global__ void l_row_f32_kernel(const double *__restrict__ L, int ldL, int s, float *__restrict__ lrow) {
-    for (int t = threadIdx.x; t < s; t += blockDim.x) lrow[t] = __double2float_rn(L[(size_t)s * ldL + t]);
-    if (threadIdx.x == 0) lrow[s] = __double2float_rn(__drcp_rn(L[(size_t)s * ldL + s]));
-}
 
 }  // namespace
 
@@ -595,16 +590,14 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
 
 extern "C" int irwls_sgma_tc_partials(int l) { return ceil_div(l, TC_BM); }
 
-// lrow: scratch of at least s + 1 floats.
-extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const double *d_L,
-                              int ldL, float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq) {
+// lrow: row s of L in FP32 (s values, then 1 / L3), from irwls_sgma_linv_update.
+extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s,
+                              const float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq) {
     const int s4 = (s + 127) / 128 * 128;
     if (s4 > ldq) {
         irwls_set_error(-12, "Q leading dimension %d below the padded order %d", ldq, s4);
         return -12;
     }
-    l_row_f32_kernel<<<1, 256, 0, irwls_stream()>>>(d_L, ldL, s, lrow);
-    IRWLS_LAUNCH_CHECK("l_row_f32");
     const size_t smem = ((size_t)s4 + X->ld) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int blocks = std::min(ceil_div(l, 8), 8 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));

@@ -1,10 +1,12 @@
 /*
  * mixed.c -- host orchestration of the precision form of budgeted IRWLS
  * (same loops, exit tests and random draws as budgeted_train.c):
- *   SGMA: candidate kernel rows, factor L of K_CC + jitter and its forward
- *         solves in FP64; scores from Q w on the tensor cores in split BF16
- *         (Q = K_nm L^-T, kept in FP32 and as bf16 hi/lo), candidate kernel
- *         rows of the score epilogue in FP32.
+ *   SGMA: candidate kernel rows, the factor L of K_CC + jitter and its
+ *         inverse (kept explicitly, as the reference keeps invKC) in FP64;
+ *         the candidate solves W = K_CN L^-T as one FP64 GEMM; scores from
+ *         Q w on the tensor cores in split BF16 (Q = K_nm L^-T, kept in FP32
+ *         and as bf16 hi/lo), candidate kernel rows of the score epilogue in
+ *         FP32.
  *   IRWLSpar (budgeted_train.c, irwls_par_dev) accumulates its Gram in
  *   double-float FP32 pairs; its factor, solves, residuals and convergence
  *   test stay FP64. Its system K1 = KC + K_nm^T D_a K_nm carries weights up
@@ -23,8 +25,13 @@
 #include "irwls_dev.h"
 #include "irwls_gpu.h"
 
-int irwls_sgma_cand_forward(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s, const double *d_L,
-                            int ldL, double *d_W, double *d_KN, int ldz, double *d_eta);
+int irwls_sgma_cand_inv(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s, const double *d_Linv,
+                        int ldi, double *d_KN, int ldz, double *d_wpart, int ldp, double *d_W, void *Whi, void *Wlo,
+                        int ldq, double *d_eta);
+int irwls_sgma_linv_update(const double *d_L, int ldL, double *d_Linv, int ldi, int s, double *d_lpart,
+                           float *d_lrow);
+size_t irwls_sgma_wpart_count(int m);
+size_t irwls_sgma_lpart_count(int m);
 int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, const int *d_cand, int s, int *d_cent,
                         int *d_best, double *d_bestval);
 int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W, int ldz,
@@ -32,11 +39,10 @@ int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const in
 int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
                         const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, double *d_part);
 int irwls_sgma_tc_partials(int l);
-int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const double *d_L, int ldL,
-                   float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq);
+int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const float *lrow, float *Qf,
+                   void *Qhi, void *Qlo, int ldq);
 void *irwls_f32_mirror(const irwls_dev_set *X);
 void irwls_f32_mirror_free(void *h);
-int irwls_split_bf16_f64(const double *X, long long rows, int cols, int ldx, void *hi, void *lo, int ldo);
 int irwls_tc_status(void);
 int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m);
 void irwls_record_run_info(int par_iterations, int active_rows);
@@ -64,7 +70,8 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     const int nblk = irwls_sgma_tc_partials(l);
     int rc = 0;
     int *d_cand = NULL, *d_cent = NULL, *d_best = NULL;
-    double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_part = NULL, *d_val = NULL;
+    double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_part = NULL, *d_val = NULL, *d_Linv = NULL,
+           *d_wpart = NULL, *d_lpart = NULL;
     float *Qf = NULL, *lrow = NULL;
     void *Qhi = NULL, *Qlo = NULL, *Whi = NULL, *Wlo = NULL;
     void *F = irwls_f32_mirror(X);
@@ -87,32 +94,35 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     rc |= irwls_dev_malloc(&Whi, (size_t)64 * ldq * 2);
     rc |= irwls_dev_malloc(&Wlo, (size_t)64 * ldq * 2);
     rc |= irwls_dev_malloc((void **)&lrow, (size_t)(m + 1) * sizeof(float));
+    rc |= irwls_dev_malloc((void **)&d_Linv, (size_t)m * ldL * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_wpart, irwls_sgma_wpart_count(m) * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_lpart, irwls_sgma_lpart_count(m) * sizeof(double));
     if (rc) goto done;
     {
         int first[2] = {l, l + 1};
         rc |= irwls_dev_h2d(d_cand, cand, (size_t)m * 64 * sizeof(int));
         rc |= irwls_dev_h2d(d_cent, first, (m > 1 ? 2 : 1) * sizeof(int));
         rc |= irwls_dev_memset(d_L, 0, (size_t)m * ldL * sizeof(double));
+        rc |= irwls_dev_memset(d_Linv, 0, (size_t)m * ldL * sizeof(double));
         rc |= irwls_dev_memset(d_W, 0, (size_t)64 * ldz * sizeof(double));
         rc |= irwls_dev_memset(Qf, 0, (size_t)l * ldq * sizeof(float));
         rc |= irwls_dev_memset(Qhi, 0, (size_t)l * ldq * 2);
         rc |= irwls_dev_memset(Qlo, 0, (size_t)l * ldq * 2);
-        rc |= irwls_sgma_factor(X, 0, d_cent, d_best, d_W, ldz, d_L, ldL);
-        rc |= irwls_q_column(X, F, l, d_cent, 0, d_L, ldL, lrow, Qf, Qhi, Qlo, ldq);
-        if (m > 1) {
-            rc |= irwls_sgma_factor(X, 1, d_cent, d_best, d_W, ldz, d_L, ldL);
-            rc |= irwls_q_column(X, F, l, d_cent, 1, d_L, ldL, lrow, Qf, Qhi, Qlo, ldq);
+        /* centroids 0 and 1 are the class means (src/budgeted-train.c:127-147) */
+        for (int s = 0; s < 2 && s < m && !rc; s++) {
+            rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
+            rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
+            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq);
         }
         for (int s = 2; s < m && !rc; s++) {
-            rc |= irwls_sgma_cand_forward(X, d_cand + (size_t)s * 64, d_cent, s, d_L, ldL, d_W, d_KN, ldz, d_eta);
-            irwls_prof_begin(IRWLS_PROF_SGMA_CAND);
-            rc |= irwls_split_bf16_f64(d_W, 64, s, ldz, Whi, Wlo, ldq);
-            irwls_prof_end(IRWLS_PROF_SGMA_CAND);
+            rc |= irwls_sgma_cand_inv(X, d_cand + (size_t)s * 64, d_cent, s, d_Linv, ldL, d_KN, ldz, d_wpart, m, d_W,
+                                      Whi, Wlo, ldq, d_eta);
             rc |= irwls_sgma_tc_score(X, F, l, d_cand + (size_t)s * 64, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
             irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
             rc |= irwls_sgma_select_n(d_part, nblk, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
-            rc |= irwls_q_column(X, F, l, d_cent, s, d_L, ldL, lrow, Qf, Qhi, Qlo, ldq);
+            rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
+            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq);
             irwls_prof_end(IRWLS_PROF_SGMA_UPDATE);
         }
         if (rc) goto done;
@@ -136,7 +146,8 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
 done:
     free(cand);
     {
-        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qhi, Qlo, Whi, Wlo, lrow};
+        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qhi, Qlo, Whi, Wlo, lrow,
+                        d_Linv, d_wpart, d_lpart};
         for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
         irwls_f32_mirror_free(F);
     }
