@@ -2,22 +2,29 @@
 """Benchmark of the budgeted-IRWLS training path (SGMA centroid selection +
 IRWLS weighted least squares) on one GB300.
 
-Workload (plain FP64 form): n = 200,000 rows, d = 54 (10 N(0,1) features +
-one-hot groups of 4 and 40; labels from a seeded random 2-layer tanh network
-with 5% flipped; seeded synthetic data, since the reference's public demo set
-is not available offline), RBF gamma = 0.1, C = 100, budget m = 1000, 64
-candidates per SGMA step (the count the reference hard-codes).
+Workload: n = 200,000 rows, d = 54 (10 N(0,1) features + one-hot groups of 4
+and 40; labels from a seeded random 2-layer tanh network with 5% flipped;
+seeded synthetic data, since the reference's public demo set is not available
+offline), RBF gamma = 0.1, C = 100, budget m = 1000, 64 candidates per SGMA
+step (the count the reference hard-codes).
 
-One step = one complete training (SGMA + IRWLSpar) of that workload.
-  value : train seconds per step with the dataset already resident on the GPU
-          (CUDA events on the library's stream; L2 flushed between steps).
-  e2e   : train seconds per step through the reference-facing C ABI
-          (SGMA() + IRWLSpar() on the host svm_dataset): host-to-device copies
-          of the dataset and device-to-host copies of the results included.
-  roofline: the SGMA score GEMM (l x s x 64 FP64 GEMM with the candidate
-          kernel rows evaluated in its epilogue), FP64-FMA bound; algorithmic
-          flops 2*l*s*64 per launch; peak = FP64 FMA throughput measured live
-          by the library's DFMA-chain probe.
+One step = one complete training (SGMA + IRWLSpar) of that workload. Both
+forms are timed in the same run, on the same resident dataset:
+  plain FP64 : the reference's arithmetic, the form the parity tests pin;
+  precision  : SGMA scores in split BF16 on the tensor cores, IRWLSpar's Gram
+               in double-float FP32 pairs, factors/solves/residuals in FP64.
+  value : train seconds per step of the precision form when it meets the
+          accuracy bars against the plain run of the same job (relative primal
+          objective difference <= 1e-4, held-out accuracy change <= 0.1%),
+          else of the plain form; dataset resident on the GPU, CUDA events on
+          the library's stream, L2 flushed between steps.
+  e2e   : the same form through the reference-facing C ABI (SGMA() +
+          IRWLSpar() on the host svm_dataset), host-to-device copies of the
+          dataset and device-to-host copies of the results included.
+  roofline: the dominant kernel of that form (double-float Gram: FP32-issue
+          bound at 12 instructions per product-sum, against a live FP32 FMA
+          probe; plain form: the FP64 SGMA GEMM against a live FP64 probe).
+  kernels : the other measured kernel rooflines of both forms.
   cpu_baseline: the CPU restatement of the reference (oracle/irwls_port.c,
           reference arithmetic and BLAS/LAPACK calls) on all host cores, on a
           bounded sample extrapolated to the full workload: SGMA steps timed at
@@ -26,6 +33,7 @@ One step = one complete training (SGMA + IRWLSpar) of that workload.
           and second iterations timed at m = 1000 (later iterations costed
           as the second), with the iteration count of the GPU run.
 
+`--form plain|mixed` times one form only (no accuracy comparison).
 `--workload full` measures the dense full-IRWLS workload instead (n = 4000
 train rows, d = 20, two Gaussian classes with 10% flipped labels, RBF gamma =
 0.05, C = 10, working set 500); its CPU baseline is the restatement's whole
@@ -71,7 +79,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
     ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full"])
-    ap.add_argument("--no-mixed", action="store_true", help="skip the precision-form measurement")
+    ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
+                    help="forms to time: both (headline = precision form if it meets the accuracy bars), "
+                         "or only one of them")
     return ap.parse_args()
 
 
@@ -91,9 +101,8 @@ def props(budget, algorithm=1, threads=1):
 
 def config(args, extra=None):
     c = {
-        "workload": "budgeted IRWLS (SGMA + weighted LS), plain FP64: n=%d, d=54 (10 N(0,1) + one-hot 4 + "
-                    "one-hot 40), RBF gamma=0.1, C=100, budget m=%d, 64 candidates per SGMA step"
-                    % (args.rows, args.budget),
+        "workload": "budgeted IRWLS (SGMA + weighted LS): n=%d, d=54 (10 N(0,1) + one-hot 4 + one-hot 40), "
+                    "RBF gamma=0.1, C=100, budget m=%d, 64 candidates per SGMA step" % (args.rows, args.budget),
         "n": args.rows, "d": 54, "gamma": GAMMA, "C": COST, "budget": args.budget, "candidates_per_step": 64,
         "form": "plain FP64", "parallelism": "replicas" if args.gpus > 1 else "single GPU",
         "l2": "flushed between timed steps (512 MiB overwrite); K_nm alone is %.1f GB"
@@ -220,6 +229,131 @@ class Clocks:
                 "samples": len(rows), "reasons": reasons}
 
 
+PROFILE_SLOTS = {"sgma_scores": 0, "sgma_candidate_solves": 5, "sgma_select_and_factor": 6, "irwls_gram": 1,
+                 "irwls_cholesky": 3}
+PRIMAL_BAR, ACC_BAR = 1e-4, 1e-3
+
+
+def profile_read(lib, slot, steps):
+    ms, n = C.c_double(), C.c_longlong()
+    lib.irwls_profile_read(slot, C.byref(ms), C.byref(n))
+    return ms.value / 1000.0 / max(steps, 1), n.value // max(steps, 1)
+
+
+def measured_peaks():
+    """Measured HBM / bf16 peaks of this GPU pool, if present."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f), "measured (MEASURED_PEAKS.json)"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback (one earlier GB300 measurement)"
+
+
+def timed_trainings(lib, libc, res, p, args, cent, w, precision, clocks=None):
+    """W untimed then K timed trainings of one form on the resident dataset
+    (L2 flushed before each; CUDA events on the library's stream). Returns
+    mean seconds, per-stage profile, launches and the clock record."""
+    lib.irwls_set_precision(precision)
+
+    def step():
+        libc.srand(1)
+        if lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD)) != 0:
+            raise SystemExit("training failed: " + lib.irwls_last_error_message().decode())
+
+    for _ in range(args.warmup):
+        step()
+    lib.irwls_profile_enable(1)
+    lib.irwls_profile_reset()
+    launches0 = lib.irwls_kernel_launches()
+    if clocks:
+        clocks.start()
+    times = []
+    for _ in range(args.steps):
+        lib.irwls_l2_flush(512 << 20)
+        lib.irwls_timer_start()
+        step()
+        times.append(lib.irwls_timer_stop() / 1000.0)
+    clk = clocks.stop() if clocks else None
+    launches = lib.irwls_kernel_launches() - launches0
+    prof = {name: profile_read(lib, slot, args.steps) for name, slot in PROFILE_SLOTS.items()}
+    lib.irwls_profile_enable(0)
+    iters, nact = C.c_int(), C.c_int()
+    lib.irwls_last_run_info(C.byref(iters), C.byref(nact))
+    return {"s": statistics.mean(times), "prof": prof, "launches": launches, "clocks": clk,
+            "iters": iters.value, "nact": nact.value, "gram_flops": lib.irwls_last_gram_flops()}
+
+
+def end_to_end(lib, libc, hd, p, args, precision, ref_cent):
+    """SGMA() + IRWLSpar() through the reference-facing C ABI on the host
+    svm_dataset: host-to-device copies of the dataset and device-to-host
+    copies of the results inside the timed region."""
+    import numpy as np
+
+    lib.irwls_set_precision(precision)
+    h0, d0 = C.c_longlong(), C.c_longlong()
+    lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
+    e_times = []
+    for _ in range(args.steps):
+        lib.irwls_l2_flush(512 << 20)
+        t0 = time.perf_counter()
+        libc.srand(1)
+        lib.initMemory(1, args.budget)
+        cp = lib.SGMA(hd.struct, p)
+        wp = lib.IRWLSpar(hd.struct, cp, p)
+        if not cp or not wp:
+            raise SystemExit("e2e training failed: " + lib.irwls_last_error_message().decode())
+        e_times.append(time.perf_counter() - t0)
+        got = np.ctypeslib.as_array(cp, shape=(args.budget,)).copy()
+    h1, d1 = C.c_longlong(), C.c_longlong()
+    lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
+    assert np.array_equal(got, ref_cent), "end-to-end run selected different centroids"
+    return {"value": round(statistics.mean(e_times), 3), "unit": "s",
+            "h2d_bytes_per_step": int((h1.value - h0.value) // args.steps),
+            "d2h_bytes_per_step": int((d1.value - d0.value) // args.steps)}
+
+
+def primal_objective(hd, cent, w, gamma, cost, f):
+    """Budgeted primal 1/2 w^T (K_mm + 1e-5 I) w + C sum_i max(0, 1 - y_i f_i)
+    in FP64 on the host (f = K_nm w from the library's prediction path)."""
+    import numpy as np
+
+    from libirwls_gb300 import _abi
+
+    rows, y, q = _abi.dataset_rows(hd.struct, hd.n_rows)
+    d = max(int(r[0].max()) for r in rows if len(r[0])) + 1
+    Xc = np.zeros((len(cent), d))
+    for k, c in enumerate(cent):
+        Xc[k, rows[c][0]] = rows[c][1]
+    qc = q[cent]
+    Kmm = np.exp(-gamma * (qc[:, None] + qc[None, :] - 2.0 * Xc @ Xc.T)) + 1e-5 * np.eye(len(cent))
+    return float(0.5 * w @ Kmm @ w + cost * np.maximum(0.0, 1.0 - y[:hd.l] * f).sum())
+
+
+def quality(lib, hd, p, cent, w):
+    """Primal objective on the training rows and accuracy on the held-out
+    rows (labelled by the training set's network) of one trained model."""
+    import numpy as np
+
+    from libirwls_gb300 import _abi, synth
+
+    te = synth.budgeted_test_set(20000)
+    ht = _abi.build_dataset(te.indptr, te.indices, te.values, te.y, with_means=False)
+    c = np.ascontiguousarray(cent, dtype=np.int32)
+    ww = np.ascontiguousarray(w)
+    mdl = lib.calculateBudgetedModel(p, hd.struct, c.ctypes.data_as(PI), ww.ctypes.data_as(PD))
+    soft = np.ctypeslib.as_array(lib.softTest(hd.struct, mdl, _abi.make_predict_properties(soft=1)),
+                                 shape=(hd.l,)).copy()
+    pred = np.ctypeslib.as_array(lib.test(ht.struct, mdl, _abi.make_predict_properties(soft=0)),
+                                 shape=(ht.l,)).copy()
+    lib.freeModel(mdl)
+    return primal_objective(hd, c, ww, GAMMA, COST, soft), float((pred == te.y).mean())
+
+
+def breakdown(run):
+    return {k: round(v[0], 4) for k, v in run["prof"].items()}
+
+
 def run_ours(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -243,209 +377,111 @@ def run_ours(args):
     res = lib.irwls_resident_upload(hd.struct, p, 1)
     if not res:
         raise SystemExit(lib.irwls_last_error_message().decode())
-    cent = np.zeros(args.budget, np.int32)
-    w = np.zeros(args.budget)
-
-    def barrier():
+    forms = {"both": (0, 1), "plain": (0,), "mixed": (1,)}[args.form]
+    runs, cents, weights = {}, {}, {}
+    for prec in forms:
+        cent = np.zeros(args.budget, np.int32)
+        w = np.zeros(args.budget)
         if world > 1:
             import torch.distributed as dist
 
             dist.barrier()
-
-    def step():
-        libc.srand(1)
-        rc = lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD))
-        if rc != 0:
-            raise SystemExit("training failed: " + lib.irwls_last_error_message().decode())
-
-    for _ in range(args.warmup):
-        step()
-    lib.irwls_profile_enable(1)
-    lib.irwls_profile_reset()
-    launches0 = lib.irwls_kernel_launches()
-    clocks = Clocks(local)
-    times = []
-    barrier()
-    clocks.start()
-    for _ in range(args.steps):
-        lib.irwls_l2_flush(512 << 20)
-        lib.irwls_timer_start()
-        step()
-        times.append(lib.irwls_timer_stop() / 1000.0)
-    clk = clocks.stop()
-    barrier()
-    launches = lib.irwls_kernel_launches() - launches0
-    ms_g, n_g = C.c_double(), C.c_longlong()
-    lib.irwls_profile_read(0, C.byref(ms_g), C.byref(n_g))
-    ms_gram, n_gram = C.c_double(), C.c_longlong()
-    lib.irwls_profile_read(1, C.byref(ms_gram), C.byref(n_gram))
-    lib.irwls_profile_enable(0)
-    iters, nact = C.c_int(), C.c_int()
-    lib.irwls_last_run_info(C.byref(iters), C.byref(nact))
-    step_s = statistics.mean(times)
+        headline = prec == forms[-1]
+        runs[prec] = timed_trainings(lib, libc, res, p, args, cent, w, prec, Clocks(local) if headline else None)
+        cents[prec], weights[prec] = cent, w
+    lib.irwls_resident_free(res)
+    head = forms[-1]
+    step_s = runs[head]["s"]
     if world > 1:
         import torch
         import torch.distributed as dist
 
+        dist.barrier()
         t = torch.tensor([step_s])
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_s = float(t.item())
-
-    # roofline of the SGMA score GEMM: 2*l*s*64 flops at order s, s = 2..m-1
-    flops_per_pass = sum(2.0 * args.rows * s * 64 for s in range(2, args.budget))
-    gemm_s = ms_g.value / 1000.0 / max(args.steps, 1)
-    achieved = flops_per_pass / gemm_s / 1e12 if gemm_s > 0 else 0.0
-    peak = lib.irwls_fp64_peak_tflops(5)
-    roofline = {"bound": "fp64", "kernel": "sgma_gemm_kernel", "achieved": round(achieved, 4),
-                "peak": round(peak, 4), "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
-                "traffic": None,
-                "peak_source": "measured live: FP64 FMA-chain probe of the library (irwls_fp64_peak_tflops); "
-                               "MEASURED_PEAKS.json has no FP64 figure",
-                "launches_per_step": int(n_g.value // max(args.steps, 1)),
-                "share_of_step": round(gemm_s / step_s, 4),
-                "gram_share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / step_s, 4),
-                "gram_tflops": gram_rate(lib, ms_gram.value, args.steps),
-                "breakdown_s": profile_breakdown(lib, args.steps)}
-
-    # end to end through the reference-facing API with host buffers
-    e2e = None
-    if not args.no_e2e:
-        h0, d0 = C.c_longlong(), C.c_longlong()
-        lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
-        e_times = []
-        for _ in range(args.steps):
-            lib.irwls_l2_flush(512 << 20)
-            t0 = time.perf_counter()
-            libc.srand(1)
-            lib.initMemory(1, args.budget)
-            cp = lib.SGMA(hd.struct, p)
-            wp = lib.IRWLSpar(hd.struct, cp, p)
-            if not cp or not wp:
-                raise SystemExit("e2e training failed: " + lib.irwls_last_error_message().decode())
-            e_times.append(time.perf_counter() - t0)
-            e2e_cent = np.ctypeslib.as_array(cp, shape=(args.budget,)).copy()
-        h1, d1 = C.c_longlong(), C.c_longlong()
-        lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
-        assert np.array_equal(e2e_cent, cent), "end-to-end run selected different centroids"
-        e2e = {"value": round(statistics.mean(e_times), 3), "unit": "s",
-               "h2d_bytes_per_step": int((h1.value - h0.value) // args.steps),
-               "d2h_bytes_per_step": int((d1.value - d0.value) // args.steps)}
-    mixed = None if args.no_mixed else measure_mixed(lib, libc, res, hd, p, args, cent, w, step_s)
-    lib.irwls_resident_free(res)
-
+    e2e = {prec: None if args.no_e2e else end_to_end(lib, libc, hd, p, args, prec, cents[prec]) for prec in forms}
+    lib.irwls_set_precision(0)
     if rank != 0:
         return
-    base = None if args.no_cpu else cpu_baseline(hd, args.budget, iters.value)
-    line = {"metric": METRIC, "value": round(step_s, 3), "unit": "s", "n_gpus": world if world > 1 else args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1000, 1),
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+
+    peaks, peak_src = measured_peaks()
+    fp64_peak = lib.irwls_fp64_peak_tflops(5)
+    fp32_peak = lib.irwls_fp32_peak_tflops(5)
+    sgma_flops = sum(2.0 * args.rows * s * 64 for s in range(2, args.budget))
+    kernels = {}
+    if 0 in runs:
+        g_s = runs[0]["prof"]["sgma_scores"][0]
+        ach = sgma_flops / g_s / 1e12 if g_s > 0 else 0.0
+        kernels["sgma_gemm_kernel (plain FP64)"] = {
+            "bound": "fp64", "achieved": round(ach, 4), "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
+            "frac": round(ach / fp64_peak, 4) if fp64_peak else None,
+            "share_of_step": round(g_s / runs[0]["s"], 4)}
+        gr_s = runs[0]["prof"]["irwls_gram"][0]
+        ach = runs[0]["gram_flops"] / gr_s / 1e12 if gr_s > 0 else 0.0
+        kernels["gram_kernel (plain FP64)"] = {
+            "bound": "fp64", "achieved": round(ach, 4), "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
+            "frac": round(ach / fp64_peak, 4) if fp64_peak else None,
+            "share_of_step": round(gr_s / runs[0]["s"], 4)}
+    if 1 in runs:
+        gr_s = runs[1]["prof"]["irwls_gram"][0]
+        ach = runs[1]["gram_flops"] / gr_s / 1e12 if gr_s > 0 else 0.0
+        df_peak = fp32_peak / 12.0
+        kernels["gram_df_kernel (precision form, double-float)"] = {
+            "bound": "fp32 issue (12 FP32 instructions per FP64-equivalent product-sum)",
+            "achieved": round(ach, 4), "peak": round(df_peak, 4), "unit": "TFLOP/s FP64-equivalent",
+            "frac": round(ach / df_peak, 4) if df_peak else None,
+            "share_of_step": round(gr_s / runs[1]["s"], 4)}
+        sc_s = runs[1]["prof"]["sgma_scores"][0]
+        ach = 3 * sgma_flops / sc_s / 1e12 if sc_s > 0 else 0.0
+        kernels["sgma_tc_score_kernel (precision form, tcgen05 split BF16)"] = {
+            "bound": "tensor", "achieved": round(ach, 2), "peak": peaks.get("bf16_tflops"),
+            "unit": "TFLOP/s (3 bf16 products per FP32-accumulated product)",
+            "frac": round(ach / peaks["bf16_tflops"], 4) if peaks.get("bf16_tflops") else None,
+            "peak_source": peak_src + " bf16 burst", "share_of_step": round(sc_s / runs[1]["s"], 4)}
+    # roofline: the dominant kernel of the headline form
+    if head == 1:
+        k = kernels["gram_df_kernel (precision form, double-float)"]
+        roofline = dict(k, kernel="gram_df_kernel", traffic=None,
+                        peak_source="measured live: FP32 FMA-chain probe of the library "
+                                    "(irwls_fp32_peak_tflops = %.1f TFLOP/s) / 12" % fp32_peak)
+    else:
+        k = kernels["sgma_gemm_kernel (plain FP64)"]
+        roofline = dict(k, kernel="sgma_gemm_kernel", traffic=None,
+                        peak_source="measured live: FP64 FMA-chain probe of the library "
+                                    "(irwls_fp64_peak_tflops); MEASURED_PEAKS.json has no FP64 figure")
+
+    accuracy, value, form = None, step_s, ("plain FP64" if head == 0 else "precision (mixed)")
+    if forms == (0, 1):
+        obj = {prec: quality(lib, hd, p, cents[prec], weights[prec]) for prec in forms}
+        rel = abs(obj[1][0] - obj[0][0]) / abs(obj[0][0])
+        dacc = obj[1][1] - obj[0][1]
+        ok = rel <= PRIMAL_BAR and abs(dacc) <= ACC_BAR
+        accuracy = {"primal_rel_err_vs_plain": rel, "primal_plain": obj[0][0], "primal_mixed": obj[1][0],
+                    "test_acc_plain": obj[0][1], "test_acc_mixed": obj[1][1], "test_acc_change": dacc,
+                    "centroids_identical": int((cents[1] == cents[0]).sum()),
+                    "bars": {"primal_rel_err": PRIMAL_BAR, "test_acc_change": ACC_BAR}, "meets_bars": ok}
+        if not ok:
+            # the precision form missed the bar: report the plain form as the value
+            head, value, form = 0, runs[0]["s"], "plain FP64 (precision form missed the accuracy bar)"
+    plain = None
+    if 0 in runs:
+        plain = {"value": round(runs[0]["s"], 3), "unit": "s", "e2e": e2e[0], "launches": int(runs[0]["launches"]),
+                 "breakdown_s": breakdown(runs[0]), "par_iterations": runs[0]["iters"],
+                 "active_rows_final": runs[0]["nact"]}
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "s", "n_gpus": world if world > 1 else args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1000, 1),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if head == 0 else "bf16x3 (SGMA scores) + f32x2 (IRWLSpar Gram) + f64 (factors, solves)",
             "data": "synthetic (seeded generator)",
-            "config": config(args, {"par_iterations": iters.value, "active_rows_final": nact.value}),
-            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": base,
-            "clocks": clk, "mixed": mixed}
+            "config": config(args, {"form": form, "par_iterations": runs[head]["iters"],
+                                    "active_rows_final": runs[head]["nact"]}),
+            "e2e": e2e[head], "gpu_launches": int(runs[head]["launches"]), "roofline": roofline,
+            "cpu_baseline": None if args.no_cpu else cpu_baseline(hd, args.budget, runs[head]["iters"]),
+            "clocks": runs[forms[-1]]["clocks"], "breakdown_s": breakdown(runs[head]),
+            "speedup_vs_plain_fp64": round(runs[0]["s"] / value, 2) if 0 in runs else None,
+            "accuracy": accuracy, "plain_fp64": plain, "kernels": kernels}
     print(json.dumps(line), flush=True)
-
-
-PROFILE_SLOTS = {"sgma_scores": 0, "sgma_candidate_solves": 5, "sgma_select_and_factor": 6, "irwls_gram": 1,
-                 "irwls_cholesky": 3}
-
-
-def profile_breakdown(lib, steps):
-    """Seconds per step of each profiled stage (CUDA events on the library's
-    stream around the stage's launches)."""
-    out = {}
-    for name, slot in PROFILE_SLOTS.items():
-        ms, n = C.c_double(), C.c_longlong()
-        lib.irwls_profile_read(slot, C.byref(ms), C.byref(n))
-        out[name] = round(ms.value / 1000.0 / max(steps, 1), 4)
-    return out
-
-
-def gram_rate(lib, ms_total, steps):
-    """Algorithmic TFLOP/s of the IRWLSpar Gram updates of the last training
-    (active_rows * (m + 1) * m per iteration over the profiled kernel time)."""
-    per_step_s = ms_total / 1000.0 / max(steps, 1)
-    return round(lib.irwls_last_gram_flops() / per_step_s / 1e12, 3) if per_step_s > 0 else None
-
-
-def primal_objective(hd, cent, w, gamma, cost, f):
-    """Budgeted primal 1/2 w^T (K_mm + 1e-5 I) w + C sum_i max(0, 1 - y_i f_i)
-    in FP64 on the host (f = K_nm w from the library's prediction path)."""
-    import numpy as np
-
-    from libirwls_gb300 import _abi
-
-    rows, y, q = _abi.dataset_rows(hd.struct, hd.n_rows)
-    d = max(int(r[0].max()) for r in rows if len(r[0])) + 1
-    Xc = np.zeros((len(cent), d))
-    for k, c in enumerate(cent):
-        Xc[k, rows[c][0]] = rows[c][1]
-    qc = q[cent]
-    Kmm = np.exp(-gamma * (qc[:, None] + qc[None, :] - 2.0 * Xc @ Xc.T)) + 1e-5 * np.eye(len(cent))
-    return float(0.5 * w @ Kmm @ w + cost * np.maximum(0.0, 1.0 - y[:hd.l] * f).sum())
-
-
-def measure_mixed(lib, libc, res, hd, p, args, cent_plain, w_plain, plain_s):
-    """Precision form (split-BF16 tensor-core SGMA scores) on the same resident
-    workload: train seconds, centroid agreement with the plain run, relative
-    primal-objective difference and held-out accuracy change."""
-    import numpy as np
-
-    from libirwls_gb300 import _abi, synth
-
-    cent = np.zeros(args.budget, np.int32)
-    w = np.zeros(args.budget)
-    lib.irwls_set_precision(1)
-    for _ in range(args.warmup):
-        libc.srand(1)
-        lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD))
-    lib.irwls_profile_enable(1)
-    lib.irwls_profile_reset()
-    times = []
-    for _ in range(args.steps):
-        lib.irwls_l2_flush(512 << 20)
-        lib.irwls_timer_start()
-        libc.srand(1)
-        rc = lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD))
-        times.append(lib.irwls_timer_stop() / 1000.0)
-        if rc != 0:
-            raise SystemExit("mixed training failed: " + lib.irwls_last_error_message().decode())
-    ms_g, n_g = C.c_double(), C.c_longlong()
-    lib.irwls_profile_read(0, C.byref(ms_g), C.byref(n_g))
-    ms_gram, n_gram = C.c_double(), C.c_longlong()
-    lib.irwls_profile_read(1, C.byref(ms_gram), C.byref(n_gram))
-    breakdown = profile_breakdown(lib, args.steps)
-    lib.irwls_profile_enable(0)
-    lib.irwls_set_precision(0)
-    te = synth.budgeted_test_set(20000)
-    ht = _abi.build_dataset(te.indptr, te.indices, te.values, te.y, with_means=False)
-    out = {}
-    for name, c, ww in (("plain", cent_plain, w_plain), ("mixed", cent, w)):
-        c = np.ascontiguousarray(c, dtype=np.int32)
-        ww = np.ascontiguousarray(ww)
-        mdl = lib.calculateBudgetedModel(p, hd.struct, c.ctypes.data_as(PI), ww.ctypes.data_as(PD))
-        soft = np.ctypeslib.as_array(lib.softTest(hd.struct, mdl, _abi.make_predict_properties(soft=1)),
-                                     shape=(hd.l,)).copy()
-        pred = np.ctypeslib.as_array(lib.test(ht.struct, mdl, _abi.make_predict_properties(soft=0)),
-                                     shape=(ht.l,)).copy()
-        out[name] = (primal_objective(hd, c, ww, GAMMA, COST, soft), float((pred == te.y).mean()))
-    value = statistics.mean(times)
-    flops = sum(3 * 2.0 * args.rows * s * 64 for s in range(2, args.budget))
-    gemm_s = ms_g.value / 1000.0 / max(args.steps, 1)
-    return {"form": "SGMA scores in split BF16 on tcgen05 (Q = K_nm L^-T formulation); IRWLSpar Gram in "
-                    "double-float FP32 pairs; FP64 factors, solves, residuals and convergence tests",
-            "value": round(value, 3), "unit": "s", "speedup_vs_plain_fp64": round(plain_s / value, 2),
-            "centroids_identical": int((cent == cent_plain).sum()), "budget": args.budget,
-            "primal_rel_err": abs(out["mixed"][0] - out["plain"][0]) / abs(out["plain"][0]),
-            "test_acc_plain": out["plain"][1], "test_acc_mixed": out["mixed"][1],
-            "test_acc_change": out["mixed"][1] - out["plain"][1],
-            "score_gemm": {"kernel": "sgma_tc_score_kernel",
-                           "tflops_3_products": round(flops / gemm_s / 1e12, 2) if gemm_s > 0 else None,
-                           "share_of_step": round(gemm_s / value, 4)},
-            "breakdown_s": breakdown,
-            "gram": {"kernel": "df_pack_kernel + gram_df_kernel",
-                     "tflops_fp64_equivalent": gram_rate(lib, ms_gram.value, args.steps),
-                     "share_of_step": round(ms_gram.value / 1000.0 / max(args.steps, 1) / value, 4)}}
 
 
 # ----------------------------------------------------------------------------

@@ -77,6 +77,9 @@ double irwls_timer_stop(void);
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-chain
  * kernel: the roofline denominator of the FP64 kernels. */
 double irwls_fp64_peak_tflops(int reps);
+/* FP32 FMA throughput of the device (TFLOP/s, one FMA = 2 flops), measured
+ * the same way: the denominator of the precision form's double-float Gram. */
+double irwls_fp32_peak_tflops(int reps);
 
 /* Cholesky factorization and solve of one system on the GPU that allocates
  * no memory; no counterpart in the reference. For callers that cannot let a

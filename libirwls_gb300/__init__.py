@@ -49,6 +49,7 @@ def load() -> C.CDLL:
         "irwls_timer_start": (C.c_int, []),
         "irwls_timer_stop": (C.c_double, []),
         "irwls_fp64_peak_tflops": (C.c_double, [C.c_int]),
+        "irwls_fp32_peak_tflops": (C.c_double, [C.c_int]),
         "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "irwls_last_gram_flops": (C.c_double, []),
         "irwls_tc_status": (C.c_int, []),

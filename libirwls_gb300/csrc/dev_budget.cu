@@ -153,10 +153,10 @@ __global__ void __launch_bounds__(128) cand_rows_kernel(KView X, const int *__re
 }
 
 // Partial W^T over one chunk of WT columns of Linv: item (eb, tc) covers rows
-// e in [32 eb, 32 eb + 32) and t in [WT tc, WT tc + WT) (t <= e only, Linv is
+// e in [WE eb, WE eb + WE) and t in [WT tc, WT tc + WT) (t <= e only, Linv is
 // zero above); part[(tc * 64 + c) * ldp + e]. Rows of Linv and KN stream
 // through a cp.async double buffer of WK columns.
-constexpr int WE = 32, WT = 128, WK = 16;
+constexpr int WE = 16, WT = 64, WK = 16;
 __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ Linv, int ldi,
                                                      const double *__restrict__ KN, int ldz, int s,
                                                      double *__restrict__ part, int ldp) {
@@ -166,12 +166,8 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
     const int t1 = min(min(t0 + WT, e0 + WE), s);
     __shared__ __align__(16) double Ls[2][WE][WK + 1];
     __shared__ __align__(16) double Ks[2][NCAND][WK + 1];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    double acc[2][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;  // row e0 + ty, candidates tx + 16 b
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
     auto load = [&](int buf, int t) {
         for (int u = tid; u < (WE + NCAND) * WK; u += 256) {
             const int r = u / WK, k = u % WK;
@@ -203,22 +199,16 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < WK; ++k) {
-            const double l0 = Ls[buf][ty][k], l1 = Ls[buf][ty + 16][k];
+            const double l0 = Ls[buf][ty][k];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const double kv = Ks[buf][tx + 16 * b][k];
-                acc[0][b] = fma(l0, kv, acc[0][b]);
-                acc[1][b] = fma(l1, kv, acc[1][b]);
-            }
+            for (int b = 0; b < 4; ++b) acc[b] = fma(l0, Ks[buf][tx + 16 * b][k], acc[b]);
         }
         __syncthreads();
     }
+    const int e = e0 + ty;
+    if (e < s) {
 #pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        const int e = e0 + ty + 16 * a;
-        if (e >= s) continue;
-#pragma unroll
-        for (int b = 0; b < 4; ++b) part[((size_t)tc * NCAND + tx + 16 * b) * ldp + e] = acc[a][b];
+        for (int b = 0; b < 4; ++b) part[((size_t)tc * NCAND + tx + 16 * b) * ldp + e] = acc[b];
     }
 }
 
@@ -414,17 +404,38 @@ __global__ void __launch_bounds__(NCAND) sgma_select_kernel(const double *__rest
 // Appends centroid s: KSC column (separate launch), and row s of L:
 // L[s, :s] = L^-1 k_C(c_s) (the forward result of the winning candidate),
 // L[s, s] = sqrt(k(c_s, c_s) + jitter - |L[s, :s]|^2)  (src/budgeted-train.c:247-279).
-__global__ void sgma_factor_kernel(KView X, int s, const int *__restrict__ cent, const int *__restrict__ best,
-                                   const double *__restrict__ W, int ldz, double *__restrict__ L, int ldL) {
+// tree = 1 (precision form): |L[s, :s]|^2 by a fixed-order block reduction
+// instead of the reference's left-to-right sum.
+__global__ void __launch_bounds__(128) sgma_factor_kernel(KView X, int s, const int *__restrict__ cent,
+                                                          const int *__restrict__ best, const double *__restrict__ W,
+                                                          int ldz, double *__restrict__ L, int ldL, int tree) {
     extern __shared__ double sA[];
+    __shared__ double red[128];
     const int gc = cent[s];
     for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sA[t] = X.X[(size_t)gc * X.ld + t];
     __syncthreads();
+    double ss = 0.0;
     if (s >= 2) {
         const int bb = best[0];
-        for (int t = threadIdx.x; t < s; t += blockDim.x) L[(size_t)s * ldL + t] = W[(size_t)bb * ldz + t];
+        for (int t = threadIdx.x; t < s; t += blockDim.x) {
+            const double v = W[(size_t)bb * ldz + t];
+            L[(size_t)s * ldL + t] = v;
+            ss = fma(v, v, ss);
+        }
     }
+    red[threadIdx.x] = ss;
     __syncthreads();
+    if (tree && s >= 2) {
+        for (int o = 64; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            const double kcc = kentry(X, sA, X.q[gc], gc);
+            L[(size_t)s * ldL + s] = sqrt(__dsub_rn(__dadd_rn(kcc, 0.00001), red[0]));
+        }
+        return;
+    }
     if (threadIdx.x == 0) {
         const double kcc = kentry(X, sA, X.q[gc], gc);
         if (s == 0) {
@@ -802,7 +813,7 @@ extern "C" int irwls_sgma_first(const irwls_dev_set *X, int l, int *d_cent, doub
     if (irwls_dev_kernel_block_t(X, d_cent, 1, X, nullptr, l, d_KSC, l, 0)) return -2;
     const size_t smem = (size_t)X->ld * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), 0, d_cent, nullptr, nullptr, 0, d_L, ldL);
+    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), 0, d_cent, nullptr, nullptr, 0, d_L, ldL, 0);
     IRWLS_LAUNCH_CHECK("sgma_factor");
     return 0;
 }
@@ -834,13 +845,6 @@ extern "C" int irwls_sgma_score(const irwls_dev_set *X, int l, const int *d_cand
 }
 
 extern "C" int irwls_sgma_partials(int l) { return sgma_gemm_grid(l); }
-
-extern "C" int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, const int *d_cand, int s,
-                                   int *d_cent, int *d_best, double *d_bestval) {
-    sgma_select_kernel<<<1, NCAND, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval);
-    IRWLS_LAUNCH_CHECK("sgma_select");
-    return 0;
-}
 
 // Precision form: W = K_CN L^-T for the 64 candidates of step s, eta and the
 // bf16 split of W. wpart: irwls_sgma_wpart_count(m) doubles.
@@ -890,7 +894,7 @@ extern "C" int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cen
                                  int ldz, double *d_L, int ldL) {
     const size_t smem = (size_t)X->ld * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL);
+    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL, 1);
     IRWLS_LAUNCH_CHECK("sgma_factor");
     return 0;
 }
@@ -910,7 +914,7 @@ extern "C" int irwls_sgma_extend(const irwls_dev_set *X, int l, int s, const int
     if (irwls_dev_kernel_block_t(X, d_cent + s, 1, X, nullptr, l, d_KSC + (size_t)s * l, l, 0)) return -2;
     const size_t smem = (size_t)X->ld * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL);
+    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL, 0);
     IRWLS_LAUNCH_CHECK("sgma_factor");
     return 0;
 }

@@ -408,7 +408,48 @@ __global__ void fp64_probe_kernel(double *out, int iters) {
     for (int k = 0; k < 8; ++k) s += a[k];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+__global__ void fp32_probe_kernel(float *out, int iters) {
+    float a[8];
+    for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-3f + k;
+    const float b = 0.9999f, c = 1e-4f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], b, c);
+    }
+    float s = 0;
+    for (int k = 0; k < 8; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 }  // namespace
+
+// FP32 FMA throughput in TFLOP/s (one FMA = 2 flops), best of `reps` timed
+// launches: the denominator of the double-float Gram, whose product-sum costs
+// twelve FP32 instructions.
+extern "C" double irwls_fp32_peak_tflops(int reps) {
+    if (irwls_dev_init()) return 0.0;
+    const int blocks = 4 * g_num_sms, threads = 256, iters = 100000;
+    float *d = nullptr;
+    if (irwls_dev_malloc((void **)&d, (size_t)blocks * threads * sizeof(float))) return 0.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 0.0;
+    fp32_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
+    for (int r = 0; r < reps; ++r) {
+        cudaEventRecord(e0, g_stream);
+        fp32_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
+        cudaEventRecord(e1, g_stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double tf = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+        if (tf > best) best = tf;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    return best;
+}
 
 // FP64 FMA throughput in TFLOP/s, best of `reps` timed launches.
 extern "C" double irwls_fp64_peak_tflops(int reps) {

@@ -419,12 +419,12 @@ __device__ __forceinline__ void kentry8_f32(const KViewF &B, const float *a, int
 
 // SGMA scores in the precision form: R = Q W^T on the tensor cores (rows of
 // the CTA's 128-row tile x 64 candidates), r = R - k(cand, row) in FP32, and
-// the per-candidate sums of r^2 over the tile (in FP64) to part[tile][64].
+// the per-candidate sums of r^2 over the tile (FP32 tree) to part[tile][64].
 __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int l, const int *__restrict__ cand,
                                                                    const __nv_bfloat16 *Qhi, const __nv_bfloat16 *Qlo,
                                                                    int ldq, const __nv_bfloat16 *Whi,
                                                                    const __nv_bfloat16 *Wlo, int kst,
-                                                                   double *__restrict__ part, int *flags) {
+                                                                   float *__restrict__ part, int *flags) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
@@ -441,9 +441,11 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int
     const uint32_t tmem = tmem_slot;
     const bool ok = tc_mainloop<64>(smem, mbar, tmem, Qhi, Qlo, ldq, m0, l, Whi, Wlo, ldq, 0, 64, 0, kst);
     if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
-    // residual squares of this thread's row into the (now free) stage buffer
-    float *sr = (float *)smem;  // [128][65]
+    // residual squares of this thread's row, summed per candidate over the
+    // tile: warp shuffles (FP32 tree) then the four warps in a fixed order
+    __shared__ float wred[TC_THREADS / 32][64];
     const int row = m0 + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c0 = 0; c0 < 64; c0 += 8) {
         float v[8], kv[8];
         if (ok) tc_ld8(tmem, c0, v);
@@ -457,16 +459,56 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int
                 const float r = v[j] - kv[j];
                 r2 = r * r;
             }
-            sr[threadIdx.x * 65 + c0 + j] = r2;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+            if (lane == 0) wred[warp][c0 + j] = r2;
         }
     }
     __syncthreads();
-    if (threadIdx.x < 64) {
-        double acc = 0.0;
-        for (int r = 0; r < TC_BM; ++r) acc += (double)sr[r * 65 + threadIdx.x];
-        part[(size_t)blockIdx.x * 64 + threadIdx.x] = acc;
-    }
+    if (threadIdx.x < 64)
+        part[(size_t)blockIdx.x * 64 + threadIdx.x] =
+            (wred[0][threadIdx.x] + wred[1][threadIdx.x]) + (wred[2][threadIdx.x] + wred[3][threadIdx.x]);
     tc_teardown<64>(tmem);
+}
+
+// Scores of the precision form: per candidate, the tile sums in 16 strided
+// groups with Kahan-compensated FP32 adds, the 16 group sums in FP64 in a
+// fixed order, score = sum / eta; strict ">" argmax, first index wins.
+__global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__restrict__ part, int nblk,
+                                                              const double *__restrict__ eta,
+                                                              const int *__restrict__ cand, int s, int *cent,
+                                                              int *best, double *bestval) {
+    __shared__ double grp[16][64];
+    __shared__ double sc[64];
+    const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
+    float sum = 0.f, comp = 0.f;
+    for (int b = g; b < nblk; b += 16) {
+        const float y = __fsub_rn(part[(size_t)b * 64 + c], comp);
+        const float t = __fadd_rn(sum, y);
+        comp = __fsub_rn(__fsub_rn(t, sum), y);
+        sum = t;
+    }
+    grp[g][c] = (double)sum - (double)comp;
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        double v = 0.0;
+        for (int k = 0; k < 16; ++k) v += grp[k][threadIdx.x];
+        const double et = eta[threadIdx.x];
+        sc[threadIdx.x] = (et > 0.0) ? v / et : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double val = sc[0];
+        int bb = 0;
+        for (int i = 1; i < 64; ++i)
+            if (sc[i] > val) {
+                val = sc[i];
+                bb = i;
+            }
+        cent[s] = cand[bb];
+        best[0] = bb;
+        bestval[s] = val;
+    }
 }
 
 // New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, one warp
@@ -488,9 +530,10 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
     const float qa = X.q[gc];
     const int lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
-    for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += gridDim.x * warps) {
+    const int stride = gridDim.x * warps;
+    auto partial = [&](int i, float &acc, float &kd) {
         const float4 *qrow = (const float4 *)(Qf + (size_t)i * ldq);
-        float acc = 0.f;
+        acc = 0.f;
         for (int j4 = lane; j4 < s4 / 4; j4 += 32) {
             const float4 qv = qrow[j4];
             const float4 lv = *(const float4 *)(l2 + 4 * j4);
@@ -499,7 +542,7 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
             acc = fmaf(qv.z, lv.z, acc);
             acc = fmaf(qv.w, lv.w, acc);
         }
-        float kd = 0.f;
+        kd = 0.f;
         if (X.mode == IRWLS_K_RAW_RBF) {
             const float *b = X.X + (size_t)i * X.ld;
             for (int t = lane; t < X.width; t += 32) {
@@ -509,20 +552,33 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
         } else {
             for (int p = X.rp[i] + lane; p < X.rp[i + 1]; p += 32) kd = fmaf(X.cv[p], sc[X.ci[p]], kd);
         }
+    };
+    auto finish = [&](int i, float acc, float kd) {
+        float kv;
+        if (X.mode == IRWLS_K_RAW_RBF) kv = __expf(X.ng * kd);
+        else if (X.mode == IRWLS_K_LINEAR) kv = kd;
+        else kv = __expf(X.ng * fmaxf(qa + X.q[i] - 2.f * kd, 0.f));
+        const float q = (kv - acc) * inv_l3;
+        Qf[(size_t)i * ldq + s] = q;
+        const __nv_bfloat16 h = __float2bfloat16_rn(q);
+        Qhi[(size_t)i * ldq + s] = h;
+        Qlo[(size_t)i * ldq + s] = __float2bfloat16_rn(q - __bfloat162float(h));
+    };
+    // two rows in flight per warp
+    for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += 2 * stride) {
+        const int i2 = i + stride;
+        float a0, k0, a1 = 0.f, k1 = 0.f;
+        partial(i, a0, k0);
+        if (i2 < l) partial(i2, a1, k1);
         for (int o = 16; o > 0; o >>= 1) {
-            acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            kd += __shfl_xor_sync(0xffffffffu, kd, o);
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            k0 += __shfl_xor_sync(0xffffffffu, k0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            k1 += __shfl_xor_sync(0xffffffffu, k1, o);
         }
         if (lane == 0) {
-            float kv;
-            if (X.mode == IRWLS_K_RAW_RBF) kv = __expf(X.ng * kd);
-            else if (X.mode == IRWLS_K_LINEAR) kv = kd;
-            else kv = __expf(X.ng * fmaxf(qa + X.q[i] - 2.f * kd, 0.f));
-            const float q = (kv - acc) * inv_l3;
-            Qf[(size_t)i * ldq + s] = q;
-            const __nv_bfloat16 h = __float2bfloat16_rn(q);
-            Qhi[(size_t)i * ldq + s] = h;
-            Qlo[(size_t)i * ldq + s] = __float2bfloat16_rn(q - __bfloat162float(h));
+            finish(i, a0, k0);
+            if (i2 < l) finish(i2, a1, k1);
         }
     }
 }
@@ -571,7 +627,7 @@ extern "C" void irwls_f32_mirror_free(void *h) {
 }
 
 extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
-                                   const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, double *d_part) {
+                                   const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, float *d_part) {
     const int kst = (s + TC_BK - 1) / TC_BK;
     const size_t smem = 2 * TcStage<64>::BYTES + 1024 + (size_t)64 * X->ld * sizeof(float);
     if (smem > 220 * 1024) {
@@ -589,6 +645,13 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
 }
 
 extern "C" int irwls_sgma_tc_partials(int l) { return ceil_div(l, TC_BM); }
+
+extern "C" int irwls_sgma_tc_select(const float *d_part, int nblk, const double *d_eta, const int *d_cand, int s,
+                                    int *d_cent, int *d_best, double *d_bestval) {
+    sgma_select_f32_kernel<<<1, 1024, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval);
+    IRWLS_LAUNCH_CHECK("sgma_select_f32");
+    return 0;
+}
 
 // lrow: row s of L in FP32 (s values, then 1 / L3), from irwls_sgma_linv_update.
 extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s,

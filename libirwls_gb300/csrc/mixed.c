@@ -32,12 +32,12 @@ int irwls_sgma_linv_update(const double *d_L, int ldL, double *d_Linv, int ldi, 
                            float *d_lrow);
 size_t irwls_sgma_wpart_count(int m);
 size_t irwls_sgma_lpart_count(int m);
-int irwls_sgma_select_n(const double *d_part, int nblk, const double *d_eta, const int *d_cand, int s, int *d_cent,
-                        int *d_best, double *d_bestval);
+int irwls_sgma_tc_select(const float *d_part, int nblk, const double *d_eta, const int *d_cand, int s, int *d_cent,
+                         int *d_best, double *d_bestval);
 int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W, int ldz,
                       double *d_L, int ldL);
 int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
-                        const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, double *d_part);
+                        const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, float *d_part);
 int irwls_sgma_tc_partials(int l);
 int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const float *lrow, float *Qf,
                    void *Qhi, void *Qlo, int ldq);
@@ -70,8 +70,9 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     const int nblk = irwls_sgma_tc_partials(l);
     int rc = 0;
     int *d_cand = NULL, *d_cent = NULL, *d_best = NULL;
-    double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_part = NULL, *d_val = NULL, *d_Linv = NULL,
-           *d_wpart = NULL, *d_lpart = NULL;
+    double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_val = NULL, *d_Linv = NULL, *d_wpart = NULL,
+           *d_lpart = NULL;
+    float *d_part = NULL;
     float *Qf = NULL, *lrow = NULL;
     void *Qhi = NULL, *Qlo = NULL, *Whi = NULL, *Wlo = NULL;
     void *F = irwls_f32_mirror(X);
@@ -86,7 +87,7 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     rc |= irwls_dev_malloc((void **)&d_W, (size_t)64 * ldz * sizeof(double));
     rc |= irwls_dev_malloc((void **)&d_KN, (size_t)64 * ldz * sizeof(double));
     rc |= irwls_dev_malloc((void **)&d_eta, 64 * sizeof(double));
-    rc |= irwls_dev_malloc((void **)&d_part, (size_t)nblk * 64 * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_part, (size_t)nblk * 64 * sizeof(float));
     rc |= irwls_dev_malloc((void **)&d_val, (size_t)m * sizeof(double));
     rc |= irwls_dev_malloc((void **)&Qf, (size_t)l * ldq * sizeof(float));
     rc |= irwls_dev_malloc(&Qhi, (size_t)l * ldq * 2);
@@ -119,7 +120,7 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
                                       Whi, Wlo, ldq, d_eta);
             rc |= irwls_sgma_tc_score(X, F, l, d_cand + (size_t)s * 64, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
             irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
-            rc |= irwls_sgma_select_n(d_part, nblk, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
+            rc |= irwls_sgma_tc_select(d_part, nblk, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
             rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
             rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq);
