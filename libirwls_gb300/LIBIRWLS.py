@@ -123,6 +123,21 @@ def budgeted_train(data, labels, gamma=1.0, C=1.0, threads=1, size=10, algorithm
     return Classifier(mdl)
 
 
+def set_precision(mode):
+    """Budgeted training's arithmetic for this process: "fp64" (the
+    reference's, the default) or "mixed" (tensor-core SGMA scores and a
+    double-float IRWLS Gram; same loops and random draws). Not part of the
+    reference module."""
+    modes = {"fp64": 0, "mixed": 1}
+    if mode not in modes:
+        raise ValueError("precision must be one of %s" % sorted(modes))
+    _load_lib().irwls_set_precision(modes[mode])
+
+
+def get_precision():
+    return {0: "fp64", 1: "mixed"}[_load_lib().irwls_get_precision()]
+
+
 def predict(classifier, data, labels=None, threads=1, Soft=0, verbose=1):
     """Decision values (Soft=1) or +-1 labels; prints the accuracy when labels
     are given (pythonmodule.c:72-128)."""

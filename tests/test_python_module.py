@@ -120,3 +120,15 @@ def test_module_training_matches_oracle():
     w = H.arr(port.IRWLSpar(dsm, c, pb), 12)
     assert H.rel_err(bclf.weights(), w) < 1e-9
     lib.freeDataset(dsm)
+
+
+def test_precision_switch():
+    assert LIBIRWLS.get_precision() == "fp64"
+    LIBIRWLS.set_precision("mixed")
+    try:
+        assert LIBIRWLS.get_precision() == "mixed"
+        assert load().irwls_get_precision() == 1
+    finally:
+        LIBIRWLS.set_precision("fp64")
+    with pytest.raises(ValueError):
+        LIBIRWLS.set_precision("fp16")
