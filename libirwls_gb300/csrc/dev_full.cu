@@ -8,6 +8,8 @@
 // Kernel tiles and solves are in dev_tiles.cu and dev_chol.cu.
 #include <string.h>
 
+#include <algorithm>
+
 #include "dev_common.cuh"
 
 namespace {
@@ -297,6 +299,10 @@ __global__ void __launch_bounds__(CT) apply_ws_kernel(const int *__restrict__ SW
                                 },
                                 s_scan);
     if (threadIdx.x == 0) cnt[0] = n;
+    // sum |beta change| (the precision form's error bound of this update)
+    __shared__ double red[33];
+    const double l1 = block_sum_ordered(n, [&](int p) { return fabs(cb[p]); }, red);
+    if (threadIdx.x == 0) dbias[1] = l1;
 }
 
 __global__ void __launch_bounds__(CT) norms_kernel(const double *__restrict__ beta, const double *__restrict__ bnew,
@@ -379,7 +385,97 @@ __global__ void fill_ws_kernel(int *SW, int nSW, int *SIN, int nSIN, const int *
     }
 }
 
+// Precision form: the rows whose errors are kept exact (FP64 increments):
+// support vectors, rows with |e_i y_i| < band, and the working set SW.
+// flag[i] says whether row i was exact before; rows entering the set are
+// listed in Snew (their errors must be recomputed) unless `all_exact`.
+// mark: scratch of l ints, zero on entry and on exit.
+__global__ void __launch_bounds__(CT) exact_set_kernel(const double *__restrict__ e, const double *__restrict__ y,
+                                                       const double *__restrict__ beta, int l,
+                                                       const int *__restrict__ SW, int nSW, double band,
+                                                       int all_exact, int *flag, int *mark, int *S, int *Snew,
+                                                       int *counts) {
+    __shared__ int s_scan[CT];
+    for (int k = threadIdx.x; k < nSW; k += CT) mark[SW[k]] = 1;
+    __syncthreads();
+    auto in_set = [&](int i) { return beta[i] != 0.0 || fabs(e[i] * y[i]) < band || mark[i] != 0; };
+    const int nnew = all_exact ? 0
+                               : block_compact(l, [&](int i) { return in_set(i) && flag[i] == 0; },
+                                               [&](int p, int i) { Snew[p] = i; }, s_scan);
+    const int ns = block_compact(l, in_set, [&](int p, int i) { S[p] = i; }, s_scan);
+    for (int i = threadIdx.x; i < l; i += CT) flag[i] = in_set(i) ? 1 : 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < nSW; k += CT) mark[SW[k]] = 0;
+    if (threadIdx.x == 0) {
+        counts[0] = ns;
+        counts[1] = nnew;
+    }
+}
+
+__global__ void gather_kernel(const double *__restrict__ src, const int *__restrict__ idx, int n,
+                              double *__restrict__ dst) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) dst[k] = src[idx[k]];
+}
+
+__global__ void scatter_kernel(const double *__restrict__ src, const int *__restrict__ idx, int n,
+                               double *__restrict__ dst) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) dst[idx[k]] = src[k];
+}
+
+// Precision form: the support vectors (beta != 0 over the l samples) as a
+// compact list with their weights, in index order.
+__global__ void __launch_bounds__(CT) sv_list_kernel(const double *__restrict__ beta, int l, int *lst, double *cb,
+                                                     int *cnt) {
+    __shared__ int s_scan[CT];
+    const int n = block_compact(l, [&](int i) { return beta[i] != 0.0; },
+                                [&](int p, int i) {
+                                    lst[p] = i;
+                                    cb[p] = beta[i];
+                                },
+                                s_scan);
+    if (threadIdx.x == 0) cnt[0] = n;
+}
+
 }  // namespace
+
+// e = y - K(:, SV) beta_SV - b in FP64 over all l rows (the exact error
+// vector that the incremental updates approximate).
+extern "C" int irwls_full_exact_errors(const irwls_dev_set *X, int l, const double *d_beta, int *d_lst, double *d_cb,
+                                       int *d_cnt, double *d_e) {
+    sv_list_kernel<<<1, CT, 0, irwls_stream()>>>(d_beta, l, d_lst, d_cb, d_cnt);
+    IRWLS_LAUNCH_CHECK("sv_list");
+    return irwls_dev_kernel_rowsum_n(X, nullptr, l, X, d_lst, d_cnt, d_cb, nullptr, nullptr, -1, X->y, d_beta + l,
+                                     d_e);
+}
+
+extern "C" int irwls_full_sv_list(const double *d_beta, int l, int *d_lst, double *d_cb, int *d_cnt) {
+    sv_list_kernel<<<1, CT, 0, irwls_stream()>>>(d_beta, l, d_lst, d_cb, d_cnt);
+    IRWLS_LAUNCH_CHECK("sv_list");
+    return 0;
+}
+
+extern "C" int irwls_full_exact_set(const double *d_e, const double *d_y, const double *d_beta, int l,
+                                    const int *d_SW, int nSW, double band, int all_exact, int *d_flag, int *d_mark,
+                                    int *d_S, int *d_Snew, int *d_counts) {
+    exact_set_kernel<<<1, CT, 0, irwls_stream()>>>(d_e, d_y, d_beta, l, d_SW, nSW, band, all_exact, d_flag, d_mark,
+                                                   d_S, d_Snew, d_counts);
+    IRWLS_LAUNCH_CHECK("exact_set");
+    return 0;
+}
+
+extern "C" int irwls_dev_gather(const double *d_src, const int *d_idx, int n, double *d_dst) {
+    if (n <= 0) return 0;
+    gather_kernel<<<std::min(ceil_div(n, 256), 1024), 256, 0, irwls_stream()>>>(d_src, d_idx, n, d_dst);
+    IRWLS_LAUNCH_CHECK("gather");
+    return 0;
+}
+
+extern "C" int irwls_dev_scatter(const double *d_src, const int *d_idx, int n, double *d_dst) {
+    if (n <= 0) return 0;
+    scatter_kernel<<<std::min(ceil_div(n, 256), 1024), 256, 0, irwls_stream()>>>(d_src, d_idx, n, d_dst);
+    IRWLS_LAUNCH_CHECK("scatter");
+    return 0;
+}
 
 extern "C" int irwls_sub_alloc(irwls_sub_ws *ws, int cap) {
     memset(ws, 0, sizeof *ws);

@@ -76,76 +76,96 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return done != 0;
 }
 
-// Shared memory of one K stage: A hi/lo (128 rows) and B hi/lo (BN rows).
-template <int BN>
+// Shared memory of one K stage: the P pieces of A (128 rows) then the P
+// pieces of B (BN rows). P = 2 (hi, lo): three products; P = 3 (hi, mid,
+// lo): six products (all terms down to 2^-24 of the product).
+template <int BN, int P = 2>
 struct TcStage {
     static constexpr int A_BYTES = TC_BM * TC_BK * 2;
     static constexpr int B_BYTES = BN * TC_BK * 2;
-    static constexpr int BYTES = 2 * A_BYTES + 2 * B_BYTES;
+    static constexpr int BYTES = P * A_BYTES + P * B_BYTES;
 };
 
 // Copies K stage `ks` of the CTA's rows into stage buffer `sb` (cp.async).
-template <int BN>
-__device__ __forceinline__ void tc_load_stage(unsigned char *sb, const __nv_bfloat16 *Ahi, const __nv_bfloat16 *Alo,
-                                              int lda, int m0, int M, const __nv_bfloat16 *Bhi,
-                                              const __nv_bfloat16 *Blo, int ldb, int n0, int N, int ks) {
+// A[p] / B[p]: the P pieces of each operand.
+template <int BN, int P = 2>
+__device__ __forceinline__ void tc_load_stage_p(unsigned char *sb, const __nv_bfloat16 *const *A, int lda, int m0,
+                                                int M, const __nv_bfloat16 *const *B, int ldb, int n0, int N, int ks) {
+    using S = TcStage<BN, P>;
     const int k0 = ks * TC_BK;
     const uint32_t base = smem_u32(sb);
-    // A: 2 x 128 rows x 8 chunks of 16 B
-    for (int t = threadIdx.x; t < 2 * TC_BM * 8; t += TC_THREADS) {
+    for (int t = threadIdx.x; t < P * TC_BM * 8; t += TC_THREADS) {
         const int which = t / (TC_BM * 8), rem = t % (TC_BM * 8);
         const int r = rem / 8, c = rem % 8;
         const int gr = m0 + r;
-        const __nv_bfloat16 *src = (which ? Alo : Ahi) + (size_t)(gr < M ? gr : 0) * lda + k0 + c * 8;
-        const uint32_t dst = base + which * TcStage<BN>::A_BYTES + (r / 8) * 1024 + c * 128 + (r % 8) * 16;
+        const __nv_bfloat16 *src = A[which] + (size_t)(gr < M ? gr : 0) * lda + k0 + c * 8;
+        const uint32_t dst = base + which * S::A_BYTES + (r / 8) * 1024 + c * 128 + (r % 8) * 16;
         cp_async16(dst, src, gr < M ? 16 : 0);
     }
-    for (int t = threadIdx.x; t < 2 * BN * 8; t += TC_THREADS) {
+    for (int t = threadIdx.x; t < P * BN * 8; t += TC_THREADS) {
         const int which = t / (BN * 8), rem = t % (BN * 8);
         const int r = rem / 8, c = rem % 8;
         const int gr = n0 + r;
-        const __nv_bfloat16 *src = (which ? Blo : Bhi) + (size_t)(gr < N ? gr : 0) * ldb + k0 + c * 8;
-        const uint32_t dst =
-            base + 2 * TcStage<BN>::A_BYTES + which * TcStage<BN>::B_BYTES + (r / 8) * 1024 + c * 128 + (r % 8) * 16;
+        const __nv_bfloat16 *src = B[which] + (size_t)(gr < N ? gr : 0) * ldb + k0 + c * 8;
+        const uint32_t dst = base + P * S::A_BYTES + which * S::B_BYTES + (r / 8) * 1024 + c * 128 + (r % 8) * 16;
         cp_async16(dst, src, gr < N ? 16 : 0);
     }
     asm volatile("cp.async.commit_group;\n" ::);
 }
 
-// Issues the 12 MMAs of one K stage (thread 0 only).
 template <int BN>
+__device__ __forceinline__ void tc_load_stage(unsigned char *sb, const __nv_bfloat16 *Ahi, const __nv_bfloat16 *Alo,
+                                              int lda, int m0, int M, const __nv_bfloat16 *Bhi,
+                                              const __nv_bfloat16 *Blo, int ldb, int n0, int N, int ks) {
+    const __nv_bfloat16 *A[2] = {Ahi, Alo}, *B[2] = {Bhi, Blo};
+    tc_load_stage_p<BN, 2>(sb, A, lda, m0, M, B, ldb, n0, N, ks);
+}
+
+// Issues the MMAs of one K stage (thread 0 only): per 16-wide K step, the
+// products of piece pairs (i, j) with i + j < P (3 for P = 2, 6 for P = 3).
+template <int BN, int P = 2>
 __device__ __forceinline__ void tc_mma_stage(unsigned char *sb, uint32_t tmem, bool first) {
+    using S = TcStage<BN, P>;
     const uint32_t base = smem_u32(sb);
-    const uint32_t aHi = base, aLo = base + TcStage<BN>::A_BYTES;
-    const uint32_t bHi = base + 2 * TcStage<BN>::A_BYTES, bLo = bHi + TcStage<BN>::B_BYTES;
     constexpr uint32_t idesc = tc_idesc(TC_BM, BN);
 #pragma unroll
     for (int kk = 0; kk < TC_BK / 16; ++kk) {
         const uint32_t off = kk * 256;  // 16 elements = 2 core matrices along K
-        mma_bf16(tmem, tc_desc(aHi + off), tc_desc(bHi + off), idesc, (first && kk == 0) ? 0u : 1u);
-        mma_bf16(tmem, tc_desc(aHi + off), tc_desc(bLo + off), idesc, 1u);
-        mma_bf16(tmem, tc_desc(aLo + off), tc_desc(bHi + off), idesc, 1u);
+        bool init = first && kk == 0;
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P - i; ++j) {
+                const uint32_t a = base + i * S::A_BYTES + off, b = base + P * S::A_BYTES + j * S::B_BYTES + off;
+                mma_bf16(tmem, tc_desc(a), tc_desc(b), idesc, init ? 0u : 1u);
+                init = false;
+            }
     }
 }
 
 // The main loop shared by the kernels below: accumulates the CTA's
 // 128 x BN tile over K stages [ks0, ks1) into tensor memory. Returns false if
-// a wait ran out.
-template <int BN>
-__device__ bool tc_mainloop(unsigned char *smem, uint64_t *mbar, uint32_t tmem, const __nv_bfloat16 *Ahi,
-                            const __nv_bfloat16 *Alo, int lda, int m0, int M, const __nv_bfloat16 *Bhi,
-                            const __nv_bfloat16 *Blo, int ldb, int n0, int N, int ks0, int ks1) {
-    constexpr int SB = TcStage<BN>::BYTES;
+// a wait ran out. Stage i commits to mbar[i & 1]; `used` holds how many
+// phases each barrier has completed before this call (0 for fresh barriers)
+// and is advanced by the call, which waits for every commit it made, so a
+// kernel can run the loop again on the same barriers and tensor memory.
+template <int BN, int P>
+__device__ bool tc_mainloop_p(unsigned char *smem, uint64_t *mbar, uint32_t tmem, const __nv_bfloat16 *const *A,
+                              int lda, int m0, int M, const __nv_bfloat16 *const *B, int ldb, int n0, int N, int ks0,
+                              int ks1, uint32_t *used) {
+    constexpr int SB = TcStage<BN, P>::BYTES;
     const int nst = ks1 - ks0;
     bool ok = true;
     if (nst <= 0) return true;
-    tc_load_stage<BN>(smem, Ahi, Alo, lda, m0, M, Bhi, Blo, ldb, n0, N, ks0);
+    const uint32_t u0 = used ? used[0] : 0u, u1 = used ? used[1] : 0u;
+    auto parity = [&](int stage) { return ((stage & 1 ? u1 : u0) + (uint32_t)(stage >> 1)) & 1u; };
+    tc_load_stage_p<BN, P>(smem, A, lda, m0, M, B, ldb, n0, N, ks0);
     for (int i = 0; i < nst; ++i) {
         const int buf = i & 1;
         if (i + 1 < nst) {
             // the other buffer was last read by the MMAs of stage i - 1
-            if (i >= 1 && !mbar_wait(smem_u32(&mbar[buf ^ 1]), ((i - 1) >> 1) & 1)) ok = false;
-            tc_load_stage<BN>(smem + (buf ^ 1) * SB, Ahi, Alo, lda, m0, M, Bhi, Blo, ldb, n0, N, ks0 + i + 1);
+            if (i >= 1 && !mbar_wait(smem_u32(&mbar[buf ^ 1]), parity(i - 1))) ok = false;
+            tc_load_stage_p<BN, P>(smem + (buf ^ 1) * SB, A, lda, m0, M, B, ldb, n0, N, ks0 + i + 1);
             asm volatile("cp.async.wait_group 1;\n" ::);
         } else {
             asm volatile("cp.async.wait_group 0;\n" ::);
@@ -155,18 +175,33 @@ __device__ bool tc_mainloop(unsigned char *smem, uint64_t *mbar, uint32_t tmem, 
         if (!ok) break;
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-            tc_mma_stage<BN>(smem + buf * SB, tmem, i == 0);
+            tc_mma_stage<BN, P>(smem + buf * SB, tmem, i == 0);
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                 smem_u32(&mbar[buf])));
         }
     }
     asm volatile("cp.async.wait_group 0;\n" ::);
-    // the last stage's commit covers all earlier MMAs
+    // the last stage's commit covers all earlier MMAs; the one before it is
+    // waited for too, so that both barriers end with every phase observed
     const int last = nst - 1;
-    if (ok && !mbar_wait(smem_u32(&mbar[last & 1]), (last >> 1) & 1)) ok = false;
+    if (ok && !mbar_wait(smem_u32(&mbar[last & 1]), parity(last))) ok = false;
+    if (ok && nst >= 2 && !mbar_wait(smem_u32(&mbar[(last - 1) & 1]), parity(last - 1))) ok = false;
     ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (used) {
+        used[0] = u0 + (uint32_t)((nst + 1) / 2);
+        used[1] = u1 + (uint32_t)(nst / 2);
+    }
     return ok;
+}
+
+template <int BN>
+__device__ bool tc_mainloop(unsigned char *smem, uint64_t *mbar, uint32_t tmem, const __nv_bfloat16 *Ahi,
+                            const __nv_bfloat16 *Alo, int lda, int m0, int M, const __nv_bfloat16 *Bhi,
+                            const __nv_bfloat16 *Blo, int ldb, int n0, int N, int ks0, int ks1,
+                            uint32_t *used = nullptr) {
+    const __nv_bfloat16 *A[2] = {Ahi, Alo}, *B[2] = {Bhi, Blo};
+    return tc_mainloop_p<BN, 2>(smem, mbar, tmem, A, lda, m0, M, B, ldb, n0, N, ks0, ks1, used);
 }
 
 template <int BN>
@@ -667,5 +702,227 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
     q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
                                                             (__nv_bfloat16 *)Qhi, (__nv_bfloat16 *)Qlo, ldq);
     IRWLS_LAUNCH_CHECK("q_column");
+    return 0;
+}
+
+// ===========================================================================
+// Precision form of full IRWLS: the error update over every training row,
+//   e_i <- (e_i - sum_j cb_j k(x_i, x_{b_j})) - tail,   j over the working set,
+// with the kernel values from dot products on the tensor cores: each value is
+// split into three bf16 pieces hi + mid + lo (24 significant bits) and the six
+// piece products down to 2^-24 are accumulated in FP32, then
+// k = exp(-gamma (q_i + q_j - 2 x_i . x_j)) (RBF, the norm form) or x_i . x_j
+// (linear). The error update is incremental, so its per-entry error has to
+// stay near FP32 rounding: the two-piece (16-bit) split's 1e-5 moved the
+// errors across the classification threshold within a few updates. The
+// dataset is kept once per training as a dense three-piece copy (K padded to
+// 64); the working-set rows are gathered into B before each update. A CTA
+// owns 128 rows and walks the working set in passes of 128 columns through
+// one tensor-memory accumulator; each row's sum is Kahan-compensated FP32 in
+// a fixed column order.
+// ===========================================================================
+
+namespace {
+
+constexpr int KR_BN = 128, KR_P = 3;
+
+struct Pieces {
+    const __nv_bfloat16 *p[KR_P];
+};
+
+__global__ void __launch_bounds__(TC_THREADS) tc_kernel_rowsum_kernel(
+    Pieces Ap, int lda, int M, const float *__restrict__ qa, Pieces Bp, int ldb, const int *__restrict__ d_n, int nmax,
+    const float *__restrict__ qb, const double *__restrict__ cb, int kst, int rbf, float ng,
+    const double *init, const double *__restrict__ tail, double *out, int *flags) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ float qs[KR_BN], cs[KR_BN];
+    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
+    const int N = min(*d_n, nmax);  // the gathered rows held in B
+    const int m0 = blockIdx.x * TC_BM;
+    const int row = m0 + threadIdx.x;
+    const float qi = row < M ? qa[row] : 0.f;
+    float sum = 0.f, comp = 0.f;
+    tc_setup<KR_BN>(mbar, &tmem_slot);
+    const uint32_t tmem = tmem_slot;
+    uint32_t used[2] = {0u, 0u};
+    bool ok = true;
+    for (int n0 = 0; n0 < N && ok; n0 += KR_BN) {
+        for (int t = threadIdx.x; t < KR_BN; t += TC_THREADS) {
+            const int j = n0 + t;
+            qs[t] = j < N ? qb[j] : 0.f;
+            cs[t] = j < N ? (float)cb[j] : 0.f;
+        }
+        ok = tc_mainloop_p<KR_BN, KR_P>(smem, mbar, tmem, Ap.p, lda, m0, M, Bp.p, ldb, n0, N, 0, kst, used);
+        if (!ok) break;
+        const int ncol = min(KR_BN, N - n0);
+        for (int c0 = 0; c0 < ncol; c0 += 8) {
+            float v[8];
+            tc_ld8(tmem, c0, v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int c = c0 + j;
+                if (c < ncol) {
+                    const float k = rbf ? expf(ng * fmaxf(qi + qs[c] - 2.f * v[j], 0.f)) : v[j];
+                    const float y = __fsub_rn(__fmul_rn(cs[c], k), comp);
+                    const float t = __fadd_rn(sum, y);
+                    comp = __fsub_rn(__fsub_rn(t, sum), y);
+                    sum = t;
+                }
+            }
+        }
+        // the next pass overwrites the accumulator and qs/cs
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+        __syncthreads();
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
+    if (ok && row < M) out[row] = __dsub_rn(__dsub_rn(init[row], (double)sum - (double)comp), tail ? tail[0] : 0.0);
+    tc_teardown<KR_BN>(tmem);
+}
+
+// B rows j < *d_n: the dense split rows idx[j] of the set, and their norms.
+__global__ void tc_gather_rows_kernel(Pieces X, int ld, const float *__restrict__ q, const int *__restrict__ idx,
+                                      const int *__restrict__ d_n, int nmax, __nv_bfloat16 *B0, __nv_bfloat16 *B1,
+                                      __nv_bfloat16 *B2, float *qb) {
+    const int n = min(*d_n, nmax);
+    const int per = ld / 8;  // 16-byte pieces per row
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * per;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(t / per), c = (int)(t % per);
+        const size_t src = (size_t)idx[j] * ld + (size_t)c * 8, dst = (size_t)j * ld + (size_t)c * 8;
+        *(uint4 *)(B0 + dst) = *(const uint4 *)(X.p[0] + src);
+        *(uint4 *)(B1 + dst) = *(const uint4 *)(X.p[1] + src);
+        *(uint4 *)(B2 + dst) = *(const uint4 *)(X.p[2] + src);
+        if (c == 0) qb[j] = q[idx[j]];
+    }
+}
+
+// Three-piece split of the first `cols` columns of a row-major FP64 matrix
+// (rounded to FP32 first), zero up to ldo.
+__global__ void split3_kernel(const double *__restrict__ X, long long rows, int cols, int ldx, __nv_bfloat16 *p0,
+                              __nv_bfloat16 *p1, __nv_bfloat16 *p2, int ldo) {
+    const long long total = rows * (long long)ldo;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long r = t / ldo;
+        const int c = (int)(t % ldo);
+        const float x = c < cols ? __double2float_rn(X[r * ldx + c]) : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        const float r1 = x - __bfloat162float(h);
+        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+        p0[t] = h;
+        p1[t] = m;
+        p2[t] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+    }
+}
+
+struct TcSet {
+    __nv_bfloat16 *X[KR_P], *B[KR_P];
+    float *q, *qb;
+    int rows, ld, wmax, rbf;
+    float ng;
+    double kbound;
+};
+
+// max over rows of q (one CTA): |x_i . x_j| <= max q bounds linear kernel values.
+__global__ void __launch_bounds__(1024) max_q_kernel(const float *__restrict__ q, int n, float *out) {
+    __shared__ float red[1024];
+    float m = 0.f;
+    for (int i = threadIdx.x; i < n; i += 1024) m = fmaxf(m, q[i]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 512; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+
+}  // namespace
+
+// Dense split copy of rows 0..rows-1 of a device set for the precision form
+// of full IRWLS, with room for `wmax` gathered working-set rows.
+extern "C" void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax) {
+    TcSet *t = (TcSet *)calloc(1, sizeof(TcSet));
+    if (!t) return nullptr;
+    t->rows = rows;
+    t->ld = ceil_div(X->width, TC_BK) * TC_BK;
+    t->wmax = wmax;
+    t->rbf = X->mode != IRWLS_K_LINEAR;
+    t->ng = (float)X->neg_gamma;
+    int rc = 0;
+    const size_t xb = (size_t)(rows > 0 ? rows : 1) * t->ld * sizeof(__nv_bfloat16);
+    const size_t bb = (size_t)(wmax > 0 ? wmax : 1) * t->ld * sizeof(__nv_bfloat16);
+    for (int k = 0; k < KR_P; ++k) {
+        rc |= irwls_dev_malloc((void **)&t->X[k], xb);
+        rc |= irwls_dev_malloc((void **)&t->B[k], bb);
+    }
+    rc |= irwls_dev_malloc((void **)&t->q, (size_t)(rows > 0 ? rows : 1) * sizeof(float));
+    rc |= irwls_dev_malloc((void **)&t->qb, (size_t)(wmax > 0 ? wmax : 1) * sizeof(float));
+    if (!rc && rows > 0) {
+        const long long total = (long long)rows * t->ld;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 65535);
+        split3_kernel<<<blocks, 256, 0, irwls_stream()>>>(X->X, rows, X->width, X->ld, t->X[0], t->X[1], t->X[2],
+                                                           t->ld);
+        irwls_count_launch(1);
+        to_f32_kernel<<<ceil_div(rows, 256), 256, 0, irwls_stream()>>>(X->q, rows, t->q);
+        irwls_count_launch(1);
+        if (cudaPeekAtLastError() != cudaSuccess) rc = -1;
+    }
+    t->kbound = 1.0;
+    if (!rc && !t->rbf && rows > 0) {
+        max_q_kernel<<<1, 1024, 0, irwls_stream()>>>(t->q, rows, t->qb);
+        irwls_count_launch(1);
+        float mq = 0.f;
+        rc |= irwls_dev_d2h(&mq, t->qb, sizeof(float));
+        rc |= irwls_dev_sync();
+        t->kbound = 1.01 * (double)mq;
+    }
+    if (rc) {
+        irwls_tc_set_free(t);
+        irwls_set_error(-3, "cannot create the split copy of the dataset");
+        return nullptr;
+    }
+    return t;
+}
+
+extern "C" double irwls_tc_set_kbound(void *h) { return ((TcSet *)h)->kbound; }
+
+extern "C" void irwls_tc_set_free(void *h) {
+    TcSet *t = (TcSet *)h;
+    if (!t) return;
+    for (int k = 0; k < KR_P; ++k) {
+        irwls_dev_free(t->X[k]);
+        irwls_dev_free(t->B[k]);
+    }
+    irwls_dev_free(t->q);
+    irwls_dev_free(t->qb);
+    free(t);
+}
+
+// out_i = (init_i - sum_{j < *d_n} cb_j k(x_i, x_{idx_j})) - tail[0] for every
+// row of the set (init may alias out; tail may be NULL).
+extern "C" int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n, const double *d_cb,
+                                      const double *d_init, const double *d_tail, double *d_out) {
+    TcSet *t = (TcSet *)h;
+    const int per = t->ld / 8;
+    Pieces xp, bp;
+    for (int k = 0; k < KR_P; ++k) {
+        xp.p[k] = t->X[k];
+        bp.p[k] = t->B[k];
+    }
+    const int gb = std::max(1, std::min(ceil_div((long long)t->wmax * per, 256), 4096));
+    tc_gather_rows_kernel<<<gb, 256, 0, irwls_stream()>>>(xp, t->ld, t->q, d_idx, d_n, t->wmax, t->B[0], t->B[1],
+                                                          t->B[2], t->qb);
+    IRWLS_LAUNCH_CHECK("tc_gather_rows");
+    const size_t smem = 2 * TcStage<KR_BN, KR_P>::BYTES + 1024;
+    cudaFuncSetAttribute(tc_kernel_rowsum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
+    tc_kernel_rowsum_kernel<<<ceil_div(t->rows, TC_BM), TC_THREADS, smem, irwls_stream()>>>(
+        xp, t->ld, t->rows, t->q, bp, t->ld, d_n, t->wmax, t->qb, d_cb, t->ld / TC_BK, t->rbf, t->ng, d_init, d_tail,
+        d_out, irwls_dev_flags());
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
+    IRWLS_LAUNCH_CHECK("tc_kernel_rowsum");
     return 0;
 }

@@ -112,6 +112,22 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
     irwls_sub_ws ws;
     memset(&ws, 0, sizeof ws);
     const size_t L1 = (size_t)(l + 1);
+    /* precision form: the error update of most rows runs on the tensor cores
+       from a split copy of the dataset (irwls_tc_kernel_rowsum, about 1e-5
+       relative per kernel value); the rows whose errors decide anything --
+       support vectors, rows within `band` of the margin, the working set --
+       keep FP64 increments (the exact set S), rows entering S are recomputed
+       from the support vectors, and every row is recomputed once the
+       accumulated error bound of the others reaches band / 5. The working-set
+       solves, GIN and the in-set updates are the FP64 form's. */
+    void *tcs = NULL;
+    if (irwls_get_precision() == IRWLS_PRECISION_MIXED && !(tcs = irwls_tc_set_create(X, l, W))) return -1;
+    const double band = 0.05, eps = 2e-5 * (tcs ? irwls_tc_set_kbound(tcs) : 1.0);
+    int *xflag = NULL, *xmark = NULL, *xS = NULL, *xSnew = NULL, *svlst = NULL, *svcnt = NULL, *xcnt = NULL,
+        *h_xcnt = NULL;
+    double *eS = NULL, *svcb = NULL, *h_l1 = NULL;
+    int nS = 0;
+    double acc = 0.0;
     rc |= irwls_dev_malloc((void **)&e, L1 * sizeof(double));
     rc |= irwls_dev_malloc((void **)&beta, L1 * sizeof(double));
     rc |= irwls_dev_malloc((void **)&bnew, L1 * sizeof(double));
@@ -128,6 +144,23 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
     rc |= irwls_dev_host_alloc((void **)&h_counts, sizeof(irwls_outer_counts));
     rc |= irwls_dev_host_alloc((void **)&h_norms, 2 * sizeof(double));
     rc |= irwls_sub_alloc(&ws, W);
+    if (tcs) {
+        rc |= irwls_dev_malloc((void **)&xflag, L1 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&xmark, L1 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&xS, L1 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&xSnew, L1 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&svlst, L1 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&svcnt, 2 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&xcnt, 2 * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&eS, L1 * sizeof(double));
+        rc |= irwls_dev_malloc((void **)&svcb, L1 * sizeof(double));
+        rc |= irwls_dev_host_alloc((void **)&h_xcnt, 2 * sizeof(int));
+        rc |= irwls_dev_host_alloc((void **)&h_l1, sizeof(double));
+        if (!rc) {
+            rc |= irwls_dev_memset(xflag, 0, L1 * sizeof(int));
+            rc |= irwls_dev_memset(xmark, 0, L1 * sizeof(int));
+        }
+    }
     if (rc) goto done;
 
     /* initial working set: every tenth sample, up to W (src/full-train.c:411-423) */
@@ -149,6 +182,14 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
         free(hsw);
         free(hsin);
         if (rc) goto done;
+        if (tcs) {
+            /* e = y is exact everywhere: S is the first working set */
+            rc |= irwls_full_exact_set(e, X->y, bnew, l, SW, nSW, band, 1, xflag, xmark, xS, xSnew, xcnt);
+            rc |= irwls_dev_d2h(h_xcnt, xcnt, 2 * sizeof(int));
+            rc |= irwls_dev_sync();
+            if (rc) goto done;
+            nS = h_xcnt[0];
+        }
     }
 
     int stop = 0, since_best = 0;
@@ -163,9 +204,20 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
         if (run_sub(&ws, X, &props)) goto fail;
         /* betaNew over the working set; e -= K(:, SW) (betaNew - beta) - dbias (:488-510) */
         if (irwls_full_apply_ws(SW, nSW, ws.bbest, beta, l, bnew, lst, cb, cnt, dbias)) goto fail;
-        if (irwls_dev_kernel_rowsum_n(X, NULL, l, X, lst, cnt, cb, NULL, NULL, -1, e, dbias, e)) goto fail;
+        if (tcs) {
+            /* FP64 increments of the exact rows, tensor-core update of all
+               rows, then the exact values written back */
+            if (nS > 0 && (irwls_dev_gather(e, xS, nS, eS) ||
+                           irwls_dev_kernel_rowsum_n(X, xS, nS, X, lst, cnt, cb, NULL, NULL, -1, eS, dbias, eS)))
+                goto fail;
+            if (irwls_tc_kernel_rowsum(tcs, lst, cnt, cb, e, dbias, e)) goto fail;
+            if (irwls_dev_scatter(eS, xS, nS, e) || irwls_dev_d2h(h_l1, dbias + 1, sizeof(double))) goto fail;
+        } else if (irwls_dev_kernel_rowsum_n(X, NULL, l, X, lst, cnt, cb, NULL, NULL, -1, e, dbias, e)) {
+            goto fail;
+        }
         if (irwls_full_norms(beta, bnew, l + 1, norms)) goto fail;
         if (irwls_dev_d2h(h_norms, norms, 2 * sizeof(double)) || irwls_dev_sync()) goto fail;
+        if (tcs) acc += eps * h_l1[0];
         const double ratio = h_norms[0] / h_norms[1];
         if (ratio < props.Eta) stop = 1;
         if (irwls_dev_d2d(beta, bnew, L1 * sizeof(double))) goto fail;
@@ -199,6 +251,27 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
             nSW += space;
             nSIN += nSC - space;
         }
+        if (tcs && !stop) {
+            /* the exact set of the next update; all rows recomputed when the
+               error bound of the others nears the band */
+            int all_exact = 0;
+            if (acc > band / 5) {
+                if (irwls_full_exact_errors(X, l, bnew, svlst, svcb, svcnt, e)) goto fail;
+                acc = 0.0;
+                all_exact = 1;
+            }
+            if (irwls_full_exact_set(e, X->y, bnew, l, SW, nSW, band, all_exact, xflag, xmark, xS, xSnew, xcnt) ||
+                irwls_dev_d2h(h_xcnt, xcnt, 2 * sizeof(int)) || irwls_dev_sync())
+                goto fail;
+            nS = h_xcnt[0];
+            const int nnew = h_xcnt[1];
+            if (nnew > 0 && (irwls_full_sv_list(bnew, l, svlst, svcb, svcnt) ||
+                             irwls_dev_gather(X->y, xSnew, nnew, eS) ||
+                             irwls_dev_kernel_rowsum_n(X, xSnew, nnew, X, svlst, svcnt, svcb, NULL, NULL, -1, eS,
+                                                       bnew + l, eS) ||
+                             irwls_dev_scatter(eS, xSnew, nnew, e)))
+                goto fail;
+        }
     }
     if (irwls_dev_d2h(beta_out, bnew, L1 * sizeof(double)) || irwls_dev_sync()) goto fail;
     goto done;
@@ -206,6 +279,11 @@ fail:
     rc = -1;
 done:
     irwls_sub_release(&ws);
+    irwls_tc_set_free(tcs);
+    void *xbufs[] = {xflag, xmark, xS, xSnew, svlst, svcnt, xcnt, eS, svcb};
+    for (size_t k = 0; k < sizeof xbufs / sizeof xbufs[0]; k++) irwls_dev_free(xbufs[k]);
+    irwls_dev_host_free(h_xcnt);
+    irwls_dev_host_free(h_l1);
     void *bufs[] = {e, beta, bnew, cb, dbias, norms, SW, SIN, SC, lst, perm_d, cnt, counts};
     for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
     irwls_dev_host_free(h_counts);

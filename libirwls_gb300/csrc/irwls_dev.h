@@ -184,6 +184,27 @@ int irwls_par_weights(const double *d_Da, const double *d_y, int l, int *d_act, 
                       int *d_nact);
 int irwls_par_delta(const double *d_bnew, double *d_beta, int m, double *d_out2);
 
+/* Precision form of full IRWLS (dev_tc.cu): split-BF16 copy of a set and the
+ * tensor-core error update out_i = (init_i - sum_j cb_j k(x_i, x_{idx_j})) -
+ * tail[0] over all of its rows, j < *d_n <= wmax. */
+void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax);
+/* e = y - K(:, SV) beta_SV - beta[l] in FP64 (dev_full.cu); lst/cb/cnt are scratch of l entries. */
+int irwls_full_exact_errors(const irwls_dev_set *X, int l, const double *d_beta, int *d_lst, double *d_cb, int *d_cnt,
+                            double *d_e);
+/* The exact-error row set of the precision form (dev_full.cu): S = support
+ * vectors, rows with |e y| < band, and SW; Snew = rows of S not flagged
+ * before (none when all_exact); counts = {|S|, |Snew|}. */
+int irwls_full_exact_set(const double *d_e, const double *d_y, const double *d_beta, int l, const int *d_SW, int nSW,
+                         double band, int all_exact, int *d_flag, int *d_mark, int *d_S, int *d_Snew, int *d_counts);
+int irwls_full_sv_list(const double *d_beta, int l, int *d_lst, double *d_cb, int *d_cnt);   /* beta != 0, i < l */
+int irwls_dev_gather(const double *d_src, const int *d_idx, int n, double *d_dst);    /* dst[k] = src[idx[k]] */
+int irwls_dev_scatter(const double *d_src, const int *d_idx, int n, double *d_dst);   /* dst[idx[k]] = src[k] */
+/* Bound on |k(x_i, x_j)| over the set (1 for RBF, max q for linear). */
+double irwls_tc_set_kbound(void *h);
+void irwls_tc_set_free(void *h);
+int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n, const double *d_cb, const double *d_init,
+                           const double *d_tail, double *d_out);
+
 /* Resident-dataset drivers (full_train.c, budgeted_train.c). */
 int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double *beta_out);
 int irwls_sgma_dev(const irwls_dev_set *X, const svm_dataset *ds, properties props, int *cent_out);

@@ -98,6 +98,48 @@ def budgeted_test_set(n=20_000, seed=20240604, label_seed=20240603):
     return mixed_onehot(n, seed, label_seed=label_seed)
 
 
+def proto_digits(n: int, seed: int, proto_seed: int = 20240605, d: int = 784, n_proto: int = 10,
+                 support: float = 0.2, keep: float = 0.9, extra: float = 0.015):
+    """Sparse-valued dense rows from seeded prototype patterns: prototype k
+    lights a random ``support`` fraction of the d pixels with base
+    intensities U(0.3, 1); a sample of class k keeps each lit pixel with
+    probability ``keep`` (intensity x (1 + 0.25 N(0, 1))), lights each other
+    pixel with probability ``extra`` (U(0, 0.5)), and is quantised to 8-bit
+    integers / 255 (about 19 % nonzero). Label +1 for prototypes 0-4, -1 for
+    5-9. The prototypes come from ``proto_seed`` so that sets drawn with
+    different ``seed`` share them. Returns the dense (n, d) matrix and labels."""
+    prng = np.random.default_rng(proto_seed)
+    lit = np.zeros((n_proto, d), dtype=bool)
+    base = np.zeros((n_proto, d))
+    for k in range(n_proto):
+        idx = prng.choice(d, size=int(round(support * d)), replace=False)
+        lit[k, idx] = True
+        base[k, idx] = prng.uniform(0.3, 1.0, size=idx.size)
+    rng = np.random.default_rng(seed)
+    cls = rng.integers(0, n_proto, n)
+    X = np.zeros((n, d), dtype=np.float32)
+    chunk = 8192
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        k = cls[a:b]
+        on = lit[k] & (rng.random((b - a, d)) < keep)
+        val = base[k] * (1.0 + 0.25 * rng.standard_normal((b - a, d)))
+        ex = (~lit[k]) & (rng.random((b - a, d)) < extra)
+        val = np.where(ex, rng.uniform(0.0, 0.5, (b - a, d)), np.where(on, val, 0.0))
+        X[a:b] = np.rint(np.clip(val, 0.0, 1.0) * 255.0)
+    y = np.where(cls < n_proto // 2, 1.0, -1.0)
+    return X.astype(np.float64) / 255.0, y
+
+
+def precision_full_workload(n_train=100_000, n_test=10_000, seed=20240606):
+    """Full-IRWLS workload of the precision form: 784 features, 8-bit values,
+    about 19 % nonzero, prototypes 0-4 against 5-9 (zeros omitted, so the
+    reader flags the set as sparse)."""
+    Xtr, ytr = proto_digits(n_train, seed)
+    Xte, yte = proto_digits(n_test, seed + 1)
+    return from_dense(Xtr, ytr, keep_zeros=False), from_dense(Xte, yte, keep_zeros=False)
+
+
 def write_libsvm(path: str, data: Sparse, labeled: bool = True) -> None:
     with open(path, "w") as f:
         ip, ix, vv = data.indptr, data.indices, data.values

@@ -1,4 +1,5 @@
-"""Precision form of budgeted IRWLS (irwls_set_precision(IRWLS_PRECISION_MIXED)).
+"""Precision form (irwls_set_precision(IRWLS_PRECISION_MIXED)) of budgeted and
+full IRWLS.
 
 SGMA: the candidate scores come from split-BF16 tensor-core products on the
 Nystrom features Q = K_nm L^-T, with the factor and its solves in FP64. Its
@@ -52,3 +53,34 @@ def test_mixed_budgeted_matches_reference(case):
         lib.freeModel(mdl)
     agree = float((labels == g["hard"]).mean())
     assert agree >= 0.999
+
+
+# Relative dual-objective difference allowed for full IRWLS (the precision
+# form's contract is 1e-4).
+DUAL_TOL = 1e-5
+
+
+@pytest.mark.parametrize("case", H.FULL_CASES)
+def test_mixed_full_matches_reference(case):
+    lib = load()
+    g = H.golden(case)
+    p = H.params(g)
+    tr, te = H.datasets(g)
+    lib.irwls_set_precision(1)
+    try:
+        beta, ptr, prop = H.run_full(lib, tr, p)
+    finally:
+        lib.irwls_set_precision(0)
+    assert lib.irwls_tc_status() == 0
+    ref = H.dual_objective(tr, g["beta"], p["gamma"], p["kernel"])
+    got = H.dual_objective(tr, beta, p["gamma"], p["kernel"])
+    same_sv = np.array_equal(np.nonzero(beta[:-1])[0], np.nonzero(g["beta"][:-1])[0])
+    print("%s: beta rel err %.3g, dual rel err %.3g, same SV set %s" % (case, H.rel_err(beta, g["beta"]),
+                                                                      abs(got - ref) / abs(ref), same_sv))
+    assert abs(got - ref) <= DUAL_TOL * abs(ref)
+    mdl = lib.calculateFULLModel(prop, tr.struct, ptr)
+    try:
+        labels = H.predict(lib, te, mdl, 0)
+    finally:
+        lib.freeModel(mdl)
+    assert float((labels == g["hard"]).mean()) >= 0.999
