@@ -36,8 +36,11 @@ forms are timed in the same run, on the same resident dataset:
 `--form plain|mixed` times one form only (no accuracy comparison).
 `--workload full` measures the dense full-IRWLS workload instead (n = 4000
 train rows, d = 20, two Gaussian classes with 10% flipped labels, RBF gamma =
-0.05, C = 10, working set 500); its CPU baseline is the restatement's whole
-training on all host cores (about 1-3 s, no extrapolation).
+0.05, C = 10, working set 500), `--workload full784` the full-IRWLS workload
+of the precision form (n = 100000, d = 784 8-bit values at 19% density from
+10 prototypes, RBF gamma = 0.02, C = 10); both time the two forms with the
+same bars (dual objective instead of primal); their CPU baseline is the
+restatement's whole training on all host cores (no extrapolation).
 
 `--impl reference` runs only the CPU baseline measurement above (the reference
 sources cannot be built on the GPU host, so the restatement stands in for it)
@@ -78,7 +81,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
-    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full"])
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784"])
     ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
@@ -485,66 +488,113 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------
-# dense full-IRWLS workload
+# full-IRWLS workloads
 # ----------------------------------------------------------------------------
-FULL = dict(n=4000, d=20, seed=20240601, gamma=0.05, C=10.0, w=500)
+FULL = {
+    "full": dict(n=4000, n_test=1000, d=20, seed=20240601, gamma=0.05, C=10.0, w=500,
+                 desc="full IRWLS: n=4000, d=20 dense (two Gaussian classes, means +-0.5, 10%% labels flipped), "
+                      "RBF gamma=0.05, C=10, working set 500"),
+    "full784": dict(n=100_000, n_test=10_000, d=784, seed=20240606, gamma=0.02, C=10.0, w=500, cpu_rows=20_000,
+                    desc="full IRWLS: n=100000 train / 10000 test, d=784 sparse-valued dense (8-bit values / 255, "
+                         "19%% nonzero, 10 seeded prototypes, 0-4 vs 5-9), RBF gamma=0.02, C=10, working set 500"),
+}
 
 
-def full_workload():
+def full_workload(cfg):
     from libirwls_gb300 import _abi, synth
 
-    X, y = synth.two_gaussians(FULL["n"], FULL["d"], FULL["seed"])
-    data = synth.from_dense(X, y, keep_zeros=True)
-    return _abi.build_dataset(data.indptr, data.indices, data.values, data.y)
+    if cfg["d"] == 784:
+        tr, te = synth.precision_full_workload(cfg["n"], cfg["n_test"], seed=cfg["seed"])
+    else:
+        X, y = synth.two_gaussians(cfg["n"] + cfg["n_test"], cfg["d"], cfg["seed"])
+        tr = synth.from_dense(X[:cfg["n"]], y[:cfg["n"]], keep_zeros=True)
+        te = synth.from_dense(X[cfg["n"]:], y[cfg["n"]:], keep_zeros=True)
+    hd = _abi.build_dataset(tr.indptr, tr.indices, tr.values, tr.y)
+    ht = _abi.build_dataset(te.indptr, te.indices, te.values, te.y, with_means=False)
+    return hd, ht, te.y
 
 
-def full_props(threads=1):
+def full_props(cfg, threads=1):
     from libirwls_gb300 import _abi
 
-    return _abi.make_properties(gamma=FULL["gamma"], C_=FULL["C"], working_set=FULL["w"], threads=threads)
+    return _abi.make_properties(gamma=cfg["gamma"], C_=cfg["C"], working_set=cfg["w"], threads=threads, verbose=0)
 
 
-def full_config():
-    return {"workload": "full IRWLS, plain FP64: n=4000, d=20 dense (two Gaussian classes, means +-0.5, "
-                        "10%% labels flipped), RBF gamma=0.05, C=10, working set 500",
-            "n": FULL["n"], "d": FULL["d"], "gamma": FULL["gamma"], "C": FULL["C"], "working_set": FULL["w"],
-            "form": "plain FP64", "parallelism": "single GPU",
-            "l2": "flushed between timed steps (512 MiB overwrite); the training set (0.7 MB) fits in L2"}
+def full_config(cfg, form):
+    return {"workload": cfg["desc"], "n": cfg["n"], "d": cfg["d"], "gamma": cfg["gamma"], "C": cfg["C"],
+            "working_set": cfg["w"], "form": form, "parallelism": "single GPU",
+            "l2": "flushed between timed steps (512 MiB overwrite)"}
 
 
-def full_cpu(hd):
+def full_cpu(hd, cfg):
+    """The restatement's whole training on all host cores; for workloads with
+    `cpu_rows`, on a training set of that many rows from the same generator,
+    scaled linearly in the row count (the error update over all rows is the
+    bulk of each outer iteration)."""
     from libirwls_gb300 import _abi
+
+    scale, note = 1.0, ""
+    if cfg.get("cpu_rows") and cfg["cpu_rows"] < hd.l:
+        sub = dict(cfg, n=cfg["cpu_rows"], n_test=10)
+        hd, _, _ = full_workload(sub)
+        scale = cfg["n"] / cfg["cpu_rows"]
+        note = " on %d rows x %.0f (linear in rows)" % (cfg["cpu_rows"], scale)
 
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
-    port = _abi.load_library(os.path.join(ROOT, "oracle", "_build", "libirwls_port.so"))
+    port_path = os.path.join(ROOT, "oracle", "_build", "libirwls_port.so")
+    if not os.path.exists(port_path):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+    port = _abi.load_library(port_path)
     cores = os.cpu_count() or 1
     libc = C.CDLL(None)
+    port.initMemory(cores, cfg["w"] + 1)
     libc.srand(0)
     t0 = time.perf_counter()
-    b = port.trainFULL(hd.struct, full_props(threads=cores))
+    b = port.trainFULL(hd.struct, full_props(cfg, threads=cores))
     dt = time.perf_counter() - t0
     libc.free.argtypes = [C.c_void_p]
     libc.free(C.cast(b, C.c_void_p))
-    return {"value": round(dt, 3), "unit": "s", "cores": cores, "kind": "port",
-            "sample": "whole training by the CPU restatement of the reference, %d OpenMP threads" % cores}
+    return {"value": round(dt * scale, 3), "unit": "s", "cores": cores, "kind": "port",
+            "sample": "whole training by the CPU restatement of the reference, %d OpenMP threads%s (%.1f s measured)"
+                      % (cores, note, dt)}
+
+
+def dual_objective(hd, beta, gamma):
+    """D(beta) = sum_i y_i beta_i - 1/2 beta^T K beta over the support vectors
+    (RBF, norm form), in FP64 on the host."""
+    import numpy as np
+
+    from libirwls_gb300 import _abi
+
+    rows, y, q = _abi.dataset_rows(hd.struct, hd.l)
+    sv = np.nonzero(beta[:hd.l])[0]
+    d = max([int(rows[i][0].max()) for i in sv if len(rows[i][0])] + [0]) + 1
+    Xs = np.zeros((len(sv), d))
+    for k, i in enumerate(sv):
+        Xs[k, rows[i][0]] = rows[i][1]
+    qs = q[sv]
+    K = np.exp(-gamma * np.maximum(qs[:, None] + qs[None, :] - 2 * Xs @ Xs.T, 0.0))
+    b = beta[sv]
+    return float((y[sv] * b).sum() - 0.5 * b @ K @ b)
 
 
 def run_full(args):
     import numpy as np
 
-    from libirwls_gb300 import load
+    from libirwls_gb300 import _abi, load
 
-    hd = full_workload()
+    cfg = FULL[args.workload]
+    hd, ht, yt = full_workload(cfg)
     if args.impl == "reference":
-        vals = [full_cpu(hd)["value"] for _ in range(args.warmup + args.steps)][args.warmup:]
+        vals = [full_cpu(hd, cfg)["value"] for _ in range(args.warmup + args.steps)][args.warmup:]
         v = statistics.mean(vals)
-        base = full_cpu(hd)
+        base = full_cpu(hd, cfg)
         base["value"] = round(v, 3)
         print(json.dumps({"metric": METRIC, "value": round(v, 3), "unit": "s", "impl": "reference",
                           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                           "ms_per_step": round(v * 1000, 1), "higher_is_better": False, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-                          "config": full_config(), "cpu_baseline": base,
+                          "config": full_config(cfg, "plain FP64"), "cpu_baseline": base,
                           "e2e": {"value": round(v, 3), "unit": "s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return
@@ -552,39 +602,47 @@ def run_full(args):
     if not lib.irwls_gpu_available():
         raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
     libc = C.CDLL(None)
-    p = full_props()
+    p = full_props(cfg)
     res = lib.irwls_resident_upload(hd.struct, p, 0)
-    beta = np.zeros(hd.l + 1)
+    forms = {"both": (0, 1), "plain": (0,), "mixed": (1,)}[args.form]
+    runs, betas = {}, {}
+    for prec in forms:
+        lib.irwls_set_precision(prec)
+        beta = np.zeros(hd.l + 1)
 
-    def step():
-        libc.srand(0)
-        if lib.irwls_resident_full(res, p, beta.ctypes.data_as(PD)) != 0:
-            raise SystemExit("training failed: " + lib.irwls_last_error_message().decode())
+        def step():
+            libc.srand(0)
+            if lib.irwls_resident_full(res, p, beta.ctypes.data_as(PD)) != 0:
+                raise SystemExit("training failed: " + lib.irwls_last_error_message().decode())
 
-    for _ in range(args.warmup):
-        step()
-    lib.irwls_profile_enable(1)
-    lib.irwls_profile_reset()
-    launches0 = lib.irwls_kernel_launches()
-    clocks = Clocks(0)
-    clocks.start()
-    times = []
-    for _ in range(args.steps):
-        lib.irwls_l2_flush(512 << 20)
-        lib.irwls_timer_start()
-        step()
-        times.append(lib.irwls_timer_stop() / 1000.0)
-    clk = clocks.stop()
-    launches = lib.irwls_kernel_launches() - launches0
-    shares = {}
-    for slot, name in ((2, "kernel_rowsum"), (3, "cholesky_solve")):
-        ms, n = C.c_double(), C.c_longlong()
-        lib.irwls_profile_read(slot, C.byref(ms), C.byref(n))
-        shares[name] = (ms.value / 1000.0 / args.steps, n.value // args.steps)
-    lib.irwls_profile_enable(0)
-    step_s = statistics.mean(times)
-    e2e = None
-    if not args.no_e2e:
+        for _ in range(args.warmup):
+            step()
+        lib.irwls_profile_enable(1)
+        lib.irwls_profile_reset()
+        launches0 = lib.irwls_kernel_launches()
+        clocks = Clocks(0) if prec == forms[-1] else None
+        if clocks:
+            clocks.start()
+        times = []
+        for _ in range(args.steps):
+            lib.irwls_l2_flush(512 << 20)
+            lib.irwls_timer_start()
+            step()
+            times.append(lib.irwls_timer_stop() / 1000.0)
+        clk = clocks.stop() if clocks else None
+        prof = {name: profile_read(lib, slot, args.steps) for name, slot in (("kernel_rowsums", 2),
+                                                                             ("cholesky_solves", 3))}
+        lib.irwls_profile_enable(0)
+        runs[prec] = {"s": statistics.mean(times), "launches": lib.irwls_kernel_launches() - launches0,
+                      "clocks": clk, "prof": prof}
+        betas[prec] = beta.copy()
+    lib.irwls_resident_free(res)
+    e2e = {}
+    for prec in forms:
+        if args.no_e2e:
+            e2e[prec] = None
+            continue
+        lib.irwls_set_precision(prec)
         h0, d0 = C.c_longlong(), C.c_longlong()
         lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
         e_times = []
@@ -592,39 +650,70 @@ def run_full(args):
             lib.irwls_l2_flush(512 << 20)
             t0 = time.perf_counter()
             libc.srand(0)
-            lib.initMemory(1, FULL["w"] + 1)
+            lib.initMemory(1, cfg["w"] + 1)
             bp = lib.trainFULL(hd.struct, p)
             if not bp:
                 raise SystemExit("e2e training failed: " + lib.irwls_last_error_message().decode())
             e_times.append(time.perf_counter() - t0)
+            libc.free.argtypes = [C.c_void_p]
+            libc.free(C.cast(bp, C.c_void_p))
         h1, d1 = C.c_longlong(), C.c_longlong()
         lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
-        e2e = {"value": round(statistics.mean(e_times), 3), "unit": "s",
-               "h2d_bytes_per_step": int((h1.value - h0.value) // args.steps),
-               "d2h_bytes_per_step": int((d1.value - d0.value) // args.steps)}
-    lib.irwls_resident_free(res)
-    chol_s, chol_n = shares["cholesky_solve"]
-    peak = lib.irwls_fp64_peak_tflops(5)
-    # the systems solved have order ~ working-set free count + 1; their flops
-    # (n^3/3 per factorization) are not recorded per call, so the roofline is
-    # reported for the kernel row sums, with 2 flops per term plus the kernel
-    # entry (3d + 2 FP64 operations and one exp, counted as 3d + 2)
-    roofline = {"bound": "latency", "kernel": "cholesky_solve (blocked panel/update/backsolve launches)",
+        e2e[prec] = {"value": round(statistics.mean(e_times), 3), "unit": "s",
+                     "h2d_bytes_per_step": int((h1.value - h0.value) // args.steps),
+                     "d2h_bytes_per_step": int((d1.value - d0.value) // args.steps)}
+    lib.irwls_set_precision(0)
+
+    def test_acc(beta):
+        bb = np.ascontiguousarray(beta)
+        mdl = lib.calculateFULLModel(p, hd.struct, bb.ctypes.data_as(PD))
+        pred = np.ctypeslib.as_array(lib.test(ht.struct, mdl, _abi.make_predict_properties(soft=0)),
+                                     shape=(ht.l,)).copy()
+        lib.freeModel(mdl)
+        return float((pred == yt).mean())
+
+    head = forms[-1]
+    accuracy = None
+    if forms == (0, 1):
+        d0, d1 = dual_objective(hd, betas[0], cfg["gamma"]), dual_objective(hd, betas[1], cfg["gamma"])
+        a0, a1 = test_acc(betas[0]), test_acc(betas[1])
+        rel = abs(d1 - d0) / abs(d0)
+        ok = rel <= PRIMAL_BAR and abs(a1 - a0) <= ACC_BAR
+        accuracy = {"dual_rel_err_vs_plain": rel, "dual_plain": d0, "dual_mixed": d1, "test_acc_plain": a0,
+                    "test_acc_mixed": a1, "test_acc_change": a1 - a0,
+                    "support_vectors": {"plain": int((betas[0][:-1] != 0).sum()),
+                                        "mixed": int((betas[1][:-1] != 0).sum())},
+                    "bars": {"dual_rel_err": PRIMAL_BAR, "test_acc_change": ACC_BAR}, "meets_bars": ok}
+        if not ok:
+            head = 0
+    r = runs[head]
+    value = r["s"]
+    peak = lib.irwls_fp64_peak_tflops(3)
+    roofline = {"bound": "latency" if head == 0 else "mixed",
+                "kernel": "kernel row sums (FP64 ordered) and Cholesky solves",
                 "achieved": None, "peak": round(peak, 4), "unit": "TFLOP/s", "frac": None, "traffic": None,
-                "share_of_step": round(chol_s / step_s, 4), "launches_per_step": int(chol_n),
-                "rowsum_share_of_step": round(shares["kernel_rowsum"][0] / step_s, 4)}
-    base = None if args.no_cpu else full_cpu(hd)
-    print(json.dumps({"metric": METRIC, "value": round(step_s, 3), "unit": "s", "n_gpus": args.gpus,
-                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1000, 1),
-                      "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                      "data": "synthetic (seeded generator)", "config": full_config(), "e2e": e2e,
-                      "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": base,
-                      "clocks": clk}), flush=True)
+                "share_of_step": {k: round(v[0] / value, 4) for k, v in r["prof"].items()},
+                "launches_per_step": {k: int(v[1]) for k, v in r["prof"].items()}}
+    base = None if args.no_cpu else full_cpu(hd, cfg)
+    plain = None
+    if 0 in runs and head != 0:
+        plain = {"value": round(runs[0]["s"], 3), "unit": "s", "e2e": e2e[0],
+                 "breakdown_s": {k: round(v[0], 4) for k, v in runs[0]["prof"].items()}}
+    print(json.dumps({"metric": METRIC, "value": round(value, 3), "unit": "s", "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1000, 1),
+                      "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "f64" if head == 0 else "bf16x6 (error updates off the exact set) + f64",
+                      "data": "synthetic (seeded generator)",
+                      "config": full_config(cfg, "plain FP64" if head == 0 else "precision (mixed)"),
+                      "e2e": e2e[head], "gpu_launches": int(r["launches"]), "roofline": roofline,
+                      "cpu_baseline": base, "clocks": runs[forms[-1]]["clocks"],
+                      "speedup_vs_plain_fp64": round(runs[0]["s"] / value, 2) if 0 in runs else None,
+                      "accuracy": accuracy, "plain_fp64": plain}), flush=True)
 
 
 def main():
     args = parse()
-    if args.workload == "full":
+    if args.workload in FULL:
         run_full(args)
     elif args.impl == "reference":
         run_reference(args)
