@@ -77,6 +77,27 @@ double irwls_timer_stop(void);
 /* FP64 FMA throughput of the device (TFLOP/s), measured by a DFMA-chain
  * kernel: the roofline denominator of the FP64 kernels. */
 double irwls_fp64_peak_tflops(int reps);
+/* Batching form: `count` independent trainings run concurrently, `workers`
+ * at a time (<= 0: the autotuned count, 16 before any tuning), each on its
+ * own CUDA stream with its own random generator. SVM i draws the sequence
+ * srand(seeds[i]) would give (seeds NULL: 1 for every SVM), so its result
+ * equals trainFULL(datasets[i], props[i]) -- or SGMA / randomCentroids then
+ * IRWLSpar -- called after srand(seeds[i]). Outputs are malloc'd arrays
+ * (betas[i]: l_i + 1 values; centroids[i] / weights[i]: props[i].size
+ * values) that the caller frees; NULL for an SVM that failed. Returns 0 or
+ * the first error. These have no counterpart in the reference. */
+int irwls_full_train_batch(const svm_dataset *datasets, const properties *props, const unsigned *seeds, int count,
+                           int workers, double **betas);
+int irwls_budgeted_train_batch(const svm_dataset *datasets, const properties *props, const unsigned *seeds,
+                               int count, int workers, int **centroids, double **weights);
+/* Times full trainings of the `sample` largest SVMs of the batch at 4 to 48
+ * concurrent workers, keeps the fastest count for later batches and returns
+ * it (-1 on error). */
+int irwls_batch_autotune(const svm_dataset *datasets, const properties *props, int count, int sample);
+/* Fixes the worker count used when a batch is called with workers <= 0. */
+void irwls_batch_set_workers(int workers);
+/* n numbers of the library's equivalent of libc's srand(seed); rand(). */
+void irwls_rand_sequence(unsigned seed, int n, int *out);
 /* FP32 FMA throughput of the device (TFLOP/s, one FMA = 2 flops), measured
  * the same way: the denominator of the precision form's double-float Gram. */
 double irwls_fp32_peak_tflops(int reps);

@@ -52,6 +52,12 @@ def load() -> C.CDLL:
         "irwls_fp32_peak_tflops": (C.c_double, [C.c_int]),
         "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "irwls_last_gram_flops": (C.c_double, []),
+        "irwls_full_train_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+        "irwls_budgeted_train_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                 C.c_void_p]),
+        "irwls_batch_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+        "irwls_batch_set_workers": (None, [C.c_int]),
+        "irwls_rand_sequence": (None, [C.c_uint, C.c_int, C.POINTER(C.c_int)]),
         "irwls_tc_status": (C.c_int, []),
         "irwls_set_precision": (None, [C.c_int]),
         "irwls_get_precision": (C.c_int, []),

@@ -3,8 +3,9 @@
  * SGMA centroid selection (reference src/budgeted-train.c:114-309), random
  * centroids (:73-100), IRWLSpar (:324-505) and the model packing (:519-570).
  *
- * SGMA's 64 candidates per step are drawn with libc rand() in exactly the
- * order of the reference run with one thread. The draws depend only on the
+ * SGMA's 64 candidates per step are drawn with rand() (irwls_rand: libc's on
+ * the main thread, an identical per-thread generator in batch workers) in
+ * exactly the order of the reference run with one thread. The draws depend only on the
  * labels, so all of them are made before the first kernel is launched and
  * the whole selection runs without a host synchronisation; the per-step
  * "Best Error Descent" lines are printed from device records at the end.
@@ -21,7 +22,7 @@ int *randomCentroids(svm_dataset dataset, properties props) {
     int *p = (int *)malloc((dataset.l > 0 ? dataset.l : 1) * sizeof(int));
     for (int i = 0; i < dataset.l; ++i) p[i] = i;
     for (int i = dataset.l - 1; i >= 0; --i) {
-        const int j = rand() % (i + 1);
+        const int j = irwls_rand() % (i + 1);
         const int t = p[i];
         p[i] = p[j];
         p[j] = t;
@@ -50,8 +51,8 @@ int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m) {
     for (int s = 2; s < m; s++)
         for (int i = 0; i < 64; i++) {
             const double want = (i % 2) * 2.0 - 1;
-            int pick = rand() % (ds->l);
-            while (ds->y[pick] != want) pick = rand() % (ds->l);
+            int pick = irwls_rand() % (ds->l);
+            while (ds->y[pick] != want) pick = irwls_rand() % (ds->l);
             cand[(size_t)s * 64 + i] = pick;
         }
     return cand;

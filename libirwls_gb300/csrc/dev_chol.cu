@@ -241,8 +241,6 @@ int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Di
     return 0;
 }
 
-double *g_diag = nullptr;  // factored diagonal blocks, grow-only
-size_t g_diag_bytes = 0;
 
 }  // namespace
 
@@ -272,19 +270,11 @@ extern "C" int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_
         }
     }
     const int npanel = ceil_div(n, NB);
-    const size_t dbytes = (size_t)npanel * NB * NB * sizeof(double);
-    if (dbytes > g_diag_bytes) {
-        if (g_diag) {
-            cudaStreamSynchronize(irwls_stream());
-            cudaFree(g_diag);
-        }
-        g_diag = nullptr;
-        g_diag_bytes = 0;
-        if (irwls_dev_malloc((void **)&g_diag, dbytes)) return -3;
-        g_diag_bytes = dbytes;
-    }
+    // factored diagonal blocks: the context's grow-only scratch slot 0
+    double *diag = (double *)irwls_ctx_scratch(0, (size_t)npanel * NB * NB * sizeof(double));
+    if (!diag) return -3;
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_CHOL);
-    int rc = chol_enqueue(d_M, n, ld, d_x, flags, g_diag, irwls_stream());
+    int rc = chol_enqueue(d_M, n, ld, d_x, flags, diag, irwls_stream());
     if (rc) return rc;
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_CHOL);
     return 0;

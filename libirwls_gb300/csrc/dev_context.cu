@@ -1,43 +1,102 @@
-// dev_context.cu -- device context of the library: one CUDA stream, error
+// dev_context.cu -- device context of the library: the CUDA stream, error
 // state, memory helpers, dataset upload and kernel timing.
+//
+// Every host thread works in an execution context: its stream, its device
+// status words, its error slot, its grow-only scratch buffers and its random
+// generator. The main thread uses the default context (whose generator is
+// libc rand(), as in the reference); the batch driver gives each worker
+// thread a context of its own (irwls_ctx_create / irwls_ctx_bind) so that
+// trainings run concurrently on separate streams. Device memory is allocated
+// stream-ordered (cudaMallocAsync / cudaFreeAsync on the context's stream),
+// so that no thread's free waits for the whole device.
 #include <stdarg.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <vector>
 
 #include "dev_common.cuh"
 
-static cudaStream_t g_stream = nullptr;
-static int g_inited = 0;
-static int g_num_sms = 0;
-static int g_err = 0;
-static char g_msg[512] = "";
-static long long g_launches = 0;
+namespace {
 
-static int *g_flags = nullptr;  // device status words, see irwls_dev_flags()
+constexpr int IRWLS_SCRATCH_SLOTS = 4;
+
+// glibc's rand() generator (the additive feedback generator of degree 31 and
+// separation 3 behind its random_r), restated so that a worker thread can
+// reproduce exactly the numbers srand(seed) then rand() would give in a
+// single-threaded run, without sharing libc's state.
+struct Rand31 {
+    int32_t r[31];
+    int f, b;
+    void seed(unsigned s) {
+        int32_t w = (int32_t)(s == 0 ? 1u : s);
+        r[0] = w;
+        for (int i = 1; i < 31; ++i) {
+            // 16807 * w mod (2^31 - 1) without overflow (Schrage's method)
+            const int32_t hi = w / 127773, lo = w % 127773;
+            w = 16807 * lo - 2836 * hi;
+            if (w < 0) w += 2147483647;
+            r[i] = w;
+        }
+        f = 3;
+        b = 0;
+        for (int i = 0; i < 310; ++i) next();
+    }
+    int next() {
+        const uint32_t v = (uint32_t)r[f] + (uint32_t)r[b];
+        r[f] = (int32_t)v;
+        const int out = (int)(v >> 1);
+        if (++f >= 31) f = 0;
+        if (++b >= 31) b = 0;
+        return out;
+    }
+};
+
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    int *flags = nullptr;  // device status words, see irwls_dev_flags()
+    int err = 0;
+    char msg[512] = "";
+    void *scratch[IRWLS_SCRATCH_SLOTS] = {};
+    size_t scratch_bytes[IRWLS_SCRATCH_SLOTS] = {};
+    int own_rng = 0;
+    Rand31 rng;
+};
+
+Ctx g_default;
+thread_local Ctx *t_ctx = nullptr;
+inline Ctx *cur() { return t_ctx ? t_ctx : &g_default; }
+
+int g_inited = 0;
+int g_num_sms = 0;
+std::atomic<long long> g_launches{0};
+
+}  // namespace
 
 extern "C" void irwls_set_error(int code, const char *fmt, ...) {
-    if (g_err) return;  // keep the first error
-    g_err = code;
+    Ctx *c = cur();
+    if (c->err) return;  // keep the first error
+    c->err = code;
     va_list ap;
     va_start(ap, fmt);
-    vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+    vsnprintf(c->msg, sizeof c->msg, fmt, ap);
     va_end(ap);
 }
-extern "C" int irwls_get_error(void) { return g_err; }
-extern "C" const char *irwls_get_error_message(void) { return g_msg; }
+extern "C" int irwls_get_error(void) { return cur()->err; }
+extern "C" const char *irwls_get_error_message(void) { return cur()->msg; }
 extern "C" void irwls_clear_error(void) {
-    g_err = 0;
-    g_msg[0] = 0;
+    cur()->err = 0;
+    cur()->msg[0] = 0;
 }
 
-cudaStream_t irwls_stream() { return g_stream; }
-int *irwls_dev_flags() { return g_flags; }
+cudaStream_t irwls_stream() { return cur()->stream; }
+int *irwls_dev_flags() { return cur()->flags; }
 int irwls_num_sms() { return g_num_sms; }
 
-extern "C" long long irwls_launch_count(void) { return g_launches; }
+extern "C" long long irwls_launch_count(void) { return g_launches.load(); }
 extern "C" void irwls_count_launch(int n) { g_launches += n; }
 
 static int cuda_fail(cudaError_t e, const char *what) {
@@ -48,6 +107,15 @@ static int cuda_fail(cudaError_t e, const char *what) {
 int irwls_check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, what);
+    return 0;
+}
+
+static int ctx_open(Ctx *c) {
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamCreate");
+    if ((e = cudaMalloc((void **)&c->flags, 8 * sizeof(int))) != cudaSuccess) return cuda_fail(e, "flags alloc");
+    if ((e = cudaMemset(c->flags, 0, 8 * sizeof(int))) != cudaSuccess) return cuda_fail(e, "flags init");
     return 0;
 }
 
@@ -64,16 +132,80 @@ extern "C" int irwls_dev_init(void) {
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if ((e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
         return cuda_fail(e, "cudaDeviceGetAttribute");
-    if ((e = cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking)) != cudaSuccess)
-        return cuda_fail(e, "cudaStreamCreate");
-    if ((e = cudaMalloc((void **)&g_flags, 8 * sizeof(int))) != cudaSuccess) return cuda_fail(e, "flags alloc");
-    if ((e = cudaMemset(g_flags, 0, 8 * sizeof(int))) != cudaSuccess) return cuda_fail(e, "flags init");
+    if (ctx_open(&g_default)) return -2;
     g_inited = 1;
     return 0;
 }
 
+// Execution contexts of worker threads (the library must be initialised).
+extern "C" void *irwls_ctx_create(void) {
+    if (irwls_dev_init()) return nullptr;
+    Ctx *c = new Ctx();
+    if (ctx_open(c)) {
+        delete c;
+        return nullptr;
+    }
+    c->own_rng = 1;
+    c->rng.seed(1);
+    return c;
+}
+extern "C" void irwls_ctx_bind(void *h) { t_ctx = (Ctx *)h; }
+extern "C" void irwls_ctx_destroy(void *h) {
+    Ctx *c = (Ctx *)h;
+    if (!c) return;
+    cudaStreamSynchronize(c->stream);
+    for (int k = 0; k < IRWLS_SCRATCH_SLOTS; ++k)
+        if (c->scratch[k]) cudaFreeAsync(c->scratch[k], c->stream);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->flags);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+// Error of a context (for the thread that created it, after a worker ended).
+extern "C" int irwls_ctx_error(void *h, char *msg, int cap) {
+    Ctx *c = (Ctx *)h;
+    if (msg && cap > 0) snprintf(msg, (size_t)cap, "%s", c->msg);
+    return c->err;
+}
+
+// The current context's random numbers: libc rand() in the default context,
+// the context's own glibc-equivalent generator in worker contexts.
+extern "C" void irwls_srand(unsigned seed) {
+    Ctx *c = cur();
+    if (c->own_rng) c->rng.seed(seed);
+    else srand(seed);
+}
+extern "C" int irwls_rand(void) {
+    Ctx *c = cur();
+    return c->own_rng ? c->rng.next() : rand();
+}
+// n numbers of a private generator seeded with `seed` (tests compare them
+// with libc's srand/rand).
+extern "C" void irwls_rand_sequence(unsigned seed, int n, int *out) {
+    Rand31 g;
+    g.seed(seed);
+    for (int i = 0; i < n; ++i) out[i] = g.next();
+}
+
+// Grow-only scratch buffer `slot` of the current context (stream-ordered).
+extern "C" void *irwls_ctx_scratch(int slot, size_t bytes) {
+    Ctx *c = cur();
+    if (bytes > c->scratch_bytes[slot]) {
+        if (c->scratch[slot]) cudaFreeAsync(c->scratch[slot], c->stream);
+        c->scratch[slot] = nullptr;
+        c->scratch_bytes[slot] = 0;
+        if (cudaMallocAsync(&c->scratch[slot], bytes, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            irwls_set_error(-3, "device scratch of %zu bytes failed", bytes);
+            return nullptr;
+        }
+        c->scratch_bytes[slot] = bytes;
+    }
+    return c->scratch[slot];
+}
+
 extern "C" int irwls_dev_sync(void) {
-    cudaError_t e = cudaStreamSynchronize(g_stream);
+    cudaError_t e = cudaStreamSynchronize(cur()->stream);
     if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
     return 0;
 }
@@ -81,39 +213,40 @@ extern "C" int irwls_dev_sync(void) {
 extern "C" int irwls_dev_malloc(void **p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = cudaMallocAsync(p, bytes, cur()->stream);
     if (e != cudaSuccess) {
-        irwls_set_error(-3, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        cudaGetLastError();
+        irwls_set_error(-3, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
         *p = nullptr;
         return -3;
     }
     return 0;
 }
 extern "C" int irwls_dev_free(void *p) {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, cur()->stream);
     return 0;
 }
 extern "C" void irwls_count_bytes(long long h2d, long long d2h);
 extern "C" int irwls_dev_h2d(void *d, const void *h, size_t bytes) {
     if (!bytes) return 0;
     irwls_count_bytes((long long)bytes, 0);
-    cudaError_t e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g_stream);
+    cudaError_t e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, cur()->stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "H2D copy");
 }
 extern "C" int irwls_dev_d2h(void *h, const void *d, size_t bytes) {
     if (!bytes) return 0;
     irwls_count_bytes(0, (long long)bytes);
-    cudaError_t e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, g_stream);
+    cudaError_t e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, cur()->stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "D2H copy");
 }
 extern "C" int irwls_dev_d2d(void *d, const void *s, size_t bytes) {
     if (!bytes) return 0;
-    cudaError_t e = cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToDevice, g_stream);
+    cudaError_t e = cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToDevice, cur()->stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "D2D copy");
 }
 extern "C" int irwls_dev_memset(void *d, int byte, size_t bytes) {
     if (!bytes) return 0;
-    cudaError_t e = cudaMemsetAsync(d, byte, bytes, g_stream);
+    cudaError_t e = cudaMemsetAsync(d, byte, bytes, cur()->stream);
     return e == cudaSuccess ? 0 : cuda_fail(e, "memset");
 }
 extern "C" int irwls_dev_host_alloc(void **p, size_t bytes) {
@@ -128,29 +261,15 @@ extern "C" void irwls_dev_host_free(void *p) {
     if (p) cudaFreeHost(p);
 }
 
-static void *g_ws = nullptr;
-static size_t g_ws_bytes = 0;
 extern "C" int irwls_dev_workspace(size_t bytes, void **d_ws) {
-    if (bytes > g_ws_bytes) {
-        if (g_ws) {
-            cudaStreamSynchronize(g_stream);
-            cudaFree(g_ws);
-            g_ws = nullptr;
-            g_ws_bytes = 0;
-        }
-        if (irwls_dev_malloc(&g_ws, bytes)) return -3;
-        g_ws_bytes = bytes;
-    }
-    *d_ws = g_ws;
-    return 0;
+    *d_ws = irwls_ctx_scratch(1, bytes);
+    return *d_ws ? 0 : -3;
 }
 extern "C" void irwls_dev_release_workspace(void) {
-    if (g_ws) {
-        cudaStreamSynchronize(g_stream);
-        cudaFree(g_ws);
-    }
-    g_ws = nullptr;
-    g_ws_bytes = 0;
+    Ctx *c = cur();
+    if (c->scratch[1]) cudaFreeAsync(c->scratch[1], c->stream);
+    c->scratch[1] = nullptr;
+    c->scratch_bytes[1] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -270,13 +389,8 @@ extern "C" int irwls_dev_upload_model(const model *m, int width_hint, irwls_dev_
 
 extern "C" void irwls_dev_release(irwls_dev_set *s) {
     if (!s) return;
-    cudaStreamSynchronize(g_stream);
-    cudaFree(s->X);
-    cudaFree(s->q);
-    cudaFree(s->y);
-    cudaFree(s->rp);
-    cudaFree(s->ci);
-    cudaFree(s->cv);
+    void *b[] = {s->X, s->q, s->y, s->rp, s->ci, s->cv};
+    for (void *p : b) irwls_dev_free(p);
     memset(s, 0, sizeof *s);
 }
 
@@ -302,25 +416,26 @@ static cudaEvent_t prof_event(ProfSlot &s) {
     cudaEventCreate(&e);
     return e;
 }
+// Kernel timing is recorded in the default context only.
 extern "C" void irwls_prof_enable(int on) { g_prof_on = on; }
-extern "C" int irwls_prof_on(void) { return g_prof_on; }
+extern "C" int irwls_prof_on(void) { return g_prof_on && !t_ctx; }
 extern "C" void irwls_prof_begin(int slot) {
-    if (!g_prof_on) return;
+    if (!irwls_prof_on()) return;
     ProfSlot &s = g_prof[slot];
     cudaEvent_t e = prof_event(s);
-    cudaEventRecord(e, g_stream);
+    cudaEventRecord(e, g_default.stream);
     s.pending.push_back(e);
 }
 extern "C" void irwls_prof_end(int slot) {
-    if (!g_prof_on) return;
+    if (!irwls_prof_on()) return;
     ProfSlot &s = g_prof[slot];
     cudaEvent_t e = prof_event(s);
-    cudaEventRecord(e, g_stream);
+    cudaEventRecord(e, g_default.stream);
     s.pending.push_back(e);
     if (s.pending.size() > 4096) irwls_prof_collect();
 }
 extern "C" int irwls_prof_collect(void) {
-    cudaStreamSynchronize(g_stream);
+    cudaStreamSynchronize(g_default.stream);
     for (auto &s : g_prof) {
         for (size_t i = 0; i + 1 < s.pending.size(); i += 2) {
             float ms = 0.f;
@@ -348,7 +463,7 @@ extern "C" void irwls_prof_reset(void) {
 
 extern "C" int irwls_dev_chol_info(int *info) {
     int flags[8];
-    cudaError_t e = cudaMemcpyAsync(flags, g_flags, sizeof flags, cudaMemcpyDeviceToHost, g_stream);
+    cudaError_t e = cudaMemcpyAsync(flags, cur()->flags, sizeof flags, cudaMemcpyDeviceToHost, cur()->stream);
     if (e != cudaSuccess) return cuda_fail(e, "read flags");
     if (irwls_dev_sync()) return -2;
     *info = flags[0];
@@ -360,14 +475,14 @@ extern "C" int irwls_dev_chol_info(int *info) {
 // the device's FP64 FMA throughput (the roofline denominator of the FP64
 // kernels: chains of independent DFMAs, no memory traffic).
 // ---------------------------------------------------------------------------
-static long long g_h2d = 0, g_d2h = 0;
+static std::atomic<long long> g_h2d{0}, g_d2h{0};
 extern "C" void irwls_count_bytes(long long h2d, long long d2h) {
     g_h2d += h2d;
     g_d2h += d2h;
 }
 extern "C" void irwls_transfer_bytes(long long *h2d, long long *d2h) {
-    *h2d = g_h2d;
-    *d2h = g_d2h;
+    *h2d = g_h2d.load();
+    *d2h = g_d2h.load();
 }
 
 static void *g_flush = nullptr;
@@ -384,11 +499,11 @@ extern "C" int irwls_timer_start(void) {
         cudaEventCreate(&g_t0);
         cudaEventCreate(&g_t1);
     }
-    cudaEventRecord(g_t0, g_stream);
+    cudaEventRecord(g_t0, cur()->stream);
     return 0;
 }
 extern "C" double irwls_timer_stop(void) {
-    cudaEventRecord(g_t1, g_stream);
+    cudaEventRecord(g_t1, cur()->stream);
     cudaEventSynchronize(g_t1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, g_t0, g_t1);
@@ -434,11 +549,11 @@ extern "C" double irwls_fp32_peak_tflops(int reps) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     double best = 0.0;
-    fp32_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
+    fp32_probe_kernel<<<blocks, threads, 0, cur()->stream>>>(d, iters);
     for (int r = 0; r < reps; ++r) {
-        cudaEventRecord(e0, g_stream);
-        fp32_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
-        cudaEventRecord(e1, g_stream);
+        cudaEventRecord(e0, cur()->stream);
+        fp32_probe_kernel<<<blocks, threads, 0, cur()->stream>>>(d, iters);
+        cudaEventRecord(e1, cur()->stream);
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
@@ -447,7 +562,8 @@ extern "C" double irwls_fp32_peak_tflops(int reps) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(d);
+    irwls_dev_free(d);
+    irwls_dev_sync();
     return best;
 }
 
@@ -461,11 +577,11 @@ extern "C" double irwls_fp64_peak_tflops(int reps) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     double best = 0.0;
-    fp64_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
+    fp64_probe_kernel<<<blocks, threads, 0, cur()->stream>>>(d, iters);
     for (int r = 0; r < reps; ++r) {
-        cudaEventRecord(e0, g_stream);
-        fp64_probe_kernel<<<blocks, threads, 0, g_stream>>>(d, iters);
-        cudaEventRecord(e1, g_stream);
+        cudaEventRecord(e0, cur()->stream);
+        fp64_probe_kernel<<<blocks, threads, 0, cur()->stream>>>(d, iters);
+        cudaEventRecord(e1, cur()->stream);
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
@@ -474,6 +590,7 @@ extern "C" double irwls_fp64_peak_tflops(int reps) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(d);
+    irwls_dev_free(d);
+    irwls_dev_sync();
     return best;
 }

@@ -19,7 +19,7 @@ int *rpermute(int n) {
     int *p = (int *)malloc((n > 0 ? n : 1) * sizeof(int));
     for (int k = 0; k < n; k++) p[k] = k;
     for (int k = n - 1; k > 0; k--) {
-        const int j = rand() % (k + 1);
+        const int j = irwls_rand() % (k + 1);
         const int t = p[j];
         p[j] = p[k];
         p[k] = t;

@@ -25,6 +25,18 @@ void irwls_clear_error(void);
 /* ---- context ------------------------------------------------------------ */
 int irwls_dev_init(void);                     /* idempotent; creates the stream */
 int irwls_dev_sync(void);                     /* waits for the stream, checks device flags */
+/* Execution contexts (dev_context.cu): a worker thread binds a context of its
+ * own (stream, status words, errors, scratch, random generator); NULL binds
+ * the default context of the main thread. */
+void *irwls_ctx_create(void);
+void irwls_ctx_bind(void *h);
+void irwls_ctx_destroy(void *h);
+int irwls_ctx_error(void *h, char *msg, int cap);
+void *irwls_ctx_scratch(int slot, size_t bytes);   /* grow-only, slots 0..3 */
+/* The context's random numbers: libc srand/rand in the default context, a
+ * generator that reproduces them exactly in worker contexts. */
+void irwls_srand(unsigned seed);
+int irwls_rand(void);
 int irwls_dev_malloc(void **p, size_t bytes);
 int irwls_dev_free(void *p);
 int irwls_dev_h2d(void *d_dst, const void *h_src, size_t bytes);   /* async */

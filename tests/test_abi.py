@@ -85,3 +85,17 @@ def test_training_without_gpu_fails_loudly():
     assert not lib.trainFULL(tr.struct, prop)
     assert lib.irwls_last_error() != 0
     assert b"CUDA" in lib.irwls_last_error_message() or b"device" in lib.irwls_last_error_message()
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 7, 12345, 2**31 - 1, 2**32 - 1])
+def test_batch_generator_reproduces_libc_rand(seed):
+    """Batch workers draw from the library's restatement of glibc's rand():
+    it must give exactly the libc sequence after srand(seed)."""
+    lib = load()
+    n = 2000
+    out = (C.c_int * n)()
+    lib.irwls_rand_sequence(seed, n, out)
+    libc = C.CDLL(None)
+    libc.srand(C.c_uint(seed))
+    ref = [libc.rand() for _ in range(n)]
+    assert list(out) == ref
