@@ -42,6 +42,11 @@ of the precision form (n = 100000, d = 784 8-bit values at 19% density from
 same bars (dual objective instead of primal); their CPU baseline is the
 restatement's whole training on all host cores (no extrapolation).
 
+`--workload batch` measures the batching form: 72 SVMs (a C x gamma grid of
+RBF SVMs plus linear ones) on subsets of 2000-50000 rows trained concurrently
+(worker count from the library's autotuner) against the same SVMs trained one
+at a time; every SVM's weights must be bitwise identical in both.
+
 `--impl reference` runs only the CPU baseline measurement above (the reference
 sources cannot be built on the GPU host, so the restatement stands in for it)
 and prints its line with "impl": "reference".
@@ -81,7 +86,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
-    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784"])
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch"])
     ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
@@ -711,10 +716,133 @@ def run_full(args):
                       "accuracy": accuracy, "plain_fp64": plain}), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# batching form: many SVMs trained concurrently
+# ----------------------------------------------------------------------------
+BATCH_DESC = ("batching form: 64 RBF SVMs (C in logspace(-1,3,8) x gamma in logspace(-3,0,8)) + 8 linear SVMs, "
+              "full IRWLS, working set 500, each on its own subset (n log-uniform in [2000, 50000]) of a CSR pool "
+              "(d=300, 3% density, binary/[0,1] values, labels from a seeded sparse linear rule, 8% flipped)")
+
+
+def batch_cpu(hds, prs, k=3):
+    """The restatement trains the k smallest SVMs of the batch on all host
+    cores; scaled to the batch by total rows."""
+    from libirwls_gb300 import _abi
+
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    port_path = os.path.join(ROOT, "oracle", "_build", "libirwls_port.so")
+    if not os.path.exists(port_path):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+    port = _abi.load_library(port_path)
+    cores = os.cpu_count() or 1
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    order = sorted(range(len(hds)), key=lambda i: hds[i].l)[:k]
+    t0 = time.perf_counter()
+    for i in order:
+        p = prs[i]
+        p.Threads = cores
+        port.initMemory(cores, p.MaxSize + 1)
+        libc.srand(i)
+        libc.free(C.cast(port.trainFULL(hds[i].struct, p), C.c_void_p))
+        p.Threads = 1
+    dt = time.perf_counter() - t0
+    rows_s = sum(hds[i].l for i in order)
+    scale = sum(h.l for h in hds) / rows_s
+    return {"value": round(dt * scale, 3), "unit": "s", "cores": cores, "kind": "port",
+            "sample": "CPU restatement of the reference, %d OpenMP threads, on the %d smallest SVMs (%d rows, "
+                      "%.1f s), scaled by total rows x %.1f" % (cores, k, rows_s, dt, scale)}
+
+
+def run_batch(args):
+    import numpy as np
+
+    from libirwls_gb300 import _abi, load, synth
+
+    pool, jobs = synth.batch_workload()
+    hds, prs = [], []
+    for rows, kern, cost, gamma in jobs:
+        sub = synth.subset(pool, rows)
+        hds.append(_abi.build_dataset(sub.indptr, sub.indices, sub.values, sub.y))
+        prs.append(_abi.make_properties(gamma=gamma, C_=cost, kernel=kern, working_set=500))
+    n = len(jobs)
+    cfg = {"workload": BATCH_DESC, "svms": n, "rows_total": int(sum(h.l for h in hds)),
+           "rows_min": int(min(h.l for h in hds)), "rows_max": int(max(h.l for h in hds)),
+           "form": "batching (concurrent trainings on separate streams)", "parallelism": "single GPU",
+           "l2": "the datasets (tens of MB each) are uploaded per training; L2 flushed between steps"}
+    if args.impl == "reference":
+        base = batch_cpu(hds, prs)
+        print(json.dumps({"metric": METRIC, "value": base["value"], "unit": "s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": base["value"] * 1000,
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded generator)", "config": cfg, "cpu_baseline": base,
+                          "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    lib = load()
+    if not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    dss = (_abi.SvmDataset * n)(*[h.struct for h in hds])
+    pp = (_abi.Properties * n)(*prs)
+    seeds = (C.c_uint * n)(*range(n))
+    workers = lib.irwls_batch_autotune(dss, pp, n, 8)
+    if workers <= 0:
+        raise SystemExit("autotune failed: " + lib.irwls_last_error_message().decode())
+
+    def batch(w):
+        out = (PD * n)()
+        lib.irwls_l2_flush(512 << 20)
+        lib.irwls_dev_sync()
+        h0, d0 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
+        t0 = time.perf_counter()
+        if lib.irwls_full_train_batch(dss, pp, seeds, n, w, out) != 0:
+            raise SystemExit("batch failed: " + lib.irwls_last_error_message().decode())
+        dt = time.perf_counter() - t0
+        h1, d1 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
+        res = [np.ctypeslib.as_array(out[i], shape=(hds[i].l + 1,)).copy() for i in range(n)]
+        return dt, res, h1.value - h0.value, d1.value - d0.value
+
+    seq_s, seq_res, _, _ = batch(1)
+    for _ in range(args.warmup):
+        batch(workers)
+    launches0 = lib.irwls_kernel_launches()
+    clocks = Clocks(0)
+    clocks.start()
+    times, h2d, d2h = [], 0, 0
+    for _ in range(args.steps):
+        dt, res, hb, db = batch(workers)
+        times.append(dt)
+        h2d, d2h = hb, db
+    clk = clocks.stop()
+    launches = lib.irwls_kernel_launches() - launches0
+    identical = all(np.array_equal(a, b) for a, b in zip(res, seq_res))
+    value = statistics.mean(times)
+    nsv = [int((r[:-1] != 0).sum()) for r in res]
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 1), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": dict(cfg, workers=workers, autotuned=True),
+            "e2e": {"value": round(value, 3), "unit": "s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "note": "the batch API takes host svm_datasets: every timed step uploads them"},
+            "gpu_launches": int(launches // max(args.steps, 1)),
+            "roofline": {"bound": "latency", "kernel": "concurrent trainings", "achieved": None, "peak": None,
+                         "unit": None, "frac": None, "traffic": None},
+            "cpu_baseline": None if args.no_cpu else batch_cpu(hds, prs), "clocks": clk,
+            "sequential_plain_fp64_s": round(seq_s, 3), "speedup_vs_plain_fp64": round(seq_s / value, 2),
+            "svms_per_s": round(n / value, 2), "identical_to_sequential": bool(identical),
+            "support_vectors": {"min": min(nsv), "max": max(nsv), "total": sum(nsv)}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload in FULL:
         run_full(args)
+    elif args.workload == "batch":
+        run_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

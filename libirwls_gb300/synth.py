@@ -140,6 +140,51 @@ def precision_full_workload(n_train=100_000, n_test=10_000, seed=20240606):
     return from_dense(Xtr, ytr, keep_zeros=False), from_dense(Xte, yte, keep_zeros=False)
 
 
+def sparse_linear_pool(n: int = 50_000, d: int = 300, density: float = 0.03, seed: int = 20240607,
+                       rule_nnz: int = 100, flip: float = 0.08) -> Sparse:
+    """CSR rows over d features at the given density: even features are
+    binary (1.0), odd ones U(0, 1). Labels are the sign of a seeded sparse
+    linear rule (rule_nnz N(0, 1) weights, centred at its median), with a
+    fraction ``flip`` flipped."""
+    rng = np.random.default_rng(seed)
+    mask = rng.random((n, d)) < density
+    vals = np.where(np.arange(d) % 2 == 0, 1.0, rng.random((n, d)))
+    X = np.where(mask, vals, 0.0)
+    w = np.zeros(d)
+    w[rng.choice(d, size=rule_nnz, replace=False)] = rng.standard_normal(rule_nnz)
+    s = X @ w
+    y = np.where(s >= np.median(s), 1.0, -1.0)
+    y = np.where(rng.random(n) < flip, -y, y)
+    return from_dense(X, y, keep_zeros=False)
+
+
+def subset(data: Sparse, rows) -> Sparse:
+    """The given rows of a CSR set, in the given order."""
+    rows = np.asarray(rows)
+    counts = np.diff(data.indptr)[rows]
+    indptr = np.concatenate([[0], np.cumsum(counts)])
+    take = np.concatenate([np.arange(data.indptr[r], data.indptr[r + 1]) for r in rows]) if len(rows) else []
+    take = np.asarray(take, dtype=np.int64)
+    return Sparse(indptr, data.indices[take], data.values[take], data.y[rows], data.d)
+
+
+def batch_workload(seed: int = 20240608, n_min: int = 2000, n_max: int = 50_000, linear: int = 8):
+    """SVMs of the batching form: an 8 x 8 grid of C in logspace(-1, 3, 8) x
+    gamma in logspace(-3, 0, 8) (RBF) plus ``linear`` linear-kernel SVMs over
+    the C grid, each on its own random subset of the pool with a size drawn
+    log-uniform in [n_min, n_max]. Returns (pool, [(rows, kernel, C, gamma)])."""
+    pool = sparse_linear_pool()
+    rng = np.random.default_rng(seed)
+    Cs, gammas = np.logspace(-1, 3, 8), np.logspace(-3, 0, 8)
+    specs = [(1, c, g) for c in Cs for g in gammas] + [(0, Cs[k % 8], 1.0) for k in range(linear)]
+    jobs = []
+    for kern, c, g in specs:
+        n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        rows = np.sort(rng.choice(pool.n, size=n, replace=False))
+        jobs.append((rows, kern, float(c), float(g)))
+    return pool, jobs
+
+
 def write_libsvm(path: str, data: Sparse, labeled: bool = True) -> None:
     with open(path, "w") as f:
         ip, ix, vv = data.indptr, data.indices, data.values
