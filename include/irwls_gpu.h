@@ -98,6 +98,35 @@ int irwls_batch_autotune(const svm_dataset *datasets, const properties *props, i
 void irwls_batch_set_workers(int workers);
 /* n numbers of the library's equivalent of libc's srand(seed); rand(). */
 void irwls_rand_sequence(unsigned seed, int n, int *out);
+/* Learned-proposal form of SGMA (precision form, RBF kernels): a network of
+ * 8 candidate features -> 128 -> 128 -> 1 (ReLU), parameters in the order W1
+ * [128][8], b1, W2 [128][128], b2, W3 [1][128], b3 (FP32), trained on the GPU
+ * by the library's own kernels. With a proposer set, every SGMA step scores
+ * `pool` random candidates (half of each label) with it and sends the best 32
+ * of each label to the exact score instead of 64 random ones; NULL restores
+ * the reference's random candidates. None of this has a counterpart in the
+ * reference. */
+void *irwls_mlp_create(unsigned seed);
+void irwls_mlp_free(void *mlp);
+int irwls_mlp_param_count(void);
+int irwls_mlp_feature_count(void);
+int irwls_mlp_get_params(void *mlp, float *out);
+int irwls_mlp_set_params(void *mlp, const float *in);
+/* Mean squared error of the predictions of n rows X [n][8] against T and its
+ * gradient (parameter layout); < 0 on error. */
+double irwls_mlp_loss_grad(void *mlp, const float *X, const float *T, int n, float *grad);
+int irwls_mlp_predict_host(void *mlp, const float *X, int n, float *out);
+/* Adam on minibatches, `epochs` passes over a seeded shuffle; returns the mean
+ * loss of the last pass. */
+double irwls_mlp_train(void *mlp, const float *X, const float *T, int n, int epochs, int batch, float lr,
+                       unsigned seed);
+/* Features ((size - 2) x 64 x 8) and exact scores ((size - 2) x 64) of the
+ * random candidates of one precision-form SGMA run. */
+int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float *score);
+void irwls_set_sgma_proposer(void *mlp, int pool);
+/* trace(K - K_nm K_mm^-1 K_mn) over the training rows after the last
+ * precision-form SGMA run (RBF), or -1. */
+double irwls_last_nystrom_residual(void);
 /* FP32 FMA throughput of the device (TFLOP/s, one FMA = 2 flops), measured
  * the same way: the denominator of the precision form's double-float Gram. */
 double irwls_fp32_peak_tflops(int reps);

@@ -58,6 +58,21 @@ def load() -> C.CDLL:
         "irwls_batch_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
         "irwls_batch_set_workers": (None, [C.c_int]),
         "irwls_rand_sequence": (None, [C.c_uint, C.c_int, C.POINTER(C.c_int)]),
+        "irwls_mlp_create": (C.c_void_p, [C.c_uint]),
+        "irwls_mlp_free": (None, [C.c_void_p]),
+        "irwls_mlp_param_count": (C.c_int, []),
+        "irwls_mlp_feature_count": (C.c_int, []),
+        "irwls_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "irwls_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+        "irwls_mlp_loss_grad": (C.c_double, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int,
+                                             C.POINTER(C.c_float)]),
+        "irwls_mlp_predict_host": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float)]),
+        "irwls_mlp_train": (C.c_double, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                         C.c_int, C.c_float, C.c_uint]),
+        "irwls_set_sgma_proposer": (None, [C.c_void_p, C.c_int]),
+        "irwls_sgma_traces": (C.c_int, [_abi.SvmDataset, _abi.Properties, C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float)]),
+        "irwls_last_nystrom_residual": (C.c_double, []),
         "irwls_tc_status": (C.c_int, []),
         "irwls_set_precision": (None, [C.c_int]),
         "irwls_get_precision": (C.c_int, []),

@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int
 __global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__restrict__ part, int nblk,
                                                               const double *__restrict__ eta,
                                                               const int *__restrict__ cand, int s, int *cent,
-                                                              int *best, double *bestval) {
+                                                              int *best, double *bestval, float *scores) {
     __shared__ double grp[16][64];
     __shared__ double sc[64];
     const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
@@ -530,6 +530,7 @@ __global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__re
         for (int k = 0; k < 16; ++k) v += grp[k][threadIdx.x];
         const double et = eta[threadIdx.x];
         sc[threadIdx.x] = (et > 0.0) ? v / et : 0.0;
+        if (scores) scores[threadIdx.x] = (float)sc[threadIdx.x];
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -552,7 +553,7 @@ __global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__re
 // pieces. The kernel entry is split over the warp's lanes.
 __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
                                                        const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qhi,
-                                                       __nv_bfloat16 *Qlo, int ldq) {
+                                                       __nv_bfloat16 *Qlo, int ldq, float *__restrict__ qn) {
     extern __shared__ float qsm[];
     const int s4 = (s + 127) / 128 * 128;  // <= ldq
     float *l2 = qsm;                       // s4 floats, zero past s
@@ -595,6 +596,7 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
         else kv = __expf(X.ng * fmaxf(qa + X.q[i] - 2.f * kd, 0.f));
         const float q = (kv - acc) * inv_l3;
         Qf[(size_t)i * ldq + s] = q;
+        if (qn) qn[i] = fmaf(q, q, qn[i]);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
         const __nv_bfloat16 h = __float2bfloat16_rn(q);
         Qhi[(size_t)i * ldq + s] = h;
         Qlo[(size_t)i * ldq + s] = __float2bfloat16_rn(q - __bfloat162float(h));
@@ -652,6 +654,12 @@ extern "C" void *irwls_f32_mirror(const irwls_dev_set *X) {
     return f;
 }
 
+extern "C" void irwls_f32_mirror_view(const void *h, const float **X, const float **q) {
+    const F32Mirror *f = (const F32Mirror *)h;
+    *X = f->X;
+    *q = f->q;
+}
+
 extern "C" void irwls_f32_mirror_free(void *h) {
     F32Mirror *f = (F32Mirror *)h;
     if (!f) return;
@@ -682,15 +690,16 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
 extern "C" int irwls_sgma_tc_partials(int l) { return ceil_div(l, TC_BM); }
 
 extern "C" int irwls_sgma_tc_select(const float *d_part, int nblk, const double *d_eta, const int *d_cand, int s,
-                                    int *d_cent, int *d_best, double *d_bestval) {
-    sgma_select_f32_kernel<<<1, 1024, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval);
+                                    int *d_cent, int *d_best, double *d_bestval, float *d_scores) {
+    sgma_select_f32_kernel<<<1, 1024, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval,
+                                                           d_scores);
     IRWLS_LAUNCH_CHECK("sgma_select_f32");
     return 0;
 }
 
 // lrow: row s of L in FP32 (s values, then 1 / L3), from irwls_sgma_linv_update.
 extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s,
-                              const float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq) {
+                              const float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq, float *d_qn) {
     const int s4 = (s + 127) / 128 * 128;
     if (s4 > ldq) {
         irwls_set_error(-12, "Q leading dimension %d below the padded order %d", ldq, s4);
@@ -700,7 +709,8 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
     if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int blocks = std::min(ceil_div(l, 8), 8 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
     q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
-                                                            (__nv_bfloat16 *)Qhi, (__nv_bfloat16 *)Qlo, ldq);
+                                                            (__nv_bfloat16 *)Qhi, (__nv_bfloat16 *)Qlo, ldq,
+                                                            d_qn);
     IRWLS_LAUNCH_CHECK("q_column");
     return 0;
 }

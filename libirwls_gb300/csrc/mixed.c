@@ -33,16 +33,24 @@ int irwls_sgma_linv_update(const double *d_L, int ldL, double *d_Linv, int ldi, 
 size_t irwls_sgma_wpart_count(int m);
 size_t irwls_sgma_lpart_count(int m);
 int irwls_sgma_tc_select(const float *d_part, int nblk, const double *d_eta, const int *d_cand, int s, int *d_cent,
-                         int *d_best, double *d_bestval);
+                         int *d_best, double *d_bestval, float *d_scores);
 int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W, int ldz,
                       double *d_L, int ldL);
 int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
                         const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, float *d_part);
 int irwls_sgma_tc_partials(int l);
 int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const float *lrow, float *Qf,
-                   void *Qhi, void *Qlo, int ldq);
+                   void *Qhi, void *Qlo, int ldq, float *d_qn);
 void *irwls_f32_mirror(const irwls_dev_set *X);
 void irwls_f32_mirror_free(void *h);
+void irwls_f32_mirror_view(const void *h, const float **X, const float **q);
+int irwls_learn_features(const float *X, int ld, int width, int raw, const float *q, float ng, const double *y,
+                         const int *d_cand, int nc, const int *d_probe, int np, const float *d_qn, float progress,
+                         float *d_F);
+int irwls_learn_predict(void *mlp, const float *d_F, int n, float *d_pred);
+int irwls_learn_topk(const float *d_pred, const int *d_pool, int half, int keep, int *d_out);
+int irwls_learn_residual_trace(const float *d_qn, int l, double *d_out);
+int irwls_mlp_feature_count(void);
 int irwls_tc_status(void);
 int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m);
 void irwls_record_run_info(int par_iterations, int active_rows);
@@ -61,6 +69,32 @@ int irwls_get_precision(void) {
 
 static int round_up(int x, int a) { return (x + a - 1) / a * a; }
 
+/* Learned-proposal form: the network, its pool per step, the probe rows of
+ * the features, and trace outputs (host arrays of (m - 2) x 64 x features and
+ * (m - 2) x 64 exact scores) when a trace is being recorded. */
+enum { NPROBE = 1024, NCAND = 64 };
+static void *g_proposer = NULL;
+static int g_pool = 4096;
+static float *g_trace_feat = NULL, *g_trace_score = NULL;
+static double g_last_residual = -1.0;
+
+void irwls_set_sgma_proposer(void *mlp, int pool) {
+    g_proposer = mlp;
+    if (pool < 2 * NCAND) pool = 2 * NCAND;
+    if (pool > 4096) pool = 4096;
+    g_pool = pool & ~1;
+}
+double irwls_last_nystrom_residual(void) { return g_last_residual; }
+
+/* n row indices with label `want`, drawn uniformly with the context's rand(). */
+static void draw_label_rows(const svm_dataset *ds, double want, int n, int *out) {
+    for (int k = 0; k < n; k++) {
+        int pick = irwls_rand() % ds->l;
+        while (ds->y[pick] != want) pick = irwls_rand() % ds->l;
+        out[k] = pick;
+    }
+}
+
 int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properties props, int *cent_out) {
     const int m = props.size, l = ds->l;
     if (m <= 0) return 0;
@@ -73,8 +107,14 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_val = NULL, *d_Linv = NULL, *d_wpart = NULL,
            *d_lpart = NULL;
     float *d_part = NULL;
-    float *Qf = NULL, *lrow = NULL;
+    float *Qf = NULL, *lrow = NULL, *d_qn = NULL, *d_F = NULL, *d_pred = NULL, *d_tfeat = NULL, *d_tscore = NULL;
+    int *d_probe = NULL, *d_pool = NULL;
+    double *d_resid = NULL;
     void *Qhi = NULL, *Qlo = NULL, *Whi = NULL, *Wlo = NULL;
+    /* proposals and traces need the RBF kernel's k(x, x) = 1 */
+    const int learn = g_proposer != NULL && X->mode != IRWLS_K_LINEAR && m > 2;
+    const int trace = g_trace_feat != NULL && m > 2;
+    const int nf = irwls_mlp_feature_count(), pool = g_pool, half = g_pool / 2;
     void *F = irwls_f32_mirror(X);
     if (!F) {
         free(cand);
@@ -98,6 +138,20 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     rc |= irwls_dev_malloc((void **)&d_Linv, (size_t)m * ldL * sizeof(double));
     rc |= irwls_dev_malloc((void **)&d_wpart, irwls_sgma_wpart_count(m) * sizeof(double));
     rc |= irwls_dev_malloc((void **)&d_lpart, irwls_sgma_lpart_count(m) * sizeof(double));
+    rc |= irwls_dev_malloc((void **)&d_qn, (size_t)(l + 2) * sizeof(float));
+    rc |= irwls_dev_malloc((void **)&d_resid, sizeof(double));
+    if (learn || trace) {
+        rc |= irwls_dev_malloc((void **)&d_probe, NPROBE * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&d_F, (size_t)pool * nf * sizeof(float));
+    }
+    if (learn) {
+        rc |= irwls_dev_malloc((void **)&d_pool, (size_t)m * pool * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&d_pred, (size_t)pool * sizeof(float));
+    }
+    if (trace) {
+        rc |= irwls_dev_malloc((void **)&d_tfeat, (size_t)(m - 2) * NCAND * nf * sizeof(float));
+        rc |= irwls_dev_malloc((void **)&d_tscore, (size_t)(m - 2) * NCAND * sizeof(float));
+    }
     if (rc) goto done;
     {
         int first[2] = {l, l + 1};
@@ -109,22 +163,65 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
         rc |= irwls_dev_memset(Qf, 0, (size_t)l * ldq * sizeof(float));
         rc |= irwls_dev_memset(Qhi, 0, (size_t)l * ldq * 2);
         rc |= irwls_dev_memset(Qlo, 0, (size_t)l * ldq * 2);
+        rc |= irwls_dev_memset(d_qn, 0, (size_t)(l + 2) * sizeof(float));
+        if (learn || trace) {
+            /* probe rows and the proposal pools, drawn after the reference's
+               candidates so that those stay the plain run's */
+            int *hp = (int *)malloc((size_t)(learn ? m * pool : NPROBE) * sizeof(int) + NPROBE * sizeof(int));
+            int *probe = hp + (learn ? (size_t)m * pool : 0);
+            for (int k = 0; k < NPROBE; k++) probe[k] = irwls_rand() % l;
+            rc |= irwls_dev_h2d(d_probe, probe, NPROBE * sizeof(int));
+            if (learn) {
+                memset(hp, 0, (size_t)2 * pool * sizeof(int));
+                for (int st = 2; st < m; st++) {
+                    draw_label_rows(ds, -1.0, half, hp + (size_t)st * pool);
+                    draw_label_rows(ds, 1.0, half, hp + (size_t)st * pool + half);
+                }
+                rc |= irwls_dev_h2d(d_pool, hp, (size_t)m * pool * sizeof(int));
+            }
+            rc |= irwls_dev_sync();
+            free(hp);
+        }
         /* centroids 0 and 1 are the class means (src/budgeted-train.c:127-147) */
         for (int s = 0; s < 2 && s < m && !rc; s++) {
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
             rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
-            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq);
+            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq, d_qn);
         }
+        const float *X32 = NULL, *q32 = NULL;
+        irwls_f32_mirror_view(F, &X32, &q32);
+        const int raw = X->mode == IRWLS_K_RAW_RBF;
         for (int s = 2; s < m && !rc; s++) {
-            rc |= irwls_sgma_cand_inv(X, d_cand + (size_t)s * 64, d_cent, s, d_Linv, ldL, d_KN, ldz, d_wpart, m, d_W,
-                                      Whi, Wlo, ldq, d_eta);
-            rc |= irwls_sgma_tc_score(X, F, l, d_cand + (size_t)s * 64, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
+            int *cs = d_cand + (size_t)s * 64;
+            if (learn) {
+                /* the network scores the step's pool; the best 32 of each label
+                   replace the step's random candidates */
+                rc |= irwls_learn_features(X32, X->ld, X->width, raw, q32, (float)X->neg_gamma, X->y,
+                                           d_pool + (size_t)s * pool, pool, d_probe, NPROBE, d_qn, (float)s / m, d_F);
+                rc |= irwls_learn_predict(g_proposer, d_F, pool, d_pred);
+                rc |= irwls_learn_topk(d_pred, d_pool + (size_t)s * pool, half, NCAND / 2, cs);
+            }
+            if (trace)
+                rc |= irwls_learn_features(X32, X->ld, X->width, raw, q32, (float)X->neg_gamma, X->y, cs, NCAND,
+                                           d_probe, NPROBE, d_qn, (float)s / m,
+                                           d_tfeat + (size_t)(s - 2) * NCAND * nf);
+            rc |= irwls_sgma_cand_inv(X, cs, d_cent, s, d_Linv, ldL, d_KN, ldz, d_wpart, m, d_W, Whi, Wlo, ldq, d_eta);
+            rc |= irwls_sgma_tc_score(X, F, l, cs, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
             irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
-            rc |= irwls_sgma_tc_select(d_part, nblk, d_eta, d_cand + (size_t)s * 64, s, d_cent, d_best, d_val);
+            rc |= irwls_sgma_tc_select(d_part, nblk, d_eta, cs, s, d_cent, d_best, d_val,
+                                       trace ? d_tscore + (size_t)(s - 2) * NCAND : NULL);
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
             rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
-            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq);
+            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qhi, Qlo, ldq, d_qn);
             irwls_prof_end(IRWLS_PROF_SGMA_UPDATE);
+        }
+        /* Nystrom residual trace(K - K_nm K_mm^-1 K_mn) = sum_i (k_ii - |Q_i|^2) */
+        g_last_residual = -1.0;
+        if (!rc && X->mode != IRWLS_K_LINEAR && !irwls_learn_residual_trace(d_qn, l, d_resid))
+            rc |= irwls_dev_d2h(&g_last_residual, d_resid, sizeof(double));
+        if (!rc && trace) {
+            rc |= irwls_dev_d2h(g_trace_feat, d_tfeat, (size_t)(m - 2) * NCAND * nf * sizeof(float));
+            rc |= irwls_dev_d2h(g_trace_score, d_tscore, (size_t)(m - 2) * NCAND * sizeof(float));
         }
         if (rc) goto done;
         double *val = (double *)malloc((size_t)m * sizeof(double));
@@ -148,9 +245,35 @@ done:
     free(cand);
     {
         void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qhi, Qlo, Whi, Wlo, lrow,
-                        d_Linv, d_wpart, d_lpart};
+                        d_Linv, d_wpart, d_lpart, d_qn, d_resid, d_probe, d_F, d_pool, d_pred, d_tfeat, d_tscore};
         for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
         irwls_f32_mirror_free(F);
     }
     return rc ? -1 : 0;
+}
+
+/* Records the features and exact scores of the random candidates of a
+ * precision-form SGMA run on `dataset` (RBF): feat gets (size - 2) x 64 x
+ * irwls_mlp_feature_count() values, score (size - 2) x 64. */
+int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float *score) {
+    irwls_clear_error();
+    if (props.size <= 2 || props.kernelType == 0) {
+        irwls_set_error(-9, "traces need an RBF kernel and a budget above 2");
+        return -9;
+    }
+    void *saved = g_proposer;
+    g_proposer = NULL;
+    g_trace_feat = feat;
+    g_trace_score = score;
+    irwls_dev_set X;
+    int rc = irwls_dev_upload(&dataset, dataset.l + 2, props.kernelType, props.Kgamma, 0, 0, &X);
+    if (!rc) {
+        int *cent = (int *)malloc((size_t)props.size * sizeof(int));
+        rc = irwls_sgma_mixed_dev(&X, &dataset, props, cent);
+        free(cent);
+        irwls_dev_release(&X);
+    }
+    g_trace_feat = g_trace_score = NULL;
+    g_proposer = saved;
+    return rc;
 }

@@ -185,6 +185,28 @@ def batch_workload(seed: int = 20240608, n_min: int = 2000, n_max: int = 50_000,
     return pool, jobs
 
 
+def gauss_mixture(n: int, seed: int, family_seed: int = 20240609, k: int = 50, d: int = 32, flip: float = 0.03,
+                  mean_scale: float = 0.6, spread=(0.08, 0.22)):
+    """Dense rows from a mixture of k seeded Gaussians with random
+    covariances (x = mu_j + s_j R_j z, R_j with N(0, 1/d) entries, s_j drawn
+    from ``spread``); label +1 for even components and -1 for odd ones, with a
+    fraction ``flip`` flipped. ``family_seed`` draws the mixture, ``seed`` the
+    rows. Values are rounded to FP32. Returns (X, y)."""
+    frng = np.random.default_rng(family_seed)
+    mu = frng.normal(0.0, mean_scale, (k, d))
+    R = frng.normal(0.0, 1.0 / np.sqrt(d), (k, d, d)) * frng.uniform(spread[0], spread[1], (k, 1, 1))
+    rng = np.random.default_rng(seed)
+    comp = rng.integers(0, k, n)
+    X = np.empty((n, d))
+    for a in range(0, n, 65536):
+        b = min(n, a + 65536)
+        z = rng.standard_normal((b - a, d))
+        X[a:b] = mu[comp[a:b]] + np.einsum("nij,nj->ni", R[comp[a:b]], z)
+    y = np.where(comp % 2 == 0, 1.0, -1.0)
+    y = np.where(rng.random(n) < flip, -y, y)
+    return X.astype(np.float32).astype(np.float64), y
+
+
 def write_libsvm(path: str, data: Sparse, labeled: bool = True) -> None:
     with open(path, "w") as f:
         ip, ix, vv = data.indptr, data.indices, data.values
