@@ -47,6 +47,12 @@ RBF SVMs plus linear ones) on subsets of 2000-50000 rows trained concurrently
 (worker count from the library's autotuner) against the same SVMs trained one
 at a time; every SVM's weights must be bitwise identical in both.
 
+`--workload learned` measures the learned-proposal form: a network trained on
+traces of random-candidate SGMA on 20 small sets proposes SGMA candidates on
+a 1M-row set (budget 2000 by default, --budget to change), against random
+candidates; it reports train seconds, the Nystrom residual of both, the
+primal objective and the held-out accuracy.
+
 `--impl reference` runs only the CPU baseline measurement above (the reference
 sources cannot be built on the GPU host, so the restatement stands in for it)
 and prints its line with "impl": "reference".
@@ -86,7 +92,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
-    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch"])
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned"])
     ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
@@ -837,12 +843,158 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# learned-proposal form of SGMA
+# ----------------------------------------------------------------------------
+LEARN = dict(n=1_000_000, n_test=20_000, gamma=0.5, C=10.0, trace_sets=10, trace_rows=20_000, pool=4096)
+LEARN_DESC = ("learned-proposal form, budgeted IRWLS (precision form): n=%d, d=32 dense (mixture of 50 seeded "
+              "Gaussians with random covariances, labels by component parity, 3%% flipped), RBF gamma=0.5, C=10, "
+              "budget m=%d; network 8-128-128-1 (ReLU) scores a %d-candidate pool per step and keeps the best 32 "
+              "of each label (with 8 random ones of each label) for the exact SGMA score; trained on traces of "
+              "SGMA on %d sets of %d rows (budget %d) with mixtures of their own, random candidates then on-policy")
+
+
+def _row(hd, i):
+    """(indices, values) of row i of a host svm_dataset."""
+    import numpy as np
+
+    idx, val = [], []
+    p = hd.struct.x[i]
+    k = 0
+    while p[k].index != -1:
+        idx.append(p[k].index)
+        val.append(p[k].value)
+        k += 1
+    return np.asarray(idx), np.asarray(val)
+
+
+def run_learned(args):
+    import numpy as np
+
+    from libirwls_gb300 import _abi, learned, load, synth
+
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned-proposal form (its "
+                          "random-candidate SGMA at 1M rows and budget 2000 runs for hours on the host)"}))
+        return
+    budget = args.budget if args.budget != BUDGET else 2000
+    cfg = LEARN
+    lib = load()
+    if not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    libc = C.CDLL(None)
+    # traces and the network
+    t0 = time.perf_counter()
+    runs = []
+    # traces at the workload's budget: a candidate's state depends on how many
+    # centroids cover its component, not on the dataset size
+    tprops = _abi.make_properties(gamma=cfg["gamma"], C_=cfg["C"], size=budget, algorithm=1)
+    for k in range(cfg["trace_sets"]):
+        X, y = synth.gauss_mixture(cfg["trace_rows"], 1000 + k, family_seed=5000 + k)
+        d = synth.from_dense(X, y, keep_zeros=True)
+        runs.append((_abi.build_dataset(d.indptr, d.indices, d.values, d.y), tprops))
+    lib.initMemory(1, budget)
+    libc.srand(1)
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    net, n_trace = learned.fit(runs, seed=11, rounds=2, epochs=10, batch=1024, lr=1e-3, pool=cfg["pool"])
+    net_s = time.perf_counter() - t0
+    # the workload
+    X, y = synth.gauss_mixture(cfg["n"] + cfg["n_test"], 77)
+    tr = synth.from_dense(X[:cfg["n"]], y[:cfg["n"]], keep_zeros=True)
+    te = synth.from_dense(X[cfg["n"]:], y[cfg["n"]:], keep_zeros=True)
+    hd = _abi.build_dataset(tr.indptr, tr.indices, tr.values, tr.y)
+    ht = _abi.build_dataset(te.indptr, te.indices, te.values, te.y, with_means=False)
+    p = _abi.make_properties(gamma=cfg["gamma"], C_=cfg["C"], size=budget, algorithm=1)
+    res = lib.irwls_resident_upload(hd.struct, p, 1)
+    if not res:
+        raise SystemExit(lib.irwls_last_error_message().decode())
+    lib.irwls_set_precision(1)
+    out = {}
+    clocks = Clocks(0)
+    for form in ("random", "learned"):
+        if form == "learned":
+            net.install(pool=cfg["pool"])
+        cent = np.zeros(budget, np.int32)
+        w = np.zeros(budget)
+
+        def step():
+            libc.srand(1)
+            if lib.irwls_resident_budgeted(res, p, cent.ctypes.data_as(PI), w.ctypes.data_as(PD)) != 0:
+                raise SystemExit("training failed: " + lib.irwls_last_error_message().decode())
+
+        for _ in range(args.warmup):
+            step()
+        if form == "learned":
+            clocks.start()
+            launches0 = lib.irwls_kernel_launches()
+        times = []
+        for _ in range(args.steps):
+            lib.irwls_l2_flush(512 << 20)
+            lib.irwls_timer_start()
+            step()
+            times.append(lib.irwls_timer_stop() / 1000.0)
+        resid = lib.irwls_last_nystrom_residual()
+        out[form] = {"s": statistics.mean(times), "residual": resid, "cent": cent.copy(), "w": w.copy()}
+        net.uninstall()
+    clk = clocks.stop()
+    launches = lib.irwls_kernel_launches() - launches0
+    lib.irwls_set_precision(0)
+    lib.irwls_resident_free(res)
+    # quality: primal objective (f from the library's prediction path) and held-out accuracy
+    ytr = np.asarray(tr.y)
+    for form, r in out.items():
+        c = np.ascontiguousarray(r["cent"], dtype=np.int32)
+        ww = np.ascontiguousarray(r["w"])
+        mdl = lib.calculateBudgetedModel(p, hd.struct, c.ctypes.data_as(PI), ww.ctypes.data_as(PD))
+        f = np.ctypeslib.as_array(lib.softTest(hd.struct, mdl, _abi.make_predict_properties(soft=1)),
+                                  shape=(hd.l,)).copy()
+        pred = np.ctypeslib.as_array(lib.test(ht.struct, mdl, _abi.make_predict_properties(soft=0)),
+                                     shape=(ht.l,)).copy()
+        lib.freeModel(mdl)
+        Xc = np.zeros((budget, 33))
+        for k, i in enumerate(c):
+            ix, v = _row(hd, int(i))
+            Xc[k, ix] = v
+        sq = (Xc * Xc).sum(1)
+        Kmm = np.exp(-cfg["gamma"] * np.maximum(sq[:, None] + sq[None, :] - 2 * Xc @ Xc.T, 0.0))
+        r["primal"] = float(0.5 * ww @ (Kmm + 1e-5 * np.eye(budget)) @ ww +
+                            cfg["C"] * np.maximum(0.0, 1.0 - ytr * f).sum())
+        r["test_acc"] = float((pred == np.asarray(te.y)).mean())
+    L, R = out["learned"], out["random"]
+    line = {"metric": METRIC, "value": round(L["s"], 3), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(L["s"] * 1000, 1), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3 (SGMA scores) + f32 (network) + f32x2 (IRWLSpar Gram) + f64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": LEARN_DESC % (cfg["n"], budget, cfg["pool"], cfg["trace_sets"], cfg["trace_rows"],
+                                                 budget),
+                       "n": cfg["n"], "d": 32, "budget": budget, "pool": cfg["pool"], "form": "learned proposals",
+                       "parallelism": "single GPU", "l2": "flushed between timed steps"},
+            "e2e": None, "gpu_launches": int(launches // max(args.steps, 1)),
+            "roofline": {"bound": "see the budgeted workload's kernels", "kernel": None, "achieved": None,
+                         "peak": None, "unit": None, "frac": None, "traffic": None},
+            "cpu_baseline": None, "clocks": clk,
+            "nystrom_residual": {"random_candidates": R["residual"], "learned_proposals": L["residual"],
+                                 "reduction": 1.0 - L["residual"] / R["residual"]},
+            "random_candidates_s": round(R["s"], 3),
+            "primal": {"random": R["primal"], "learned": L["primal"],
+                       "rel_change": (L["primal"] - R["primal"]) / abs(R["primal"])},
+            "test_acc": {"random": R["test_acc"], "learned": L["test_acc"]},
+            "network": {"trace_rows": int(n_trace), "sets_build_s": round(build_s, 2),
+                        "traces_and_training_s": round(net_s, 2),
+                        "rounds": "random-candidate traces, then on-policy traces of the first network"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload in FULL:
         run_full(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "learned":
+        run_learned(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

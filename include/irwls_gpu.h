@@ -102,10 +102,10 @@ void irwls_rand_sequence(unsigned seed, int n, int *out);
  * 8 candidate features -> 128 -> 128 -> 1 (ReLU), parameters in the order W1
  * [128][8], b1, W2 [128][128], b2, W3 [1][128], b3 (FP32), trained on the GPU
  * by the library's own kernels. With a proposer set, every SGMA step scores
- * `pool` random candidates (half of each label) with it and sends the best 32
- * of each label to the exact score instead of 64 random ones; NULL restores
- * the reference's random candidates. None of this has a counterpart in the
- * reference. */
+ * `pool` random candidates (half of each label) with it and sends its best 24
+ * of each label, with 8 random ones of each label, to the exact score instead
+ * of 64 random ones; NULL restores the reference's random candidates. None of
+ * this has a counterpart in the reference. */
 void *irwls_mlp_create(unsigned seed);
 void irwls_mlp_free(void *mlp);
 int irwls_mlp_param_count(void);
@@ -121,7 +121,8 @@ int irwls_mlp_predict_host(void *mlp, const float *X, int n, float *out);
 double irwls_mlp_train(void *mlp, const float *X, const float *T, int n, int epochs, int batch, float lr,
                        unsigned seed);
 /* Features ((size - 2) x 64 x 8) and exact scores ((size - 2) x 64) of the
- * random candidates of one precision-form SGMA run. */
+ * candidates of one precision-form SGMA run: random ones, or the installed
+ * proposer's (on-policy traces). */
 int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float *score);
 void irwls_set_sgma_proposer(void *mlp, int pool);
 /* trace(K - K_nm K_mm^-1 K_mn) over the training rows after the last

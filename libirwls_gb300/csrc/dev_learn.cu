@@ -3,14 +3,15 @@
 // best 32 of each label go to the exact SGMA score (the reference's step draws
 // 64 random candidates of alternating labels, src/budgeted-train.c:149-167).
 //
-// Features of a candidate c at step s (all cheap, all invariant to where the
-// data lies):
+// Features of a candidate c at step s (all cheap, and all relative to the
+// current state so that they mean the same at any budget or dataset size):
 //   d_c = k(c, c) - |Q_c|^2, the Nystrom residual of c (the exact score's
-//         denominator), from the row norms of Q kept by the Q-column update;
+//         denominator), from the row norms of Q kept by the Q-column update,
+//         relative to dbar, the mean residual of the probe rows;
 //   rho_c  = mean over probe rows p of k(c, p)          (local density);
 //   rhor_c = mean over probe rows p of d_p k(c, p)^2    (unexplained mass
-//            near c, a proxy of the exact score's numerator);
-//   the label and the progress s / m.
+//            near c, a proxy of the exact score's numerator), over dbar;
+//   log dbar (the state) and the label.
 // The network is trained on traces of the exact scores of random candidates
 // (target: log score minus the step's mean log score) by the kernels below:
 // layer forward with bias and ReLU fused, the three backward products, an
@@ -33,61 +34,97 @@ constexpr int P_W1 = 0, P_B1 = P_W1 + LH * LF, P_W2 = P_B1 + LH, P_B2 = P_W2 + L
 
 // ---- features --------------------------------------------------------------
 
-// One warp per candidate: kernel values against the probe rows from the FP32
-// dense rows (raw or norm form as the set's mode; RBF only).
+// Features of 32 candidates per CTA (4 per warp): the probe rows are staged
+// through shared memory in chunks of PCH rows and shared by the CTA's
+// candidates; kernel values in the set's form (raw or norm; RBF only). All
+// features are relative to the current state (dbar = mean residual of the
+// probes), so that they mean the same at any budget and dataset size.
+constexpr int PCH = 128, CPB = 32;
 __global__ void __launch_bounds__(256) features_kernel(const float *__restrict__ X, int ld, int width, int raw,
                                                        const float *__restrict__ q, float ng,
                                                        const double *__restrict__ y, const int *__restrict__ cand,
                                                        int nc, const int *__restrict__ probe, int np,
-                                                       const float *__restrict__ qn, float progress,
-                                                       float *__restrict__ F) {
-    extern __shared__ float rows[];  // 8 warps x ld
+                                                       const float *__restrict__ qn, float *__restrict__ F) {
+    extern __shared__ float sm[];
+    float *crow = sm;                // [CPB][ld] candidate rows
+    float *prow = sm + CPB * ld;     // [PCH][ld] probe rows of the chunk
+    float *pd = prow + PCH * ld;     // [PCH] probe residuals
+    float *pq = pd + PCH;            // [PCH] probe norms
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ci = blockIdx.x * 8 + w;
-    float *a = rows + w * ld;
-    const int c = ci < nc ? cand[ci] : 0;
-    for (int t = lane; t < ld; t += 32) a[t] = X[(size_t)c * ld + t];
-    __syncwarp();
-    if (ci >= nc) return;
-    const float qc = q[c];
-    float rho = 0.f, rhor = 0.f;
-    for (int k = lane; k < np; k += 32) {
-        const int p = probe[k];
-        const float *b = X + (size_t)p * ld;
-        float d2;
-        if (raw) {
-            d2 = 0.f;
-            for (int t = 0; t < width; ++t) {
-                const float d = a[t] - b[t];
-                d2 = fmaf(d, d, d2);
-            }
-        } else {
-            float dot = 0.f;
-            for (int t = 0; t < width; ++t) dot = fmaf(a[t], b[t], dot);
-            d2 = fmaxf(qc + q[p] - 2.f * dot, 0.f);
+    const int c0 = blockIdx.x * CPB;
+    for (int t = threadIdx.x; t < CPB * ld; t += blockDim.x) {
+        const int j = t / ld, k = t % ld;
+        crow[t] = c0 + j < nc ? X[(size_t)cand[c0 + j] * ld + k] : 0.f;
+    }
+    float rho[4] = {0.f, 0.f, 0.f, 0.f}, rhor[4] = {0.f, 0.f, 0.f, 0.f}, dsum = 0.f;
+    for (int p0 = 0; p0 < np; p0 += PCH) {
+        const int npc = min(PCH, np - p0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < npc * ld; t += blockDim.x) {
+            const int j = t / ld, k = t % ld;
+            prow[t] = X[(size_t)probe[p0 + j] * ld + k];
         }
-        const float kv = expf(ng * d2);
-        const float dp = fmaxf(1.f - qn[p], 0.f);
-        rho += kv;
-        rhor = fmaf(dp * kv, kv, rhor);
+        for (int j = threadIdx.x; j < npc; j += blockDim.x) {
+            pd[j] = fmaxf(1.f - qn[probe[p0 + j]], 0.f);
+            pq[j] = q[probe[p0 + j]];
+        }
+        __syncthreads();
+        for (int j = lane; j < npc; j += 32) {
+            const float *b = prow + j * ld;
+            dsum += pd[j];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int ci = w * 4 + u;
+                const float *a = crow + ci * ld;
+                float d2;
+                if (raw) {
+                    d2 = 0.f;
+                    for (int t = 0; t < width; ++t) {
+                        const float d = a[t] - b[t];
+                        d2 = fmaf(d, d, d2);
+                    }
+                } else {
+                    float dot = 0.f;
+                    for (int t = 0; t < width; ++t) dot = fmaf(a[t], b[t], dot);
+                    const int c = c0 + ci < nc ? cand[c0 + ci] : 0;
+                    d2 = fmaxf(q[c] + pq[j] - 2.f * dot, 0.f);
+                }
+                const float kv = expf(ng * d2);
+                rho[u] += kv;
+                rhor[u] = fmaf(pd[j] * kv, kv, rhor[u]);
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
-        rho += __shfl_xor_sync(0xffffffffu, rho, o);
-        rhor += __shfl_xor_sync(0xffffffffu, rhor, o);
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            rho[u] += __shfl_xor_sync(0xffffffffu, rho[u], o);
+            rhor[u] += __shfl_xor_sync(0xffffffffu, rhor[u], o);
+        }
     }
-    if (lane == 0) {
-        const float dc = fmaxf(1.f - qn[c], 0.f);
-        rho /= (float)np;
-        rhor /= (float)np;
-        float *f = F + (size_t)ci * LF;
-        f[0] = dc;
-        f[1] = logf(dc + 1e-6f);
-        f[2] = logf(rho + 1e-12f);
-        f[3] = logf(rhor + 1e-12f);
-        f[4] = rhor / (rho + 1e-12f);
-        f[5] = progress;
-        f[6] = (float)y[c];
-        f[7] = sqrtf(dc);
+    if (lane < 4) {
+        const int ci = c0 + w * 4 + lane;
+        if (ci < nc) {
+            const int c = cand[ci];
+            float r = rho[0], rr = rhor[0];
+            if (lane == 1) { r = rho[1]; rr = rhor[1]; }
+            if (lane == 2) { r = rho[2]; rr = rhor[2]; }
+            if (lane == 3) { r = rho[3]; rr = rhor[3]; }
+            const float dbar = dsum / (float)np + 1e-12f;
+            const float dc = fmaxf(1.f - qn[c], 0.f);
+            r /= (float)np;
+            rr /= (float)np;
+            float *f = F + (size_t)ci * LF;
+            f[0] = dc / dbar;
+            f[1] = logf(dc + 1e-9f) - logf(dbar);
+            f[2] = logf(r + 1e-12f);
+            f[3] = logf(rr + 1e-12f) - logf(dbar);
+            f[4] = rr / (r * dbar + 1e-12f);
+            f[5] = logf(dbar);
+            f[6] = (float)y[c];
+            f[7] = sqrtf(dc / dbar);
+        }
     }
 }
 
@@ -200,10 +237,11 @@ __global__ void gather_batch_kernel(const float *__restrict__ Xall, const float 
 // ---- proposals -------------------------------------------------------------
 
 // Per label group g (0: label -1, 1: label +1) of `half` pool entries: the
-// `keep` best predictions (ties to the lower pool index), written to
-// out[2 j + g] so that labels alternate as in the reference's draws.
+// `keep` best predictions (ties to the lower pool index) then `nrand` pool
+// entries taken in pool order (random draws), written to out[2 j + g] so that
+// labels alternate as in the reference's draws.
 __global__ void __launch_bounds__(1024) topk_kernel(const float *__restrict__ pred, const int *__restrict__ pool,
-                                                    int half, int keep, int *__restrict__ out) {
+                                                    int half, int keep, int nrand, int *__restrict__ out) {
     __shared__ float key[2048];
     __shared__ int idx[2048];
     const int g = blockIdx.x;
@@ -235,6 +273,7 @@ __global__ void __launch_bounds__(1024) topk_kernel(const float *__restrict__ pr
             __syncthreads();
         }
     for (int j = threadIdx.x; j < keep; j += blockDim.x) out[2 * j + g] = pool[g * half + idx[j]];
+    for (int j = threadIdx.x; j < nrand; j += blockDim.x) out[2 * (keep + j) + g] = pool[g * half + j];
 }
 
 __global__ void residual_trace_kernel(const float *__restrict__ qn, int l, double *out) {
@@ -479,11 +518,15 @@ extern "C" double irwls_mlp_train(void *h, const float *X, const float *T, int n
 
 extern "C" int irwls_learn_features(const float *X, int ld, int width, int raw, const float *q, float ng,
                                     const double *y, const int *d_cand, int nc, const int *d_probe, int np,
-                                    const float *d_qn, float progress, float *d_F) {
-    const int smem = 8 * ld * (int)sizeof(float);
+                                    const float *d_qn, float *d_F) {
+    const int smem = ((CPB + PCH) * ld + 2 * PCH) * (int)sizeof(float);
+    if (smem > 220 * 1024) {
+        irwls_set_error(-12, "feature width %d too wide for the proposal features", width);
+        return -12;
+    }
     if (smem > 48 * 1024) cudaFuncSetAttribute(features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    features_kernel<<<ceil_div(nc, 8), 256, smem, irwls_stream()>>>(X, ld, width, raw, q, ng, y, d_cand, nc, d_probe,
-                                                                    np, d_qn, progress, d_F);
+    features_kernel<<<ceil_div(nc, CPB), 256, smem, irwls_stream()>>>(X, ld, width, raw, q, ng, y, d_cand, nc,
+                                                                      d_probe, np, d_qn, d_F);
     IRWLS_LAUNCH_CHECK("learn_features");
     return 0;
 }
@@ -494,12 +537,12 @@ extern "C" int irwls_learn_predict(void *h, const float *d_F, int n, float *d_pr
     return mlp_forward(M, d_F, n, d_pred);
 }
 
-extern "C" int irwls_learn_topk(const float *d_pred, const int *d_pool, int half, int keep, int *d_out) {
-    if (half > 2048 || keep > half) {
-        irwls_set_error(-12, "proposal pool of %d per label (at most 2048) keeping %d", half, keep);
+extern "C" int irwls_learn_topk(const float *d_pred, const int *d_pool, int half, int keep, int nrand, int *d_out) {
+    if (half > 2048 || keep > half || nrand > half) {
+        irwls_set_error(-12, "proposal pool of %d per label (at most 2048) keeping %d + %d", half, keep, nrand);
         return -12;
     }
-    topk_kernel<<<2, 1024, 0, irwls_stream()>>>(d_pred, d_pool, half, keep, d_out);
+    topk_kernel<<<2, 1024, 0, irwls_stream()>>>(d_pred, d_pool, half, keep, nrand, d_out);
     IRWLS_LAUNCH_CHECK("learn_topk");
     return 0;
 }

@@ -45,10 +45,9 @@ void *irwls_f32_mirror(const irwls_dev_set *X);
 void irwls_f32_mirror_free(void *h);
 void irwls_f32_mirror_view(const void *h, const float **X, const float **q);
 int irwls_learn_features(const float *X, int ld, int width, int raw, const float *q, float ng, const double *y,
-                         const int *d_cand, int nc, const int *d_probe, int np, const float *d_qn, float progress,
-                         float *d_F);
+                         const int *d_cand, int nc, const int *d_probe, int np, const float *d_qn, float *d_F);
 int irwls_learn_predict(void *mlp, const float *d_F, int n, float *d_pred);
-int irwls_learn_topk(const float *d_pred, const int *d_pool, int half, int keep, int *d_out);
+int irwls_learn_topk(const float *d_pred, const int *d_pool, int half, int keep, int nrand, int *d_out);
 int irwls_learn_residual_trace(const float *d_qn, int l, double *d_out);
 int irwls_mlp_feature_count(void);
 int irwls_tc_status(void);
@@ -72,7 +71,7 @@ static int round_up(int x, int a) { return (x + a - 1) / a * a; }
 /* Learned-proposal form: the network, its pool per step, the probe rows of
  * the features, and trace outputs (host arrays of (m - 2) x 64 x features and
  * (m - 2) x 64 exact scores) when a trace is being recorded. */
-enum { NPROBE = 1024, NCAND = 64 };
+enum { NPROBE = 1024, NCAND = 64, NRANDOM = 8 };
 static void *g_proposer = NULL;
 static int g_pool = 4096;
 static float *g_trace_feat = NULL, *g_trace_score = NULL;
@@ -194,17 +193,16 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
         for (int s = 2; s < m && !rc; s++) {
             int *cs = d_cand + (size_t)s * 64;
             if (learn) {
-                /* the network scores the step's pool; the best 32 of each label
-                   replace the step's random candidates */
+                /* the network scores the step's pool; per label its best 24
+                   and 8 random pool entries replace the step's candidates */
                 rc |= irwls_learn_features(X32, X->ld, X->width, raw, q32, (float)X->neg_gamma, X->y,
-                                           d_pool + (size_t)s * pool, pool, d_probe, NPROBE, d_qn, (float)s / m, d_F);
+                                           d_pool + (size_t)s * pool, pool, d_probe, NPROBE, d_qn, d_F);
                 rc |= irwls_learn_predict(g_proposer, d_F, pool, d_pred);
-                rc |= irwls_learn_topk(d_pred, d_pool + (size_t)s * pool, half, NCAND / 2, cs);
+                rc |= irwls_learn_topk(d_pred, d_pool + (size_t)s * pool, half, NCAND / 2 - NRANDOM, NRANDOM, cs);
             }
             if (trace)
                 rc |= irwls_learn_features(X32, X->ld, X->width, raw, q32, (float)X->neg_gamma, X->y, cs, NCAND,
-                                           d_probe, NPROBE, d_qn, (float)s / m,
-                                           d_tfeat + (size_t)(s - 2) * NCAND * nf);
+                                           d_probe, NPROBE, d_qn, d_tfeat + (size_t)(s - 2) * NCAND * nf);
             rc |= irwls_sgma_cand_inv(X, cs, d_cent, s, d_Linv, ldL, d_KN, ldz, d_wpart, m, d_W, Whi, Wlo, ldq, d_eta);
             rc |= irwls_sgma_tc_score(X, F, l, cs, Qhi, Qlo, ldq, Whi, Wlo, s, d_part);
             irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
@@ -252,8 +250,9 @@ done:
     return rc ? -1 : 0;
 }
 
-/* Records the features and exact scores of the random candidates of a
- * precision-form SGMA run on `dataset` (RBF): feat gets (size - 2) x 64 x
+/* Records the features and exact scores of the candidates of a precision-form
+ * SGMA run on `dataset` (RBF): the random ones, or with a proposer installed
+ * the ones it proposes (on-policy traces). feat gets (size - 2) x 64 x
  * irwls_mlp_feature_count() values, score (size - 2) x 64. */
 int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float *score) {
     irwls_clear_error();
@@ -261,8 +260,6 @@ int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float 
         irwls_set_error(-9, "traces need an RBF kernel and a budget above 2");
         return -9;
     }
-    void *saved = g_proposer;
-    g_proposer = NULL;
     g_trace_feat = feat;
     g_trace_score = score;
     irwls_dev_set X;
@@ -274,6 +271,5 @@ int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float 
         irwls_dev_release(&X);
     }
     g_trace_feat = g_trace_score = NULL;
-    g_proposer = saved;
     return rc;
 }

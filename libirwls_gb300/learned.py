@@ -110,3 +110,22 @@ def training_set(runs):
         Xs.append(f.reshape(-1, f.shape[-1]))
         Ts.append(targets(s).reshape(-1))
     return np.concatenate(Xs), np.concatenate(Ts)
+
+
+def fit(runs, seed=0, rounds=2, epochs=10, batch=1024, lr=1e-3, pool=4096):
+    """Trains a proposer on traces of the (dataset, props) runs: the first
+    round on random candidates, each later round adds the exact scores of the
+    candidates the current network proposes (on-policy traces, which teach
+    it where it over-ranks) and continues training on all of them."""
+    net = Proposer(seed)
+    X, T = training_set(runs)
+    net.train(X, T, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    for r in range(1, rounds):
+        net.install(pool)
+        try:
+            X2, T2 = training_set(runs)
+        finally:
+            net.uninstall()
+        X, T = np.concatenate([X, X2]), np.concatenate([T, T2])
+        net.train(X, T, epochs=epochs, batch=batch, lr=lr, seed=seed + r)
+    return net, len(T)

@@ -72,9 +72,7 @@ def test_learned_proposals_lower_the_nystrom_residual():
     runs = [(_family_set(4000, 10 + k, 300 + k), props) for k in range(4)]
     lib.initMemory(1, m)
     H.LIBC.srand(1)
-    X, T = learned.training_set(runs)
-    net = learned.Proposer(seed=7)
-    net.train(X, T, epochs=30, batch=512, lr=1e-3, seed=3)
+    net, _ = learned.fit(runs, seed=7, rounds=2, epochs=20, batch=512, pool=1024)
     test_set = _family_set(8000, 99, 399)
     lib.irwls_set_precision(1)
     try:
