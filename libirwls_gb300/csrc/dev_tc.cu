@@ -204,6 +204,126 @@ __device__ bool tc_mainloop(unsigned char *smem, uint64_t *mbar, uint32_t tmem, 
     return tc_mainloop_p<BN, 2>(smem, mbar, tmem, A, lda, m0, M, B, ldb, n0, N, ks0, ks1, used);
 }
 
+// ---- ring pipeline: NS stages of BK K-elements ------------------------------
+//
+// Stage layout as above with BK / 8 core matrices per row group: LBO = 128 B
+// (next K core matrix), SBO = BK / 8 * 128 B (next 8-row group). Loads for
+// stage i + NS - 1 are issued while the MMAs of stage i run, so NS - 1 stages
+// of copies are in flight; a buffer is refilled only after the mbarrier of
+// the MMAs that last read it has completed.
+template <int BN, int P, int BK>
+struct TcRing {
+    static constexpr int A_BYTES = TC_BM * BK * 2;
+    static constexpr int B_BYTES = BN * BK * 2;
+    static constexpr int BYTES = P * A_BYTES + P * B_BYTES;
+    static constexpr int SBO = BK / 8 * 128;
+};
+
+__device__ __forceinline__ uint64_t tc_desc_sbo(uint32_t saddr, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((128u >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+template <int BN, int P, int BK>
+__device__ __forceinline__ void ring_load(unsigned char *sb, const __nv_bfloat16 *const *A, int lda, int m0, int M,
+                                          const __nv_bfloat16 *const *B, int ldb, int n0, int N, int k0) {
+    using S = TcRing<BN, P, BK>;
+    constexpr int CH = BK / 8;  // 16-byte chunks per row
+    const uint32_t base = smem_u32(sb);
+    for (int t = threadIdx.x; t < P * TC_BM * CH; t += TC_THREADS) {
+        const int which = t / (TC_BM * CH), rem = t % (TC_BM * CH);
+        const int r = rem / CH, c = rem % CH;
+        const int gr = m0 + r;
+        const __nv_bfloat16 *src = A[which] + (size_t)(gr < M ? gr : 0) * lda + k0 + c * 8;
+        cp_async16(base + which * S::A_BYTES + (r / 8) * S::SBO + c * 128 + (r % 8) * 16, src, gr < M ? 16 : 0);
+    }
+    for (int t = threadIdx.x; t < P * BN * CH; t += TC_THREADS) {
+        const int which = t / (BN * CH), rem = t % (BN * CH);
+        const int r = rem / CH, c = rem % CH;
+        const int gr = n0 + r;
+        const __nv_bfloat16 *src = B[which] + (size_t)(gr < N ? gr : 0) * ldb + k0 + c * 8;
+        cp_async16(base + P * S::A_BYTES + which * S::B_BYTES + (r / 8) * S::SBO + c * 128 + (r % 8) * 16, src,
+                   gr < N ? 16 : 0);
+    }
+}
+
+template <int BN, int P, int BK>
+__device__ __forceinline__ void ring_mma(unsigned char *sb, uint32_t tmem, bool first) {
+    using S = TcRing<BN, P, BK>;
+    const uint32_t base = smem_u32(sb);
+    constexpr uint32_t idesc = tc_idesc(TC_BM, BN);
+    bool init = first;
+#pragma unroll
+    for (int kk = 0; kk < BK / 16; ++kk) {
+        const uint32_t off = kk * 256;
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P - i; ++j) {
+                const uint32_t a = base + i * S::A_BYTES + off, b = base + P * S::A_BYTES + j * S::B_BYTES + off;
+                mma_bf16(tmem, tc_desc_sbo(a, S::SBO), tc_desc_sbo(b, S::SBO), idesc, init ? 0u : 1u);
+                init = false;
+            }
+    }
+}
+
+// Accumulates the CTA's 128 x BN tile over K stages [ks0, ks1) (of BK
+// elements) into tensor memory through an NS-stage ring. mbar: NS barriers;
+// used[NS]: phases each has completed before the call, advanced by it. Every
+// commit is waited for before returning. Returns false if a wait ran out.
+template <int BN, int P, int BK, int NS>
+__device__ bool tc_mainloop_ring(unsigned char *smem, uint64_t *mbar, uint32_t tmem, const __nv_bfloat16 *const *A,
+                                 int lda, int m0, int M, const __nv_bfloat16 *const *B, int ldb, int n0, int N,
+                                 int ks0, int ks1, uint32_t *used) {
+    constexpr int SB = TcRing<BN, P, BK>::BYTES;
+    const int nst = ks1 - ks0;
+    if (nst <= 0) return true;
+    auto parity = [&](int st) { return (used[st % NS] + (uint32_t)(st / NS)) & 1u; };
+    bool ok = true;
+    for (int i = 0; i < NS - 1; ++i) {
+        if (i < nst) ring_load<BN, P, BK>(smem + i * SB, A, lda, m0, M, B, ldb, n0, N, (ks0 + i) * BK);
+        asm volatile("cp.async.commit_group;\n" ::);
+    }
+    for (int i = 0; i < nst; ++i) {
+        const int j = i + NS - 1;  // the stage whose copies start now, into the buffer stage i - 1 used
+        if (j < nst) {
+            if (i >= 1 && !mbar_wait(smem_u32(&mbar[(i - 1) % NS]), parity(i - 1))) ok = false;
+            ring_load<BN, P, BK>(smem + (j % NS) * SB, A, lda, m0, M, B, ldb, n0, N, (ks0 + j) * BK);
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(NS - 1));  // stage i has landed
+        asm volatile("fence.proxy.async.shared::cta;\n" ::);
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            ring_mma<BN, P, BK>(smem + (i % NS) * SB, tmem, i == 0);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                smem_u32(&mbar[i % NS])));
+        }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    // the commits not yet waited for: the last NS stages at most
+    for (int st = (nst > NS ? nst - NS : 0); st < nst && ok; ++st)
+        if (!mbar_wait(smem_u32(&mbar[st % NS]), parity(st))) ok = false;
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    for (int b = 0; b < NS; ++b) used[b] += (uint32_t)((nst > b ? (nst - b + NS - 1) / NS : 0));
+    return ok;
+}
+
+template <int NS>
+__device__ __forceinline__ void ring_barriers_init(uint64_t *mbar) {
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NS; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[b])));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+}
+
 template <int BN>
 __device__ __forceinline__ void tc_setup(uint64_t *mbar, uint32_t *tmem_slot) {
     if (threadIdx.x == 0) {
@@ -211,6 +331,19 @@ __device__ __forceinline__ void tc_setup(uint64_t *mbar, uint32_t *tmem_slot) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
     }
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+}
+
+template <int BN, int NS>
+__device__ __forceinline__ void tc_setup_ring(uint64_t *mbar, uint32_t *tmem_slot) {
+    ring_barriers_init<NS>(mbar);
     if (threadIdx.x < 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
                      "r"(BN));
@@ -452,6 +585,8 @@ __device__ __forceinline__ void kentry8_f32(const KViewF &B, const float *a, int
     for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
 }
 
+constexpr int SC_BK = 32, SC_NS = 3;  // score kernel ring: 3 stages of 32 K-elements (2 CTAs per SM)
+
 // SGMA scores in the precision form: R = Q W^T on the tensor cores (rows of
 // the CTA's 128-row tile x 64 candidates), r = R - k(cand, row) in FP32, and
 // the per-candidate sums of r^2 over the tile (FP32 tree) to part[tile][64].
@@ -461,20 +596,23 @@ __global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int
                                                                    const __nv_bfloat16 *Wlo, int kst,
                                                                    float *__restrict__ part, int *flags) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar[SC_NS];
     __shared__ uint32_t tmem_slot;
     __shared__ float qc[64];
     unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
-    float *ca = (float *)(smem + 2 * TcStage<64>::BYTES);  // 64 candidate rows, FP32, X.ld each
+    float *ca = (float *)(smem + SC_NS * TcRing<64, 2, SC_BK>::BYTES);  // 64 candidate rows, FP32, X.ld each
     const int m0 = blockIdx.x * TC_BM;
     for (int t = threadIdx.x; t < 64 * X.ld; t += TC_THREADS) {
         const int c = t / X.ld, k = t % X.ld;
         ca[t] = X.X[(size_t)cand[c] * X.ld + k];
     }
     if (threadIdx.x < 64) qc[threadIdx.x] = X.q[cand[threadIdx.x]];
-    tc_setup<64>(mbar, &tmem_slot);
+    tc_setup_ring<64, SC_NS>(mbar, &tmem_slot);
     const uint32_t tmem = tmem_slot;
-    const bool ok = tc_mainloop<64>(smem, mbar, tmem, Qhi, Qlo, ldq, m0, l, Whi, Wlo, ldq, 0, 64, 0, kst);
+    const __nv_bfloat16 *Ap[2] = {Qhi, Qlo}, *Bp[2] = {Whi, Wlo};
+    uint32_t used[SC_NS] = {};
+    const bool ok =
+        tc_mainloop_ring<64, 2, SC_BK, SC_NS>(smem, mbar, tmem, Ap, ldq, m0, l, Bp, ldq, 0, 64, 0, kst, used);
     if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
     // residual squares of this thread's row, summed per candidate over the
     // tile: warp shuffles (FP32 tree) then the four warps in a fixed order
@@ -671,8 +809,8 @@ extern "C" void irwls_f32_mirror_free(void *h) {
 
 extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
                                    const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, float *d_part) {
-    const int kst = (s + TC_BK - 1) / TC_BK;
-    const size_t smem = 2 * TcStage<64>::BYTES + 1024 + (size_t)64 * X->ld * sizeof(float);
+    const int kst = (s + SC_BK - 1) / SC_BK;
+    const size_t smem = SC_NS * TcRing<64, 2, SC_BK>::BYTES + 1024 + (size_t)64 * X->ld * sizeof(float);
     if (smem > 220 * 1024) {
         irwls_set_error(-12, "feature width %d too wide for the precision-form SGMA tile", X->width);
         return -12;
@@ -734,7 +872,7 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
 
 namespace {
 
-constexpr int KR_BN = 128, KR_P = 3;
+constexpr int KR_BN = 128, KR_P = 3, KR_BK = 32, KR_NS = 4;
 
 struct Pieces {
     const __nv_bfloat16 *p[KR_P];
@@ -745,7 +883,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_kernel_rowsum_kernel(
     const float *__restrict__ qb, const double *__restrict__ cb, int kst, int rbf, float ng,
     const double *init, const double *__restrict__ tail, double *out, int *flags) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar[KR_NS];
     __shared__ uint32_t tmem_slot;
     __shared__ float qs[KR_BN], cs[KR_BN];
     unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
@@ -754,9 +892,9 @@ __global__ void __launch_bounds__(TC_THREADS) tc_kernel_rowsum_kernel(
     const int row = m0 + threadIdx.x;
     const float qi = row < M ? qa[row] : 0.f;
     float sum = 0.f, comp = 0.f;
-    tc_setup<KR_BN>(mbar, &tmem_slot);
+    tc_setup_ring<KR_BN, KR_NS>(mbar, &tmem_slot);
     const uint32_t tmem = tmem_slot;
-    uint32_t used[2] = {0u, 0u};
+    uint32_t used[KR_NS] = {};
     bool ok = true;
     for (int n0 = 0; n0 < N && ok; n0 += KR_BN) {
         for (int t = threadIdx.x; t < KR_BN; t += TC_THREADS) {
@@ -764,7 +902,8 @@ __global__ void __launch_bounds__(TC_THREADS) tc_kernel_rowsum_kernel(
             qs[t] = j < N ? qb[j] : 0.f;
             cs[t] = j < N ? (float)cb[j] : 0.f;
         }
-        ok = tc_mainloop_p<KR_BN, KR_P>(smem, mbar, tmem, Ap.p, lda, m0, M, Bp.p, ldb, n0, N, 0, kst, used);
+        ok = tc_mainloop_ring<KR_BN, KR_P, KR_BK, KR_NS>(smem, mbar, tmem, Ap.p, lda, m0, M, Bp.p, ldb, n0, N, 0, kst,
+                                                         used);
         if (!ok) break;
         const int ncol = min(KR_BN, N - n0);
         for (int c0 = 0; c0 < ncol; c0 += 8) {
@@ -926,11 +1065,11 @@ extern "C" int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n,
     tc_gather_rows_kernel<<<gb, 256, 0, irwls_stream()>>>(xp, t->ld, t->q, d_idx, d_n, t->wmax, t->B[0], t->B[1],
                                                           t->B[2], t->qb);
     IRWLS_LAUNCH_CHECK("tc_gather_rows");
-    const size_t smem = 2 * TcStage<KR_BN, KR_P>::BYTES + 1024;
+    const size_t smem = KR_NS * TcRing<KR_BN, KR_P, KR_BK>::BYTES + 1024;
     cudaFuncSetAttribute(tc_kernel_rowsum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
     tc_kernel_rowsum_kernel<<<ceil_div(t->rows, TC_BM), TC_THREADS, smem, irwls_stream()>>>(
-        xp, t->ld, t->rows, t->q, bp, t->ld, d_n, t->wmax, t->qb, d_cb, t->ld / TC_BK, t->rbf, t->ng, d_init, d_tail,
+        xp, t->ld, t->rows, t->q, bp, t->ld, d_n, t->wmax, t->qb, d_cb, t->ld / KR_BK, t->rbf, t->ng, d_init, d_tail,
         d_out, irwls_dev_flags());
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
     IRWLS_LAUNCH_CHECK("tc_kernel_rowsum");
