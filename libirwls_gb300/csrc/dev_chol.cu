@@ -27,39 +27,60 @@ constexpr int NB = 32;
 // Factors the nb x nb diagonal block at (k0, k0) held in D (shared, NB x NB,
 // lower part valid), with LAPACK dpotrf's failed-pivot behaviour, and forms
 // the inverse of the lower factor in Di. Uses the whole CTA; ends synced.
+// FP64 runs at a fraction of the FP32 rate on this part, so every dependent
+// FP64 operation on this serial path costs tens of cycles: the pivot's
+// reciprocal square root is formed once and the column is scaled by it (as
+// dpotf2 scales by 1 / ajj), and each entry of the inverse is a dot product
+// split over 8 lanes of a warp.
 __device__ void factor_invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], int nb, int k0, int *flags,
                                     int *failed_at) {
+    __shared__ double rp[NB];  // reciprocal of each stored pivot
     const int tid = threadIdx.x;
     if (tid == 0) *failed_at = -1;
     __syncthreads();
     for (int c = 0; c < nb; ++c) {
         if (tid == 0) {
             const double s = D[c][c];
-            if (s > 0.0) D[c][c] = sqrt(s);
-            else if (*failed_at < 0) *failed_at = c;  // stored without its root, as dpotrf leaves it
+            if (s > 0.0) {
+                const double r = rsqrt(s);
+                D[c][c] = s * r;
+                rp[c] = r;
+            } else {
+                if (*failed_at < 0) *failed_at = c;  // stored without its root, as dpotrf leaves it
+                rp[c] = 1.0 / s;
+            }
         }
         __syncthreads();
-        const double piv = D[c][c];
-        for (int r = c + 1 + tid; r < nb; r += blockDim.x) D[r][c] = D[r][c] / piv;
+        const double r = rp[c];
+        for (int rr = c + 1 + tid; rr < nb; rr += blockDim.x) D[rr][c] = D[rr][c] * r;
         __syncthreads();
         const int m = nb - c - 1;
         for (int t = tid; t < m * m; t += blockDim.x) {
-            const int r = c + 1 + t / m, j = c + 1 + t % m;
-            if (j <= r) D[r][j] = fma(-D[r][c], D[j][c], D[r][j]);
+            const int rr = c + 1 + t / m, j = c + 1 + t % m;
+            if (j <= rr) D[rr][j] = fma(-D[rr][c], D[j][c], D[rr][j]);
         }
         __syncthreads();
     }
-    // inverse of the lower factor, one column per thread
-    if (tid < NB) {
-        const int j = tid;
-        for (int r = 0; r < NB; ++r) Di[r][j] = 0.0;
-        if (j < nb) {
-            Di[j][j] = 1.0 / D[j][j];
-            for (int c = j + 1; c < nb; ++c) {
-                double acc = 0.0;
-                for (int t = j; t < c; ++t) acc = fma(D[c][t], Di[t][j], acc);
-                Di[c][j] = -acc / D[c][c];
-            }
+    // inverse of the lower factor: column j by 8 lanes (threads 8 j .. 8 j + 7),
+    // Di[c][j] = -(sum_{j <= t < c} D[c][t] Di[t][j]) / D[c][c]
+    for (int t = tid; t < NB * NB; t += blockDim.x) Di[t / NB][t % NB] = 0.0;
+    __syncthreads();
+    // (blockDim.x == 256 = 8 lanes x 32 columns; every lane of a warp runs the
+    // same iterations so that the shuffles always see the whole warp)
+    {
+        const int j = tid >> 3, q = tid & 7;
+        if (q == 0 && j < nb) Di[j][j] = rp[j];
+        __syncwarp();
+        for (int c = 1; c < NB; ++c) {
+            const bool live = j < nb && c < nb && c > j;
+            double acc = 0.0;
+            if (live)
+                for (int t = j + q; t < c; t += 8) acc = fma(D[c][t], Di[t][j], acc);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 4, 8);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2, 8);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1, 8);
+            if (live && q == 0) Di[c][j] = -acc * rp[c];
+            __syncwarp();
         }
     }
     __syncthreads();
