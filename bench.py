@@ -368,16 +368,45 @@ def breakdown(run):
     return {k: round(v[0], 4) for k, v in run["prof"].items()}
 
 
-def run_ours(args):
+def replicas():
+    """(world, rank, local rank) of this process. Under torchrun every rank is
+    an independent replica of the workload on its own GPU (the path has no
+    exchange step, so no collective touches the data); gloo carries only the
+    barriers and the max of the step times."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
-        # one independent replica per GPU; the C library uses the current device
+        # the C library uses the current device
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
         import torch.distributed as dist
 
-        dist.init_process_group("gloo")
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    """The slowest rank's value (every rank gets it)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args):
+    world, rank, local = replicas()
     import numpy as np
 
     from libirwls_gb300 import load
@@ -396,24 +425,14 @@ def run_ours(args):
     for prec in forms:
         cent = np.zeros(args.budget, np.int32)
         w = np.zeros(args.budget)
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+        barrier(world)
         headline = prec == forms[-1]
         runs[prec] = timed_trainings(lib, libc, res, p, args, cent, w, prec, Clocks(local) if headline else None)
         cents[prec], weights[prec] = cent, w
     lib.irwls_resident_free(res)
     head = forms[-1]
-    step_s = runs[head]["s"]
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        dist.barrier()
-        t = torch.tensor([step_s])
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_s = float(t.item())
+    barrier(world)
+    step_s = max_over_ranks(runs[head]["s"], world)
     e2e = {prec: None if args.no_e2e else end_to_end(lib, libc, hd, p, args, prec, cents[prec]) for prec in forms}
     lib.irwls_set_precision(0)
     if rank != 0:
