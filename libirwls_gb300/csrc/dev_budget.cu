@@ -18,6 +18,7 @@
 
 #include <algorithm>
 
+#include "blocked_bf16.cuh"
 #include "dev_common.cuh"
 
 namespace {
@@ -214,10 +215,9 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
 
 // Per candidate c: w_e = sum of the chunks of row e in chunk order, W (FP64),
 // eta = 1 - |w|^2 (fixed-order block reduction), and w as bf16 hi/lo of its
-// FP32 rounding (zero up to the padded width kpad).
+// FP32 rounding in the blocked layout (zero up to the padded width kpad).
 __global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict__ part, int ldp, int s,
-                                                       double *__restrict__ W, int ldz, __nv_bfloat16 *Whi,
-                                                       __nv_bfloat16 *Wlo, int ldq, int kpad,
+                                                       double *__restrict__ W, int ldz, __nv_bfloat16 *Wb, int kpad,
                                                        double *__restrict__ eta) {
     __shared__ double red[256];
     const int c = blockIdx.x;
@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict_
             xf = (float)w;
         }
         const __nv_bfloat16 h = __float2bfloat16_rn(xf);
-        Whi[(size_t)c * ldq + e] = h;
-        Wlo[(size_t)c * ldq + e] = __float2bfloat16_rn(xf - __bfloat162float(h));
+        Wb[wb_index(c, e, 0)] = h;
+        Wb[wb_index(c, e, 1)] = __float2bfloat16_rn(xf - __bfloat162float(h));
     }
     red[threadIdx.x] = ss;
     __syncthreads();
@@ -853,7 +853,7 @@ extern "C" size_t irwls_sgma_lpart_count(int m) { return ((size_t)ceil_div(m, LE
 
 extern "C" int irwls_sgma_cand_inv(const irwls_dev_set *X, const int *d_cand, const int *d_cent, int s,
                                    const double *d_Linv, int ldi, double *d_KN, int ldz, double *d_wpart, int ldp,
-                                   double *d_W, void *Whi, void *Wlo, int ldq, double *d_eta) {
+                                   double *d_W, void *Wb, int ldq, double *d_eta) {
     if (s < 1) return 0;
     const size_t smem = (size_t)X->ld * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(cand_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -869,8 +869,7 @@ extern "C" int irwls_sgma_cand_inv(const irwls_dev_set *X, const int *d_cand, co
     w_gemm_kernel<<<dim3(ceil_div(s, WE), ceil_div(s, WT)), 256, 0, irwls_stream()>>>(d_Linv, ldi, d_KN, ldz, s,
                                                                                     d_wpart, ldp);
     IRWLS_LAUNCH_CHECK("w_gemm");
-    w_finish_kernel<<<NCAND, 256, 0, irwls_stream()>>>(d_wpart, ldp, s, d_W, ldz, (__nv_bfloat16 *)Whi,
-                                                       (__nv_bfloat16 *)Wlo, ldq, kpad, d_eta);
+    w_finish_kernel<<<NCAND, 256, 0, irwls_stream()>>>(d_wpart, ldp, s, d_W, ldz, (__nv_bfloat16 *)Wb, kpad, d_eta);
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_CAND);
     IRWLS_LAUNCH_CHECK("w_finish");
     return 0;

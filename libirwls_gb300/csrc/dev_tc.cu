@@ -28,6 +28,7 @@
 
 #include <algorithm>
 
+#include "blocked_bf16.cuh"
 #include "dev_common.cuh"
 
 namespace {
@@ -585,65 +586,6 @@ __device__ __forceinline__ void kentry8_f32(const KViewF &B, const float *a, int
     for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
 }
 
-constexpr int SC_BK = 32, SC_NS = 3;  // score kernel ring: 3 stages of 32 K-elements (2 CTAs per SM)
-
-// SGMA scores in the precision form: R = Q W^T on the tensor cores (rows of
-// the CTA's 128-row tile x 64 candidates), r = R - k(cand, row) in FP32, and
-// the per-candidate sums of r^2 over the tile (FP32 tree) to part[tile][64].
-__global__ void __launch_bounds__(TC_THREADS) sgma_tc_score_kernel(KViewF X, int l, const int *__restrict__ cand,
-                                                                   const __nv_bfloat16 *Qhi, const __nv_bfloat16 *Qlo,
-                                                                   int ldq, const __nv_bfloat16 *Whi,
-                                                                   const __nv_bfloat16 *Wlo, int kst,
-                                                                   float *__restrict__ part, int *flags) {
-    extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t mbar[SC_NS];
-    __shared__ uint32_t tmem_slot;
-    __shared__ float qc[64];
-    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
-    float *ca = (float *)(smem + SC_NS * TcRing<64, 2, SC_BK>::BYTES);  // 64 candidate rows, FP32, X.ld each
-    const int m0 = blockIdx.x * TC_BM;
-    for (int t = threadIdx.x; t < 64 * X.ld; t += TC_THREADS) {
-        const int c = t / X.ld, k = t % X.ld;
-        ca[t] = X.X[(size_t)cand[c] * X.ld + k];
-    }
-    if (threadIdx.x < 64) qc[threadIdx.x] = X.q[cand[threadIdx.x]];
-    tc_setup_ring<64, SC_NS>(mbar, &tmem_slot);
-    const uint32_t tmem = tmem_slot;
-    const __nv_bfloat16 *Ap[2] = {Qhi, Qlo}, *Bp[2] = {Whi, Wlo};
-    uint32_t used[SC_NS] = {};
-    const bool ok =
-        tc_mainloop_ring<64, 2, SC_BK, SC_NS>(smem, mbar, tmem, Ap, ldq, m0, l, Bp, ldq, 0, 64, 0, kst, used);
-    if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
-    // residual squares of this thread's row, summed per candidate over the
-    // tile: warp shuffles (FP32 tree) then the four warps in a fixed order
-    __shared__ float wred[TC_THREADS / 32][64];
-    const int row = m0 + threadIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int c0 = 0; c0 < 64; c0 += 8) {
-        float v[8], kv[8];
-        if (ok) tc_ld8(tmem, c0, v);
-        else
-            for (int j = 0; j < 8; ++j) v[j] = 0.f;
-        if (row < l && ok) kentry8_f32(X, ca + (size_t)c0 * X.ld, X.ld, qc + c0, row, kv);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            float r2 = 0.f;
-            if (row < l && ok) {
-                const float r = v[j] - kv[j];
-                r2 = r * r;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-            if (lane == 0) wred[warp][c0 + j] = r2;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 64)
-        part[(size_t)blockIdx.x * 64 + threadIdx.x] =
-            (wred[0][threadIdx.x] + wred[1][threadIdx.x]) + (wred[2][threadIdx.x] + wred[3][threadIdx.x]);
-    tc_teardown<64>(tmem);
-}
-
 // Scores of the precision form: per candidate, the tile sums in 16 strided
 // groups with Kahan-compensated FP32 adds, the 16 group sums in FP64 in a
 // fixed order, score = sum / eta; strict ">" argmax, first index wins.
@@ -685,13 +627,319 @@ __global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__re
     }
 }
 
+// ---- persistent warp-specialized score kernel --------------------------------
+//
+// One CTA per SM walks row tiles t = blockIdx.x, + gridDim.x, ...: warp 0
+// streams the Q and W stages of every tile through an NS-deep ring
+// (cp.async, each lane signalling the stage's "full" barrier when its copies
+// land), lane 0 of warp 1 issues the MMAs into one of two tensor-memory
+// accumulators and commits the ring stages ("empty") and the finished tile
+// ("acc full"), and warps 4-11 run the epilogue of a tile while the next one
+// accumulates in the other accumulator: warp w reads tensor-memory lanes
+// 32 (w % 4) ... + 31 (its rows), warps 4-7 for candidates 0-31 and warps
+// 8-11 for candidates 32-63. The candidate rows are loaded once per CTA.
+// Every wait is bounded; on a timeout the flag word 1 is set and every role
+// leaves its loop (the epilogue warps decide together at their named
+// barrier), the MMA thread waits for its last commit and the producer for
+// its copies before the tensor memory is released.
+constexpr int WS_THREADS = 384, WS_BK = 32;
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(b)));
+}
+__device__ __forceinline__ void tc_commit(uint64_t *b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(b)));
+}
+__device__ __forceinline__ void tc_ld8_lanes(uint32_t tmem, int lane_base, int c0, float *v) {
+    uint32_t r[8];
+    const uint32_t addr = tmem + ((uint32_t)lane_base << 16) + (uint32_t)c0;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Bulk global -> shared copy completing on an mbarrier's transaction count
+// (both addresses 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(uint32_t sdst, const void *gsrc, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(sdst),
+                 "l"(gsrc), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t saddr, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(saddr), "l"(gmem));
+}
+
+// Row data of one 128-row tile staged in shared memory for the score
+// epilogue, so that a lane's kernel entries read its row from there instead
+// of walking it in global memory load after load. kind 1: the tile's CSR
+// slice (column indices, values; rows are consecutive, so the slice is
+// contiguous) with tile-relative row pointers; kind 2: the raw rows at an odd
+// stride (conflict-free row-per-lane reads); kind 0: too large for the
+// buffer, entries read from global memory.
+struct TileRows {
+    int kind, lds;
+    const int *rp;
+    const float *q;
+    const int *ci;
+    const float *cv;
+    const float *x;
+};
+
+// Issues the staging copies of rows m0 ... m0 + nr - 1 (threads et = 0 ... 255
+// of the epilogue); the caller waits for them (cp.async.wait_all + barrier).
+__device__ __forceinline__ TileRows stage_tile_rows(const KViewF &X, int m0, int nr, unsigned char *buf, int buf_bytes,
+                                                    int *srp, float *sq, int et) {
+    TileRows t;
+    t.kind = 0;
+    t.lds = 0;
+    t.rp = srp;
+    t.q = sq;
+    if (X.mode == IRWLS_K_RAW_RBF) {
+        const int lds = X.width | 1;
+        float *x = (float *)buf;
+        t.x = x;
+        t.lds = lds;
+        if (nr * lds * 4 <= buf_bytes) {
+            t.kind = 2;
+            const int n = nr * X.width;
+            for (int k = et; k < n; k += 256) {
+                const int r = k / X.width, c = k - r * X.width;
+                cp_async4(smem_u32(x + r * lds + c), X.X + (size_t)(m0 + r) * X.ld + c);
+            }
+        }
+        return t;
+    }
+    const int p0 = X.rp[m0], p1 = X.rp[m0 + nr];
+    const int nnz = p1 - p0;
+    int *ci = (int *)buf;
+    float *cv = (float *)(buf + (buf_bytes / 8) * 4);
+    t.ci = ci;
+    t.cv = cv;
+    for (int k = et; k <= nr; k += 256) srp[k] = X.rp[m0 + k] - p0;
+    if (X.mode == IRWLS_K_NORM_RBF)
+        for (int k = et; k < nr; k += 256) sq[k] = X.q[m0 + k];
+    if (nnz <= buf_bytes / 8) {
+        t.kind = 1;
+        for (int k = et; k < nnz; k += 256) {
+            cp_async4(smem_u32(ci + k), X.ci + p0 + k);
+            cp_async4(smem_u32(cv + k), X.cv + p0 + k);
+        }
+    }
+    return t;
+}
+
+// kentry8_f32 for tile row r (global row jb) from the staged rows; the same
+// FMA order, so the same values.
+__device__ __forceinline__ void kentry8_tile(const KViewF &B, const TileRows &T, const float *a, int lda,
+                                             const float *qa, int r, int jb, float out[8]) {
+    if (T.kind == 0) {
+        kentry8_f32(B, a, lda, qa, jb, out);
+        return;
+    }
+    float acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
+    if (T.kind == 2) {
+        const float *b = T.x + r * T.lds;
+        for (int t = 0; t < B.width; ++t) {
+            const float bt = b[t];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float d = a[j * lda + t] - bt;
+                acc[j] = fmaf(d, d, acc[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * acc[j]);
+        return;
+    }
+    const int p0 = T.rp[r], p1 = T.rp[r + 1];
+    for (int p = p0; p < p1; ++p) {
+        const float v = T.cv[p];
+        const int c = T.ci[p];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, a[j * lda + c], acc[j]);
+    }
+    if (B.mode == IRWLS_K_LINEAR) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out[j] = acc[j];
+        return;
+    }
+    const float qb = T.q[r];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
+}
+
+template <int NS>
+__global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
+    KViewF X, int l, const int *__restrict__ cand, const __nv_bfloat16 *__restrict__ Qb, int kbn,
+    const __nv_bfloat16 *__restrict__ Wb, int kst, float *__restrict__ part, int xs_bytes, int *flags) {
+    using S = TcRing<64, 2, WS_BK>;
+    static_assert(S::A_BYTES == 2 * QB_PIECE && S::B_BYTES == 2 * WB_PIECE, "blocked pieces are stage images");
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full[NS], empty[NS], accf[2], acce[2], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ float qc[64];
+    __shared__ float wred[8][32];
+    __shared__ volatile int abort_flag;
+    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
+    float *ca = (float *)(smem + NS * S::BYTES);
+    unsigned char *xs = (unsigned char *)(ca + 64 * X.ld);  // xs_bytes of staged tile rows
+    __shared__ int srp[TC_BM + 1];
+    __shared__ float sq[TC_BM];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (l + TC_BM - 1) / TC_BM;
+    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NS; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], 8);
+        }
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+        abort_flag = 0;
+    }
+    for (int t = threadIdx.x; t < 64 * X.ld; t += WS_THREADS) {
+        const int c = t / X.ld, k = t % X.ld;
+        ca[t] = X.X[(size_t)cand[c] * X.ld + k];
+    }
+    if (threadIdx.x < 64) qc[threadIdx.x] = X.q[cand[threadIdx.x]];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(128));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        // producer: one thread, two bulk copies per stage (the blocked Q and
+        // W hold each stage's shared-memory image contiguously)
+        if (lane == 0) {
+            const uint32_t base = smem_u32(smem);
+            int issued = 0;
+            for (int j = 0; j < my_tiles && !abort_flag; ++j) {
+                const size_t tile = (size_t)blockIdx.x + (size_t)j * gridDim.x;
+                for (int k = 0; k < kst; ++k) {
+                    const int u = j * kst + k, slot = u % NS;
+                    if (u >= NS && !mbar_wait(smem_u32(&empty[slot]), (uint32_t)(u / NS - 1) & 1u)) abort_flag = 1;
+                    if (abort_flag) break;
+                    const uint32_t sb = base + slot * S::BYTES, fb = smem_u32(&full[slot]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb),
+                                 "r"((uint32_t)S::BYTES));
+                    bulk_g2s(sb, Qb + (tile * kbn + k) * (2 * QB_PIECE), 2 * S::A_BYTES, fb);
+                    bulk_g2s(sb + 2 * S::A_BYTES, Wb + (size_t)k * (2 * WB_PIECE), 2 * S::B_BYTES, fb);
+                    issued = u + 1;
+                }
+            }
+            // no copy is left in flight: the last NS stages issued have landed
+            for (int u = issued > NS ? issued - NS : 0; u < issued; ++u)
+                if (!mbar_wait(smem_u32(&full[u % NS]), (uint32_t)(u / NS) & 1u)) abort_flag = 1;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // MMA issue
+        if (lane == 0) {
+            for (int j = 0; j < my_tiles && !abort_flag; ++j) {
+                const int b = j & 1;
+                if (j >= 2 && !mbar_wait(smem_u32(&acce[b]), (uint32_t)(j / 2 - 1) & 1u)) abort_flag = 1;
+                for (int k = 0; k < kst && !abort_flag; ++k) {
+                    const int u = j * kst + k, slot = u % NS;
+                    if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(u / NS) & 1u)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::);
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                    ring_mma<64, 2, WS_BK>(smem + slot * S::BYTES, tmem + b * 64, k == 0);
+                    tc_commit(&empty[slot]);
+                }
+                if (!abort_flag) tc_commit(&accf[b]);
+            }
+            // every MMA issued has completed before the tensor memory is released
+            tc_commit(&done);
+            if (!mbar_wait(smem_u32(&done), 0u)) abort_flag = 1;
+        }
+        __syncwarp();
+    } else if (warp >= 4) {
+        // epilogue: rows 32 (warp % 4) + lane of each tile, candidates
+        // 32 g ... 32 g + 31 of epilogue group g
+        const int ew = warp & 3, g = (warp - 4) >> 2;
+        const int et = threadIdx.x - 128;
+        for (int j = 0; j < my_tiles; ++j) {
+            const int b = j & 1, tile = (int)blockIdx.x + j * (int)gridDim.x;
+            const int m0 = tile * TC_BM, r = 32 * ew + lane, row = m0 + r;
+            // the tile's rows are copied in while its accumulator fills
+            const TileRows T = stage_tile_rows(X, m0, min(TC_BM, l - m0), xs, xs_bytes, srp, sq, et);
+            const bool acc_ok = mbar_wait(smem_u32(&accf[b]), (uint32_t)(j / 2) & 1u);
+            asm volatile("cp.async.wait_all;\n" ::);
+            // one decision for all 256 epilogue threads (an OR over them), so
+            // that none is left at a named barrier that the others skip; the
+            // barrier also publishes the staged rows
+            const int bad = (!acc_ok || abort_flag) ? 1 : 0;
+            int any;
+            asm volatile(
+                "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, 1, 256, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+                : "=r"(any)
+                : "r"(bad));
+            if (any) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            for (int c0 = 32 * g; c0 < 32 * g + 32; c0 += 8) {
+                float v[8], kv[8];
+                tc_ld8_lanes(tmem + b * 64, 32 * ew, c0, v);
+                if (row < l) kentry8_tile(X, T, ca + (size_t)c0 * X.ld, X.ld, qc + c0, r, row, kv);
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) {
+                    float r2 = 0.f;
+                    if (row < l) {
+                        const float rr = v[jj] - kv[jj];
+                        r2 = rr * rr;
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+                    if (lane == 0) wred[4 * g + ew][c0 - 32 * g + jj] = r2;
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+            if (lane == 0) mbar_arrive(&acce[b]);  // this warp's reads of accumulator b are done
+            asm volatile("bar.sync 1, 256;\n" ::);
+            if (et < 64) {
+                const float *w = &wred[4 * (et >> 5)][et & 31];
+                part[(size_t)tile * 64 + et] = (w[0] + w[32]) + (w[64] + w[96]);
+            }
+            asm volatile("bar.sync 1, 256;\n" ::);
+        }
+    }
+    if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
+}
+
 // New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, one warp
 // per row. lrow holds l2 (s floats) then 1 / L3, written by the factor step;
 // Q's columns >= s are still zero, so the dot runs over whole 128-column
 // pieces. The kernel entry is split over the warp's lanes.
 __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
-                                                       const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qhi,
-                                                       __nv_bfloat16 *Qlo, int ldq, float *__restrict__ qn) {
+                                                       const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qb,
+                                                       int ldq, float *__restrict__ qn) {
     extern __shared__ float qsm[];
     const int s4 = (s + 127) / 128 * 128;  // <= ldq
     float *l2 = qsm;                       // s4 floats, zero past s
@@ -708,7 +956,23 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
     auto partial = [&](int i, float &acc, float &kd) {
         const float4 *qrow = (const float4 *)(Qf + (size_t)i * ldq);
         acc = 0.f;
-        for (int j4 = lane; j4 < s4 / 4; j4 += 32) {
+        // the lane's float4s in order, loaded four at a time
+        const int n4 = s4 / 4;
+        int j4 = lane;
+        for (; j4 + 96 < n4; j4 += 128) {
+            float4 qv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) qv[u] = qrow[j4 + 32 * u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float4 lv = *(const float4 *)(l2 + 4 * (j4 + 32 * u));
+                acc = fmaf(qv[u].x, lv.x, acc);
+                acc = fmaf(qv[u].y, lv.y, acc);
+                acc = fmaf(qv[u].z, lv.z, acc);
+                acc = fmaf(qv[u].w, lv.w, acc);
+            }
+        }
+        for (; j4 < n4; j4 += 32) {
             const float4 qv = qrow[j4];
             const float4 lv = *(const float4 *)(l2 + 4 * j4);
             acc = fmaf(qv.x, lv.x, acc);
@@ -736,8 +1000,8 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
         Qf[(size_t)i * ldq + s] = q;
         if (qn) qn[i] = fmaf(q, q, qn[i]);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
         const __nv_bfloat16 h = __float2bfloat16_rn(q);
-        Qhi[(size_t)i * ldq + s] = h;
-        Qlo[(size_t)i * ldq + s] = __float2bfloat16_rn(q - __bfloat162float(h));
+        Qb[qb_index(i, s, ldq >> 5, 0)] = h;
+        Qb[qb_index(i, s, ldq >> 5, 1)] = __float2bfloat16_rn(q - __bfloat162float(h));
     };
     // two rows in flight per warp
     for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += 2 * stride) {
@@ -807,19 +1071,41 @@ extern "C" void irwls_f32_mirror_free(void *h) {
     free(f);
 }
 
-extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qhi,
-                                   const void *Qlo, int ldq, const void *Whi, const void *Wlo, int s, float *d_part) {
-    const int kst = (s + SC_BK - 1) / SC_BK;
-    const size_t smem = SC_NS * TcRing<64, 2, SC_BK>::BYTES + 1024 + (size_t)64 * X->ld * sizeof(float);
-    if (smem > 220 * 1024) {
+extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qb,
+                                   int ldq, const void *Wb, int s, float *d_part) {
+    constexpr size_t LIMIT = 220 * 1024, XS = 32 * 1024;
+    const int kst = (s + WS_BK - 1) / WS_BK;
+    if (kst * WS_BK > ldq || ldq % WS_BK) {
+        irwls_set_error(-12, "Q leading dimension %d does not hold order %d in 32-column blocks", ldq, s);
+        return -12;
+    }
+    const size_t fixed = 1024 + (size_t)64 * X->ld * sizeof(float);
+    const size_t stage = TcRing<64, 2, WS_BK>::BYTES;
+    if (fixed + 2 * stage > LIMIT) {
         irwls_set_error(-12, "feature width %d too wide for the precision-form SGMA tile", X->width);
         return -12;
     }
-    cudaFuncSetAttribute(sgma_tc_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // row staging when it leaves room for at least four ring stages
+    const size_t xs = fixed + XS + 4 * stage <= LIMIT ? XS : 0;
+    int ns = 8;
+    while (ns > 2 && fixed + xs + (size_t)ns * stage > LIMIT) ns = ns == 8 ? 6 : ns - 2;
+    const size_t smem = fixed + xs + (size_t)ns * stage;
+    const int ntiles = ceil_div(l, TC_BM);
+    const int grid = std::max(1, std::min(ntiles, irwls_num_sms() > 0 ? irwls_num_sms() : 148));
+    const KViewF kv = kviewf(X, (const F32Mirror *)F);
+    const __nv_bfloat16 *qb = (const __nv_bfloat16 *)Qb, *wb = (const __nv_bfloat16 *)Wb;
+    auto launch = [&](auto kern) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<grid, WS_THREADS, smem, irwls_stream()>>>(kv, l, d_cand, qb, ldq / 32, wb, kst, d_part, (int)xs,
+                                                         irwls_dev_flags());
+    };
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
-    sgma_tc_score_kernel<<<ceil_div(l, TC_BM), TC_THREADS, smem, irwls_stream()>>>(
-        kviewf(X, (const F32Mirror *)F), l, d_cand, (const __nv_bfloat16 *)Qhi, (const __nv_bfloat16 *)Qlo, ldq,
-        (const __nv_bfloat16 *)Whi, (const __nv_bfloat16 *)Wlo, kst, d_part, irwls_dev_flags());
+    switch (ns) {
+        case 8: launch(sgma_tc_score_ws_kernel<8>); break;
+        case 6: launch(sgma_tc_score_ws_kernel<6>); break;
+        case 4: launch(sgma_tc_score_ws_kernel<4>); break;
+        default: launch(sgma_tc_score_ws_kernel<2>); break;
+    }
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_GEMM);
     IRWLS_LAUNCH_CHECK("sgma_tc_score");
     return 0;
@@ -837,7 +1123,7 @@ extern "C" int irwls_sgma_tc_select(const float *d_part, int nblk, const double 
 
 // lrow: row s of L in FP32 (s values, then 1 / L3), from irwls_sgma_linv_update.
 extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s,
-                              const float *lrow, float *Qf, void *Qhi, void *Qlo, int ldq, float *d_qn) {
+                              const float *lrow, float *Qf, void *Qb, int ldq, float *d_qn) {
     const int s4 = (s + 127) / 128 * 128;
     if (s4 > ldq) {
         irwls_set_error(-12, "Q leading dimension %d below the padded order %d", ldq, s4);
@@ -847,8 +1133,7 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
     if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int blocks = std::min(ceil_div(l, 8), 8 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
     q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
-                                                            (__nv_bfloat16 *)Qhi, (__nv_bfloat16 *)Qlo, ldq,
-                                                            d_qn);
+                                                            (__nv_bfloat16 *)Qb, ldq, d_qn);
     IRWLS_LAUNCH_CHECK("q_column");
     return 0;
 }
