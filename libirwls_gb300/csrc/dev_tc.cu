@@ -933,13 +933,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
 }
 
-// New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, one warp
-// per row. lrow holds l2 (s floats) then 1 / L3, written by the factor step;
-// Q's columns >= s are still zero, so the dot runs over whole 128-column
-// pieces. The kernel entry is split over the warp's lanes.
+// New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, a warp
+// per row, four rows in flight per warp (their independent loads issued
+// together). lrow holds l2 (s floats) then 1 / L3, written by the factor
+// step; the dot runs over the row's first s columns rounded up to 4 (Q's
+// columns >= s are still zero), each lane's float4s in increasing order. The
+// kernel entry is split over the warp's lanes; lane r finishes row r.
 __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
                                                        const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qb,
                                                        int ldq, float *__restrict__ qn) {
+    constexpr int R = 4;  // rows in flight per warp
     extern __shared__ float qsm[];
     const int s4 = (s + 127) / 128 * 128;  // <= ldq
     float *l2 = qsm;                       // s4 floats, zero past s
@@ -953,71 +956,87 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
     const int lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
     const int stride = gridDim.x * warps;
-    auto partial = [&](int i, float &acc, float &kd) {
-        const float4 *qrow = (const float4 *)(Qf + (size_t)i * ldq);
-        acc = 0.f;
-        // the lane's float4s in order, loaded four at a time
-        const int n4 = s4 / 4;
-        int j4 = lane;
-        for (; j4 + 96 < n4; j4 += 128) {
-            float4 qv[4];
+    const int n4 = (s + 3) / 4;  // float4s of a row that can be nonzero
+    const bool raw = X.mode == IRWLS_K_RAW_RBF;
+    for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += R * stride) {
+        int ir[R], pb[R], pe[R];
+        float acc[R], kd[R], qi[R], qo[R];
+        // every load of the R rows that does not depend on another is issued first
 #pragma unroll
-            for (int u = 0; u < 4; ++u) qv[u] = qrow[j4 + 32 * u];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const float4 lv = *(const float4 *)(l2 + 4 * (j4 + 32 * u));
-                acc = fmaf(qv[u].x, lv.x, acc);
-                acc = fmaf(qv[u].y, lv.y, acc);
-                acc = fmaf(qv[u].z, lv.z, acc);
-                acc = fmaf(qv[u].w, lv.w, acc);
+        for (int r = 0; r < R; ++r) {
+            ir[r] = i + r * stride;
+            const bool ok = ir[r] < l;
+            pb[r] = pe[r] = 0;
+            qi[r] = qo[r] = 0.f;
+            if (ok && !raw) {
+                pb[r] = X.rp[ir[r]];
+                pe[r] = X.rp[ir[r] + 1];
             }
+            if (ok && X.mode == IRWLS_K_NORM_RBF) qi[r] = X.q[ir[r]];
+            if (ok && qn) qo[r] = qn[ir[r]];
+            acc[r] = kd[r] = 0.f;
         }
-        for (; j4 < n4; j4 += 32) {
-            const float4 qv = qrow[j4];
+        // Q_i . l2: each lane's float4s in increasing order
+        for (int j4 = lane; j4 < n4; j4 += 32) {
+            float4 qv[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                qv[r] = ir[r] < l ? ((const float4 *)(Qf + (size_t)ir[r] * ldq))[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float4 lv = *(const float4 *)(l2 + 4 * j4);
-            acc = fmaf(qv.x, lv.x, acc);
-            acc = fmaf(qv.y, lv.y, acc);
-            acc = fmaf(qv.z, lv.z, acc);
-            acc = fmaf(qv.w, lv.w, acc);
-        }
-        kd = 0.f;
-        if (X.mode == IRWLS_K_RAW_RBF) {
-            const float *b = X.X + (size_t)i * X.ld;
-            for (int t = lane; t < X.width; t += 32) {
-                const float d = sc[t] - b[t];
-                kd = fmaf(d, d, kd);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                acc[r] = fmaf(qv[r].x, lv.x, acc[r]);
+                acc[r] = fmaf(qv[r].y, lv.y, acc[r]);
+                acc[r] = fmaf(qv[r].z, lv.z, acc[r]);
+                acc[r] = fmaf(qv[r].w, lv.w, acc[r]);
             }
-        } else {
-            for (int p = X.rp[i] + lane; p < X.rp[i + 1]; p += 32) kd = fmaf(X.cv[p], sc[X.ci[p]], kd);
         }
-    };
-    auto finish = [&](int i, float acc, float kd) {
-        float kv;
-        if (X.mode == IRWLS_K_RAW_RBF) kv = __expf(X.ng * kd);
-        else if (X.mode == IRWLS_K_LINEAR) kv = kd;
-        else kv = __expf(X.ng * fmaxf(qa + X.q[i] - 2.f * kd, 0.f));
-        const float q = (kv - acc) * inv_l3;
-        Qf[(size_t)i * ldq + s] = q;
-        if (qn) qn[i] = fmaf(q, q, qn[i]);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
-        const __nv_bfloat16 h = __float2bfloat16_rn(q);
-        Qb[qb_index(i, s, ldq >> 5, 0)] = h;
-        Qb[qb_index(i, s, ldq >> 5, 1)] = __float2bfloat16_rn(q - __bfloat162float(h));
-    };
-    // two rows in flight per warp
-    for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += 2 * stride) {
-        const int i2 = i + stride;
-        float a0, k0, a1 = 0.f, k1 = 0.f;
-        partial(i, a0, k0);
-        if (i2 < l) partial(i2, a1, k1);
-        for (int o = 16; o > 0; o >>= 1) {
-            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-            k0 += __shfl_xor_sync(0xffffffffu, k0, o);
-            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-            k1 += __shfl_xor_sync(0xffffffffu, k1, o);
+        // kernel entry against the new centroid
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (ir[r] >= l) continue;
+            if (raw) {
+                const float *b = X.X + (size_t)ir[r] * X.ld;
+                for (int t = lane; t < X.width; t += 32) {
+                    const float d = sc[t] - b[t];
+                    kd[r] = fmaf(d, d, kd[r]);
+                }
+            } else {
+                for (int p = pb[r] + lane; p < pe[r]; p += 32) kd[r] = fmaf(X.cv[p], sc[X.ci[p]], kd[r]);
+            }
         }
-        if (lane == 0) {
-            finish(i, a0, k0);
-            if (i2 < l) finish(i2, a1, k1);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+                kd[r] += __shfl_xor_sync(0xffffffffu, kd[r], o);
+            }
+        // lane r finishes row r
+        if (lane < R) {
+            int row = ir[0];
+            float a = acc[0], k = kd[0], qb = qi[0], q0 = qo[0];
+#pragma unroll
+            for (int r = 1; r < R; ++r)
+                if (lane == r) {
+                    row = ir[r];
+                    a = acc[r];
+                    k = kd[r];
+                    qb = qi[r];
+                    q0 = qo[r];
+                }
+            if (row < l) {
+                float kv;
+                if (raw) kv = __expf(X.ng * k);
+                else if (X.mode == IRWLS_K_LINEAR) kv = k;
+                else kv = __expf(X.ng * fmaxf(qa + qb - 2.f * k, 0.f));
+                const float q = (kv - a) * inv_l3;
+                Qf[(size_t)row * ldq + s] = q;
+                if (qn) qn[row] = fmaf(q, q, q0);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
+                const __nv_bfloat16 h = __float2bfloat16_rn(q);
+                Qb[qb_index(row, s, ldq >> 5, 0)] = h;
+                Qb[qb_index(row, s, ldq >> 5, 1)] = __float2bfloat16_rn(q - __bfloat162float(h));
+            }
         }
     }
 }
@@ -1131,7 +1150,7 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
     }
     const size_t smem = ((size_t)s4 + X->ld) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int blocks = std::min(ceil_div(l, 8), 8 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));
+    const int blocks = std::min(ceil_div(l, 32), 4 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));  // one wave
     q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
                                                             (__nv_bfloat16 *)Qb, ldq, d_qn);
     IRWLS_LAUNCH_CHECK("q_column");
