@@ -148,9 +148,9 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
     if (P > l / 512) P = l / 512;
     if (P < 1) P = 1;
     if (P > 64) P = 64;
-    /* precision form: double-float Gram over FP32 pairs of the active rows;
-       finer split-K (chunks of at least 256 rows) since each product costs
-       twelve FP32 instructions instead of one FP64 FMA */
+    /* precision form: the Gram on the tensor cores through exact integer
+       digits of the active rows (dev_gram_tc.cu), which takes as many
+       split-K chunks of the P allowed here as fill the SMs */
     const int mixed = irwls_get_precision() == IRWLS_PRECISION_MIXED;
     void *d_A = NULL;
     if (mixed) {
@@ -158,7 +158,7 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
         if (P > l / 256) P = l / 256;
         if (P < 1) P = 1;
         if (P > 128) P = 128;
-        rc |= irwls_dev_malloc(&d_A, (size_t)l * irwls_par_df_lda(m) * 2 * sizeof(float));
+        rc |= irwls_dev_malloc(&d_A, irwls_par_gram_tc_bytes(l, m));
     }
     rc |= irwls_dev_malloc((void **)&d_idx, (size_t)m * sizeof(int));
     rc |= irwls_dev_malloc((void **)&d_act, (size_t)l * sizeof(int));
@@ -192,7 +192,7 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
         double dW = 1e9, nW = 1.0, old = 0.0, best = 1e9;
         while ((iter < 500) && (dW / nW > 1e-6) && (since_best < 5)) {
             /* K1 = KC + KSCA^T KSCA (lower) and K2 = KSCA^T Day in row m (:401-416) */
-            if (mixed ? irwls_par_gram_df(d_KSC, m, d_act, nact, d_sd, d_day, d_KC, d_K1, ld, d_part, P, d_A)
+            if (mixed ? irwls_par_gram_tc(d_KSC, m, d_act, nact, d_sd, d_day, d_KC, d_K1, ld, d_part, P, d_A)
                       : irwls_par_gram(d_KSC, m, d_act, nact, d_sd, d_day, d_KC, d_K1, ld, d_part, P))
                 goto fail;
             g_gram_flops += (double)nact * (m + 1) * m;

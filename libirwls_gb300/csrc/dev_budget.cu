@@ -934,6 +934,15 @@ extern "C" int irwls_par_first(const double *d_y, int l, double M, int *d_act, d
 
 extern "C" size_t irwls_par_gram_part_bytes(int m, int P) { return (size_t)P * (m + 1) * m * sizeof(double); }
 
+// K1 = KC + the sum of P Gram partials (the last step of both Gram forms).
+extern "C" int irwls_par_gram_reduce(const double *d_part, int P, int m, const double *d_KC, double *d_K1, int ldK1) {
+    const long long tot = (long long)(m + 1) * m;
+    gram_reduce_kernel<<<(int)std::min<long long>(ceil_div(tot, 256), 65535), 256, 0, irwls_stream()>>>(
+        d_part, P, m, d_KC, d_K1, ldK1);
+    IRWLS_LAUNCH_CHECK("gram_reduce");
+    return 0;
+}
+
 extern "C" int irwls_par_gram(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                               const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P) {
     const int T = ceil_div(m + 1, TT);

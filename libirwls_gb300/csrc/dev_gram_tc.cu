@@ -1,0 +1,412 @@
+// dev_gram_tc.cu -- the precision form's IRWLSpar Gram on the tensor cores,
+// through exact integer slices.
+//
+//   G = A'^T A',   A' = [sd * KSC[act, :], day]   (nact x (m + 1)),
+//
+// the K1/K2 system of IRWLSpar (reference src/budgeted-train.c:379-430).
+// FP64 on this part runs at about 1/64 of the FP32 rate, so the product is
+// formed on the bf16 tensor cores with every partial sum exact:
+//
+// 1. Each column c of A' gets a power of two sigma_c >= max_p |A'_pc| (a
+//    column-max pass), and each entry becomes the integer
+//    N_pc = round(A'_pc / sigma_c * 2^47), |N| <= 2^47, by integer operations
+//    on its bits. N is written in 8 balanced base-64 digits d_0 .. d_7
+//    (d_0 lowest), |d_s| <= 32 (|d_7| <= 33): small integers, exact in bf16.
+// 2. sum_p N_pi N_pj = sum_u 64^u L_u(i, j), L_u = sum_{s+t=u} sum_p
+//    d_s(p,i) d_t(p,j). The levels u = 7 ... 14 are kept (36 digit pairs);
+//    the dropped levels weigh at most 2^-44 of the top one, so each entry of
+//    G carries an error of about 2^-47 max|A'_.i| max|A'_.j| per row, the
+//    accuracy of the double-float Gram this replaces.
+// 3. A CTA owns a 128 x 64 tile of G and one split-K chunk of the rows. Per
+//    16-row stage the 36 digit-pair products go to 8 level accumulators of
+//    128 x 64 FP32 in tensor memory (all 512 columns). Every product is an
+//    integer of magnitude <= 33^2 = 1089 and a level sums at most 8 pairs, so
+//    over 1024 rows every partial sum is an integer below 8 * 1024 * 1089 <
+//    2^24: exact in FP32, whatever the order of accumulation. Every 1024 rows
+//    the epilogue drains the levels into a 96-bit integer per entry
+//    (T += sum_u 64^(u-7) L_u), so the whole sum stays exact.
+// 4. G_ij = sigma_i sigma_j 2^-52 T_ij, written as the FP64 partials that
+//    gram_reduce_kernel adds to KC.
+//
+// Operands reach shared memory by bulk copies: the slices are stored in the
+// shared-memory image of a stage (per 128-column tile and 16-row block, the 8
+// digit pieces of 128 x 16 in canonical K-major core-matrix order). Warp 0
+// copies, lane 0 of warp 1 issues the MMAs, warps 4-11 drain. Every wait is
+// bounded; a timeout sets device flag word 1.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "dev_common.cuh"
+#include "tc_ptx.cuh"
+
+namespace {
+
+constexpr int GS = 8;                  // digits per entry
+constexpr int GFRAC = 47;              // N = round(v * 2^47), |v| <= 1
+constexpr int GM = 128, GN = 64;       // tile of G: rows (A' columns) x columns
+constexpr int GBK = 16;                // rows of A' per stage
+constexpr int GPIECE = GM * GBK;       // elements of one digit piece (4 KB)
+constexpr int GDRAIN = 64;             // stages between drains (1024 rows)
+constexpr int GNS = 4;                 // ring stages
+constexpr int G_THREADS = 384;
+constexpr uint32_t A_STAGE = GS * GPIECE * 2;      // 32 KB: 8 pieces of 128 rows
+constexpr uint32_t B_PIECE = GN * GBK * 2;         // 2 KB: 64 rows of one piece
+constexpr uint32_t G_STAGE = A_STAGE + GS * B_PIECE;  // 48 KB
+
+// Element offset of (row r of the 128-row tile, k of the 16-row block) in a
+// digit piece: 8 x 8 core matrices, 128 bytes apart along k, 256 along r.
+__device__ __forceinline__ int piece_off(int r, int k) { return (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7); }
+
+// Column maxima of |A'| as FP64 bit patterns (non-negative doubles order like
+// their bits). Thread = column, block = 256 columns x GCM rows, eight rows'
+// loads in flight per thread.
+constexpr int GCM = 256;
+__global__ void __launch_bounds__(256) gram_colmax_kernel(const double *__restrict__ KSC, int m,
+                                                          const int *__restrict__ act, int nact,
+                                                          const double *__restrict__ sd,
+                                                          const double *__restrict__ day,
+                                                          unsigned long long *__restrict__ cmax) {
+    const int c = blockIdx.x * 256 + threadIdx.x;
+    if (c > m) return;
+    const int p0 = blockIdx.y * GCM, p1 = min(nact, p0 + GCM);
+    double mx[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) mx[u] = 0.0;
+    for (int p = p0; p < p1; p += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int pp = p + u;
+            if (pp < p1) {
+                const double v = c < m ? __dmul_rn(sd[pp], KSC[(size_t)act[pp] * m + c]) : day[pp];
+                mx[u] = fmax(mx[u], fabs(v));
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 1; u < 8; ++u) mx[0] = fmax(mx[0], mx[u]);
+    if (p1 > p0) atomicMax(cmax + c, (unsigned long long)__double_as_longlong(mx[0]));
+}
+
+// sigma_c = 2^e_c, the smallest power of two >= the column maximum (e = -1100:
+// the column is zero).
+__device__ __forceinline__ int col_exp(unsigned long long mxbits) {
+    const int E = (int)((mxbits >> 52) & 0x7ff);
+    if (E == 0) return -1100;
+    const bool pow2 = (mxbits & ((1ULL << 52) - 1)) == 0;
+    return E - 1023 + (pow2 ? 0 : 1);
+}
+
+// round(v * 2^(47 - e)) for |v| <= 2^e, from the bits of v (no FP64 pipe).
+__device__ __forceinline__ long long fixed47(double v, int e) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int E = (int)((b >> 52) & 0x7ff);
+    if (E == 0) return 0;  // zero (subnormals, below 2^-1022, are dropped)
+    const unsigned long long M = (b & ((1ULL << 52) - 1)) | (1ULL << 52);
+    // v = M 2^(E - 1075); N = M 2^(E - 1075 + 47 - e) = M >> sh
+    const int sh = 1075 + e - GFRAC - E;  // >= 5 since |v| <= 2^e
+    long long N = 0;
+    if (sh < 64) N = (long long)((M + (1ULL << (sh - 1))) >> sh);
+    return (b >> 63) ? -N : N;
+}
+
+// The slices of A'. Thread = (column c, group of 8 rows): the 8 digits of the
+// group's entries, one 16-byte store per digit piece. Rows >= nact and
+// columns > m are written as zeros.
+__global__ void __launch_bounds__(256) gram_slice_kernel(const double *__restrict__ KSC, int m,
+                                                         const int *__restrict__ act, int nact,
+                                                         const double *__restrict__ sd,
+                                                         const double *__restrict__ day,
+                                                         const unsigned long long *__restrict__ cmax, int ncols,
+                                                         int npb, __nv_bfloat16 *__restrict__ S) {
+    __shared__ uint16_t bf[67];  // bf16 bits of -33 ... 33
+    if (threadIdx.x < 67) {
+        const __nv_bfloat16 h = __float2bfloat16_rn((float)((int)threadIdx.x - 33));
+        bf[threadIdx.x] = *(const uint16_t *)&h;
+    }
+    __syncthreads();
+    const long long items = (long long)ncols * npb * 2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < items;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(t % ncols);
+        const long long g = t / ncols;  // 8-row group
+        const int pb = (int)(g >> 1), half = (int)(g & 1);
+        const int e = c <= m ? col_exp(cmax[c]) : -1100;
+        uint32_t w[GS][4];  // digit s of the 8 rows, packed bf16 pairs
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int p = pb * GBK + half * 8 + k;
+            long long N = 0;
+            if (p < nact && c <= m && e > -1100) {
+                const double v = c < m ? __dmul_rn(sd[p], KSC[(size_t)act[p] * m + c]) : day[p];
+                N = fixed47(v, e);
+            }
+#pragma unroll
+            for (int s = 0; s < GS; ++s) {
+                int d;
+                if (s < GS - 1) {
+                    d = (int)(N & 63);
+                    if (d >= 32) d -= 64;
+                    N = (N - d) >> 6;
+                } else {
+                    d = (int)N;  // |d| <= 33
+                }
+                const uint32_t hb = bf[d + 33];
+                if (k & 1) w[s][k >> 1] |= hb << 16;
+                else w[s][k >> 1] = hb;
+            }
+        }
+        const int ct = c >> 7, r = c & 127;
+        const size_t base = ((size_t)ct * npb + pb) * GS * GPIECE + piece_off(r, half * 8);
+#pragma unroll
+        for (int s = 0; s < GS; ++s)
+            *(uint4 *)(S + base + (size_t)s * GPIECE) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    }
+}
+
+// tcgen05.ld of 4 consecutive columns of this warp's 32 lanes.
+__device__ __forceinline__ void tc_ld4(uint32_t addr, float *v) {
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+    v[0] = __uint_as_float(r0);
+    v[1] = __uint_as_float(r1);
+    v[2] = __uint_as_float(r2);
+    v[3] = __uint_as_float(r3);
+}
+
+// 96-bit accumulator hi * 2^32 + lo (hi signed).
+struct Acc96 {
+    long long hi;
+    uint32_t lo;
+};
+
+__device__ __forceinline__ void acc_add(Acc96 &a, long long xh, uint32_t xl) {
+    const uint32_t lo = a.lo + xl;
+    a.hi += xh + (lo < xl ? 1 : 0);
+    a.lo = lo;
+}
+
+// Tile (I, J) of G for split-K chunk z: rows 128 I ... of G (columns of A'),
+// columns 64 J ...; stages [z * spc, min(npb, (z + 1) * spc)) of 16 rows.
+__global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat16 *__restrict__ S, int npb, int spc,
+                                                               int m, const unsigned long long *__restrict__ cmax,
+                                                               double *__restrict__ part, int *flags) {
+    const int J = blockIdx.x, I = blockIdx.y, z = blockIdx.z;
+    if (GN * J > GM * I + GM - 1 || GN * J >= m) return;  // above the diagonal or past the last column
+    extern __shared__ __align__(1024) unsigned char g_smem[];
+    __shared__ __align__(8) uint64_t full[GNS], empty[GNS], accf, acce, done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    unsigned char *smem = g_smem + ((1024 - (smem_u32(g_smem) & 1023)) & 1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int k0 = z * spc, nst = max(0, min(npb, k0 + spc) - k0);
+    const int nblk = (nst + GDRAIN - 1) / GDRAIN;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < GNS; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], 1);
+        }
+        mbar_init(&accf, 1);
+        mbar_init(&acce, 8);
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+        abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        // producer: the A tile's 8 pieces in one copy, the B half-pieces in 8
+        if (lane == 0) {
+            const uint32_t base = smem_u32(smem);
+            const __nv_bfloat16 *Ab = S + ((size_t)I * npb + k0) * GS * GPIECE;
+            const __nv_bfloat16 *Bb = S + ((size_t)(J >> 1) * npb + k0) * GS * GPIECE + (J & 1) * (GN / 8) * 128;
+            int issued = 0;
+            for (int k = 0; k < nst; ++k) {
+                const int slot = k % GNS;
+                if (k >= GNS && !mbar_wait(smem_u32(&empty[slot]), (uint32_t)(k / GNS - 1) & 1u)) abort_flag = 1;
+                if (abort_flag) break;
+                const uint32_t sb = base + slot * G_STAGE, fb = smem_u32(&full[slot]);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(G_STAGE));
+                bulk_g2s(sb, Ab + (size_t)k * GS * GPIECE, A_STAGE, fb);
+#pragma unroll
+                for (int s = 0; s < GS; ++s)
+                    bulk_g2s(sb + A_STAGE + s * B_PIECE, Bb + ((size_t)k * GS + s) * GPIECE, B_PIECE, fb);
+                issued = k + 1;
+            }
+            for (int k = issued > GNS ? issued - GNS : 0; k < issued; ++k)
+                if (!mbar_wait(smem_u32(&full[k % GNS]), (uint32_t)(k / GNS) & 1u)) abort_flag = 1;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // MMA issue: level u - 7 += sum_{s+t=u} A_s B_t, u = 7 ... 14
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc_idesc(GM, GN);
+            const uint32_t base = smem_u32(smem);
+            for (int k = 0; k < nst && !abort_flag; ++k) {
+                const int blk = k / GDRAIN, kin = k % GDRAIN;
+                if (kin == 0 && blk >= 1) {
+                    if (!mbar_wait(smem_u32(&acce), (uint32_t)(blk - 1) & 1u)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                }
+                const int slot = k % GNS;
+                if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(k / GNS) & 1u)) {
+                    abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                const uint32_t sa = base + slot * G_STAGE, sbb = sa + A_STAGE;
+#pragma unroll
+                for (int u = GS - 1; u <= 2 * (GS - 1); ++u) {
+#pragma unroll
+                    for (int s = u - (GS - 1); s < GS; ++s) {
+                        const int t = u - s;
+                        const uint64_t da = tc_desc_lbo_sbo(sa + s * (GPIECE * 2), 128, 256);
+                        const uint64_t db = tc_desc_lbo_sbo(sbb + t * B_PIECE, 128, 256);
+                        const bool acc = kin > 0 || s > u - (GS - 1);
+                        mma_bf16(tmem + (uint32_t)(u - (GS - 1)) * GN, da, db, idesc, acc ? 1u : 0u);
+                    }
+                }
+                tc_commit(&empty[slot]);
+                if (kin == GDRAIN - 1 || k == nst - 1) tc_commit(&accf);
+            }
+            tc_commit(&done);
+            if (!mbar_wait(smem_u32(&done), 0u)) abort_flag = 1;
+        }
+        __syncwarp();
+    } else if (warp >= 4) {
+        // drain: lanes 32 (warp % 4) ..., columns 32 h ... 32 h + 31
+        const int q = warp & 3, h = (warp - 4) >> 2;
+        Acc96 T[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) T[j] = Acc96{0, 0u};
+        for (int blk = 0; blk < nblk; ++blk) {
+            const int bad = (!mbar_wait(smem_u32(&accf), (uint32_t)blk & 1u) || abort_flag) ? 1 : 0;
+            int any;
+            asm volatile(
+                "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, 1, 256, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+                : "=r"(any)
+                : "r"(bad));
+            if (any) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            const uint32_t lanes = tmem + ((uint32_t)(32 * q) << 16) + 32 * h;
+#pragma unroll
+            for (int c4 = 0; c4 < 32; c4 += 4) {
+                float L[GS][4];
+#pragma unroll
+                for (int v = 0; v < GS; ++v) tc_ld4(lanes + v * GN + c4, L[v]);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    // levels 11-14 and 7-10 by Horner in 64-bit integers (each
+                    // below 2^44), then T += t_hi 2^24 + t_lo
+                    long long th = __float2int_rn(L[7][j]);
+                    th = th * 64 + __float2int_rn(L[6][j]);
+                    th = th * 64 + __float2int_rn(L[5][j]);
+                    th = th * 64 + __float2int_rn(L[4][j]);
+                    long long tl = __float2int_rn(L[3][j]);
+                    tl = tl * 64 + __float2int_rn(L[2][j]);
+                    tl = tl * 64 + __float2int_rn(L[1][j]);
+                    tl = tl * 64 + __float2int_rn(L[0][j]);
+                    acc_add(T[c4 + j], th >> 8, (uint32_t)th << 24);
+                    acc_add(T[c4 + j], tl >> 32, (uint32_t)tl);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+            if (lane == 0) mbar_arrive(&acce);
+        }
+        if (!abort_flag) {
+            const int r = GM * I + 32 * q + lane;
+            if (r <= m) {
+                const int er = col_exp(cmax[r]);
+                double *out = part + (size_t)z * (m + 1) * m + (size_t)r * m;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int c = GN * J + 32 * h + j;
+                    if (c < m && c <= r) {
+                        const int ec = col_exp(cmax[c]);
+                        double g = 0.0;
+                        if (er > -1100 && ec > -1100) {
+                            const double t = fma((double)T[j].hi, 4294967296.0, (double)T[j].lo);
+                            g = ldexp(t, er + ec - 52);
+                        }
+                        out[c] = g;
+                    }
+                }
+            }
+        }
+    }
+    if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512));
+}
+
+size_t slices_bytes(int l, int m) {
+    const size_t ct = (size_t)ceil_div(m + 1, GM), npb = (size_t)ceil_div(std::max(l, 1), GBK);
+    return ct * npb * GS * GPIECE * sizeof(__nv_bfloat16);
+}
+
+}  // namespace
+
+// Workspace of irwls_par_gram_tc for up to l active rows: the slices, then the
+// m + 1 column maxima.
+extern "C" size_t irwls_par_gram_tc_bytes(int l, int m) {
+    return slices_bytes(l, m) + (size_t)(m + 1) * sizeof(unsigned long long) + 256;
+}
+
+// K1 (column-major, leading dimension ldK1, lower part) = KC + the Gram of
+// the active rows, row m = K2, as irwls_par_gram_df gives; P bounds the
+// split-K chunks (part holds at least P partials).
+extern "C" int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
+                                 const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part,
+                                 int P, void *d_ws) {
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    const int ct = ceil_div(m + 1, GM), nt = ceil_div(m, GN);
+    const int npb = ceil_div(std::max(nact, 1), GBK);
+    __nv_bfloat16 *S = (__nv_bfloat16 *)d_ws;
+    unsigned long long *cmax = (unsigned long long *)((char *)d_ws + slices_bytes(nact, m));
+    // tiles of the lower part, and enough chunks to give every SM one CTA
+    int tiles = 0;
+    for (int I = 0; I < ct; ++I)
+        for (int J = 0; J < nt; ++J)
+            if (GN * J <= GM * I + GM - 1) ++tiles;
+    int pz = std::max(1, std::min(P, sms / std::max(tiles, 1)));
+    pz = std::min(pz, npb);
+    const int spc = ceil_div(npb, pz);
+    pz = ceil_div(npb, spc);
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM);
+    if (irwls_dev_memset(cmax, 0, (size_t)(m + 1) * sizeof(unsigned long long))) return -1;
+    if (nact > 0) {
+        gram_colmax_kernel<<<dim3(ceil_div(m + 1, 256), ceil_div(nact, GCM)), 256, 0, irwls_stream()>>>(
+            d_KSC, m, d_act, nact, d_sd, d_day, cmax);
+        IRWLS_LAUNCH_CHECK("gram_colmax");
+    }
+    const long long items = (long long)ct * GM * npb * 2;
+    gram_slice_kernel<<<(int)std::min<long long>(ceil_div(items, 256), 16LL * sms), 256, 0, irwls_stream()>>>(
+        d_KSC, m, d_act, nact, d_sd, d_day, cmax, ct * GM, npb, S);
+    IRWLS_LAUNCH_CHECK("gram_slice");
+    const size_t smem = (size_t)GNS * G_STAGE + 1024;
+    cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    gram_tc_kernel<<<dim3(nt, ct, pz), G_THREADS, smem, irwls_stream()>>>(S, npb, spc, m, cmax, d_part,
+                                                                          irwls_dev_flags());
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_GRAM);
+    IRWLS_LAUNCH_CHECK("gram_tc");
+    return irwls_par_gram_reduce(d_part, pz, m, d_KC, d_K1, ldK1);
+}

@@ -190,6 +190,15 @@ int irwls_par_df_lda(int m);
 int irwls_par_gram_df(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                       const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P,
                       void *d_A);
+/* Precision form of the Gram on the tensor cores (dev_gram_tc.cu): A' as
+   exact base-64 integer digits per column scale, digit-pair products summed
+   exactly in FP32 tensor memory and drained into 96-bit integers; d_ws holds
+   irwls_par_gram_tc_bytes(l, m) bytes for up to l active rows. */
+size_t irwls_par_gram_tc_bytes(int l, int m);
+int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
+                      const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P,
+                      void *d_ws);
+int irwls_par_gram_reduce(const double *d_part, int P, int m, const double *d_KC, double *d_K1, int ldK1);
 int irwls_par_residual(const double *d_KSC, int l, int m, const double *d_beta, const double *d_y, double C,
                        double M, double *d_e, double *d_Da);
 int irwls_par_weights(const double *d_Da, const double *d_y, int l, int *d_act, double *d_sd, double *d_day,

@@ -1,0 +1,81 @@
+// tc_ptx.cuh -- inline-PTX building blocks of the tcgen05 kernels (sm_103a):
+// shared-memory operand descriptors, the instruction descriptor, MMA issue,
+// bounded mbarrier waits, commits, bulk copies and tensor-memory loads.
+// Every wait is bounded by TC_WAIT_LIMIT polls and reports a timeout to its
+// caller instead of spinning on.
+#pragma once
+#include <stdint.h>
+
+namespace {
+
+constexpr long long TC_WAIT_LIMIT = 1LL << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    // D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16 (bits 10-12 = 1), K-major A
+    // and B, N >> 3 at bit 17, M >> 4 at bit 24
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (long long it = 0; it < TC_WAIT_LIMIT && !done; ++it) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity));
+    }
+    return done != 0;
+}
+
+// Descriptor of a K-major, no-swizzle operand in shared memory: core
+// matrices of 8 rows x 16 bytes, LBO bytes apart along K and SBO bytes apart
+// along the rows.
+__device__ __forceinline__ uint64_t tc_desc_lbo_sbo(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+__device__ __forceinline__ uint64_t tc_desc_sbo(uint32_t saddr, uint32_t sbo) { return tc_desc_lbo_sbo(saddr, 128, sbo); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(b)));
+}
+__device__ __forceinline__ void tc_commit(uint64_t *b) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(b)));
+}
+__device__ __forceinline__ void tc_ld8_lanes(uint32_t tmem, int lane_base, int c0, float *v) {
+    uint32_t r[8];
+    const uint32_t addr = tmem + ((uint32_t)lane_base << 16) + (uint32_t)c0;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Bulk global -> shared copy completing on an mbarrier's transaction count
+// (both addresses 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(uint32_t sdst, const void *gsrc, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(sdst),
+                 "l"(gsrc), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+}  // namespace
