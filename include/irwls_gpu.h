@@ -57,7 +57,8 @@ void irwls_profile_enable(int on);
 void irwls_profile_reset(void);
 /* slot: 0 SGMA score GEMM, 1 Gram update, 2 kernel row sums, 3 Cholesky
  * solve, 4 prediction, 5 SGMA candidate rows and solves, 6 SGMA selection
- * and factor/column update. Total milliseconds and launches since the reset. */
+ * and factor/column update, 7 digit slicing of the precision form's Gram.
+ * Total milliseconds and launches since the reset. */
 void irwls_profile_read(int slot, double *ms, long long *launches);
 /* Kernel launches issued by the library since it was loaded. */
 long long irwls_kernel_launches(void);
@@ -66,6 +67,9 @@ void irwls_last_run_info(int *par_iterations, int *active_rows);
 /* Algorithmic flops of the last IRWLSpar run's Gram updates: the sum over
  * iterations of active_rows * (m + 1) * m (lower triangle and K2 row). */
 double irwls_last_gram_flops(void);
+/* bf16 tensor-core flops issued by the precision form's Gram kernel since
+ * the last call with reset != 0 (36 digit-pair products per tile step). */
+double irwls_gram_tc_flops(int reset);
 /* Host-to-device and device-to-host bytes copied since the library was loaded. */
 void irwls_transfer_bytes(long long *h2d, long long *d2h);
 /* Overwrites a device buffer of `bytes` bytes (allocated on first use) so

@@ -222,6 +222,13 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
         g_last_nact = nact;
     }
     if (irwls_dev_d2h(weights_out, d_bbest, (size_t)m * sizeof(double)) || irwls_dev_sync()) goto fail;
+    if (mixed) {
+        const int tc = irwls_tc_status();
+        if (tc) {
+            irwls_set_error(-13, "a tensor-core pipeline wait of the Gram ran out (code %d)", tc);
+            goto fail;
+        }
+    }
     goto done;
 fail:
     rc = -1;

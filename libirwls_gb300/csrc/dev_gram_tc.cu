@@ -178,6 +178,13 @@ __device__ __forceinline__ void tc_ld4(uint32_t addr, float *v) {
     v[3] = __uint_as_float(r3);
 }
 
+// Records the first wait that ran out in device flag word 1 as
+// role * 10^8 + cta * 1000 + stage (role 1: producer empty, 2: producer
+// drain, 3: MMA acc-empty, 4: MMA full, 5: MMA done, 6: drain acc-full).
+__device__ __forceinline__ void gram_timeout(int *flags, int role, int cta, int k) {
+    atomicCAS(flags + 1, 0, role * 100000000 + min(cta, 99999) * 1000 + min(max(k, 0), 999));
+}
+
 // 96-bit accumulator hi * 2^32 + lo (hi signed).
 struct Acc96 {
     long long hi;
@@ -204,6 +211,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
     unsigned char *smem = g_smem + ((1024 - (smem_u32(g_smem) & 1023)) & 1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k0 = z * spc, nst = max(0, min(npb, k0 + spc) - k0);
+    const int cta = (int)(blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z));
     const int nblk = (nst + GDRAIN - 1) / GDRAIN;
     if (threadIdx.x == 0) {
         for (int b = 0; b < GNS; ++b) {
@@ -235,7 +243,10 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
             int issued = 0;
             for (int k = 0; k < nst; ++k) {
                 const int slot = k % GNS;
-                if (k >= GNS && !mbar_wait(smem_u32(&empty[slot]), (uint32_t)(k / GNS - 1) & 1u)) abort_flag = 1;
+                if (k >= GNS && !mbar_wait(smem_u32(&empty[slot]), (uint32_t)(k / GNS - 1) & 1u)) {
+                    gram_timeout(flags, 1, cta, k);
+                    abort_flag = 1;
+                }
                 if (abort_flag) break;
                 const uint32_t sb = base + slot * G_STAGE, fb = smem_u32(&full[slot]);
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(G_STAGE));
@@ -246,7 +257,10 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
                 issued = k + 1;
             }
             for (int k = issued > GNS ? issued - GNS : 0; k < issued; ++k)
-                if (!mbar_wait(smem_u32(&full[k % GNS]), (uint32_t)(k / GNS) & 1u)) abort_flag = 1;
+                if (!mbar_wait(smem_u32(&full[k % GNS]), (uint32_t)(k / GNS) & 1u)) {
+                    gram_timeout(flags, 2, cta, k);
+                    abort_flag = 1;
+                }
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -258,12 +272,14 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
                 const int blk = k / GDRAIN, kin = k % GDRAIN;
                 if (kin == 0 && blk >= 1) {
                     if (!mbar_wait(smem_u32(&acce), (uint32_t)(blk - 1) & 1u)) {
+                        gram_timeout(flags, 3, cta, k);
                         abort_flag = 1;
                         break;
                     }
                 }
                 const int slot = k % GNS;
                 if (!mbar_wait(smem_u32(&full[slot]), (uint32_t)(k / GNS) & 1u)) {
+                    gram_timeout(flags, 4, cta, k);
                     abort_flag = 1;
                     break;
                 }
@@ -284,7 +300,10 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
                 if (kin == GDRAIN - 1 || k == nst - 1) tc_commit(&accf);
             }
             tc_commit(&done);
-            if (!mbar_wait(smem_u32(&done), 0u)) abort_flag = 1;
+            if (!mbar_wait(smem_u32(&done), 0u)) {
+                gram_timeout(flags, 5, cta, nst);
+                abort_flag = 1;
+            }
         }
         __syncwarp();
     } else if (warp >= 4) {
@@ -294,7 +313,9 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
 #pragma unroll
         for (int j = 0; j < 32; ++j) T[j] = Acc96{0, 0u};
         for (int blk = 0; blk < nblk; ++blk) {
-            const int bad = (!mbar_wait(smem_u32(&accf), (uint32_t)blk & 1u) || abort_flag) ? 1 : 0;
+            const bool got = mbar_wait(smem_u32(&accf), (uint32_t)blk & 1u);
+            if (!got) gram_timeout(flags, 6, cta, blk * GDRAIN);
+            const int bad = (!got || abort_flag) ? 1 : 0;
             int any;
             asm volatile(
                 "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, 1, 256, p;\nselp.s32 %0, 1, 0, q;\n}\n"
@@ -351,7 +372,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
             }
         }
     }
-    if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
+    if (threadIdx.x == 0 && abort_flag) gram_timeout(flags, 9, cta, 0);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
@@ -364,6 +385,15 @@ size_t slices_bytes(int l, int m) {
 }
 
 }  // namespace
+
+// bf16 tensor-core flops issued by gram_tc_kernel since the last read (36
+// digit-pair products per 128 x 64 x 16 step of every tile).
+static double g_tc_flops = 0.0;
+extern "C" double irwls_gram_tc_flops(int reset) {
+    const double f = g_tc_flops;
+    if (reset) g_tc_flops = 0.0;
+    return f;
+}
 
 // Workspace of irwls_par_gram_tc for up to l active rows: the slices, then the
 // m + 1 column maxima.
@@ -391,7 +421,7 @@ extern "C" int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, i
     pz = std::min(pz, npb);
     const int spc = ceil_div(npb, pz);
     pz = ceil_div(npb, spc);
-    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM);
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM_SLICE);
     if (irwls_dev_memset(cmax, 0, (size_t)(m + 1) * sizeof(unsigned long long))) return -1;
     if (nact > 0) {
         gram_colmax_kernel<<<dim3(ceil_div(m + 1, 256), ceil_div(nact, GCM)), 256, 0, irwls_stream()>>>(
@@ -401,11 +431,14 @@ extern "C" int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, i
     const long long items = (long long)ct * GM * npb * 2;
     gram_slice_kernel<<<(int)std::min<long long>(ceil_div(items, 256), 16LL * sms), 256, 0, irwls_stream()>>>(
         d_KSC, m, d_act, nact, d_sd, d_day, cmax, ct * GM, npb, S);
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_GRAM_SLICE);
     IRWLS_LAUNCH_CHECK("gram_slice");
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM);
     const size_t smem = (size_t)GNS * G_STAGE + 1024;
     cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     gram_tc_kernel<<<dim3(nt, ct, pz), G_THREADS, smem, irwls_stream()>>>(S, npb, spc, m, cmax, d_part,
                                                                           irwls_dev_flags());
+    g_tc_flops += (double)tiles * npb * GBK * GM * GN * 2.0 * 36;
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_GRAM);
     IRWLS_LAUNCH_CHECK("gram_tc");
     return irwls_par_gram_reduce(d_part, pz, m, d_KC, d_K1, ldK1);

@@ -439,7 +439,8 @@ extern "C" int irwls_split_bf16_f32(const float *X, long long rows, int cols, in
     return 0;
 }
 
-// Reads (and clears) the tensor-core wait-failure flag.
+// Reads (and clears) the tensor-core wait-failure flag: 0, or the nonzero
+// code the failing kernel left (which wait of which CTA ran out).
 extern "C" int irwls_tc_status(void) {
     int flags[8];
     cudaMemcpyAsync(flags, irwls_dev_flags(), sizeof flags, cudaMemcpyDeviceToHost, irwls_stream());
@@ -448,7 +449,7 @@ extern "C" int irwls_tc_status(void) {
         int zero = 0;
         cudaMemcpyAsync(irwls_dev_flags() + 1, &zero, sizeof zero, cudaMemcpyHostToDevice, irwls_stream());
         cudaStreamSynchronize(irwls_stream());
-        return 1;
+        return flags[1];
     }
     return 0;
 }

@@ -195,6 +195,9 @@ int irwls_par_gram_df(const double *d_KSC, int m, const int *d_act, int nact, co
    exactly in FP32 tensor memory and drained into 96-bit integers; d_ws holds
    irwls_par_gram_tc_bytes(l, m) bytes for up to l active rows. */
 size_t irwls_par_gram_tc_bytes(int l, int m);
+/* Reads and clears device flag word 1: 0, or the code a tensor-core kernel
+   left when one of its bounded waits ran out. */
+int irwls_tc_status(void);
 int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                       const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P,
                       void *d_ws);
@@ -244,7 +247,8 @@ int irwls_prof_collect(void);
 void irwls_prof_read(int slot, double *ms, long long *launches);
 void irwls_prof_reset(void);
 enum { IRWLS_PROF_SGMA_GEMM = 0, IRWLS_PROF_GRAM = 1, IRWLS_PROF_ROWSUM = 2, IRWLS_PROF_CHOL = 3,
-       IRWLS_PROF_PREDICT = 4, IRWLS_PROF_SGMA_CAND = 5, IRWLS_PROF_SGMA_UPDATE = 6, IRWLS_PROF_SLOTS = 8 };
+       IRWLS_PROF_PREDICT = 4, IRWLS_PROF_SGMA_CAND = 5, IRWLS_PROF_SGMA_UPDATE = 6, IRWLS_PROF_GRAM_SLICE = 7,
+       IRWLS_PROF_SLOTS = 8 };
 long long irwls_launch_count(void);
 void irwls_count_launch(int n);
 

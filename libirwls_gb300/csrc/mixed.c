@@ -51,7 +51,6 @@ int irwls_learn_predict(void *mlp, const float *d_F, int n, float *d_pred);
 int irwls_learn_topk(const float *d_pred, const int *d_pool, int half, int keep, int nrand, int *d_out);
 int irwls_learn_residual_trace(const float *d_qn, int l, double *d_out);
 int irwls_mlp_feature_count(void);
-int irwls_tc_status(void);
 int *irwls_draw_sgma_candidates(const svm_dataset *ds, int m);
 void irwls_record_run_info(int par_iterations, int active_rows);
 
@@ -225,9 +224,12 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
         rc |= irwls_dev_d2h(cent_out, d_cent, (size_t)m * sizeof(int));
         rc |= irwls_dev_d2h(val, d_val, (size_t)m * sizeof(double));
         rc |= irwls_dev_sync();
-        if (!rc && irwls_tc_status()) {
-            irwls_set_error(-13, "a tensor-core pipeline wait ran out");
-            rc = -13;
+        if (!rc) {
+            const int tc = irwls_tc_status();
+            if (tc) {
+                irwls_set_error(-13, "a tensor-core pipeline wait ran out (code %d)", tc);
+                rc = -13;
+            }
         }
         if (!rc && props.verbose == 1) {
             for (int s = 0; s < m; s++) {
