@@ -580,124 +580,6 @@ __global__ void gram_reduce_kernel(const double *__restrict__ part, int P, int m
     }
 }
 
-// ---- precision form of the Gram: double-float (FP32 pair) accumulation ----
-//
-// The FP64 pipe of this part runs at 1/64 of the FP32 rate, so the precision
-// form keeps A' = [sd * KSC[act, :], day] as unevaluated FP32 pairs hi + lo
-// (|v - hi - lo| <= 2^-48 |v|) and forms each product as
-// hi_a hi_b (rounded) + err(hi_a hi_b) + hi_a lo_b + lo_a hi_b, where err is
-// the exact FMA residual; the rounded part is added to the running sum with
-// Knuth's TwoSum (error-free) and the rest goes to a compensation term. Twelve
-// FP32 instructions per product; every add and multiply is written with an
-// _rn intrinsic so that no contraction can merge them.
-
-// A'[p][c] for c < m, day_p at c == m, zeros up to lda; lda is a multiple of
-// 64 so the Gram tiles never leave the row.
-__global__ void df_pack_kernel(const double *__restrict__ KSC, int m, const int *__restrict__ act, int nact,
-                               const double *__restrict__ sd, const double *__restrict__ day, float2 *__restrict__ A,
-                               int lda) {
-    const long long total = (long long)nact * lda;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int p = (int)(t / lda), c = (int)(t % lda);
-        double v = 0.0;
-        if (c < m)
-            v = __dmul_rn(sd[p], KSC[(size_t)act[p] * m + c]);
-        else if (c == m)
-            v = day[p];
-        const float h = __double2float_rn(v);
-        A[t] = make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
-    }
-}
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
-}
-
-// (S, c) += a * b in double-float.
-__device__ __forceinline__ void df_fma(float &S, float &c, float2 a, float2 b) {
-    const float p = __fmul_rn(a.x, b.x);
-    float q = fmaf(a.x, b.x, -p);
-    q = fmaf(a.x, b.y, q);
-    q = fmaf(a.y, b.x, q);
-    const float t = __fadd_rn(S, p);
-    const float z = __fsub_rn(t, S);
-    const float e = __fadd_rn(__fsub_rn(S, __fsub_rn(t, z)), __fsub_rn(p, z));
-    S = t;
-    c = __fadd_rn(c, __fadd_rn(e, q));
-}
-
-// Tile (bi, bj), bi >= bj, of the lower triangle of A'^T A' (rows 0..m,
-// columns < m) over the active rows of chunk z; writes FP64 partials in the
-// layout of gram_kernel so gram_reduce_kernel finishes both forms.
-constexpr int DT = 64, DK = 16;
-__global__ void __launch_bounds__(256) gram_df_kernel(const float2 *__restrict__ A, int lda, int m, int nact,
-                                                      int chunk, double *__restrict__ part) {
-    const int bj = blockIdx.x, bi = blockIdx.y, z = blockIdx.z;
-    if (bi < bj) return;
-    const int r0 = bi * DT, c0 = bj * DT;
-    const int p0 = z * chunk, p1 = min(nact, p0 + chunk);
-    __shared__ __align__(16) float2 Ai[2][DK][DT];
-    __shared__ __align__(16) float2 Aj[2][DK][DT];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    float S[4][4], Cc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) S[a][b] = Cc[a][b] = 0.0f;
-    // DK rows x 64 pairs = 512 16-byte pieces per operand: two per thread.
-    auto load = [&](int buf, int p) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int t = tid + 256 * h;
-            const int kk = t >> 5, cc = (t & 31) * 2;
-            const int pp = p + kk;
-            const bool ok = pp < p1;
-            const float2 *row = A + (size_t)(ok ? pp : 0) * lda;
-            cp_async16(&Ai[buf][kk][cc], row + r0 + cc, ok ? 16 : 0);
-            cp_async16(&Aj[buf][kk][cc], row + c0 + cc, ok ? 16 : 0);
-        }
-        cp_async_commit();
-    };
-    if (p0 < p1) load(0, p0);
-    int it = 0;
-    for (int p = p0; p < p1; p += DK, ++it) {
-        const int buf = it & 1;
-        if (p + DK < p1) {
-            load(buf ^ 1, p + DK);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int kk = 0; kk < DK; ++kk) {
-            float2 ai[4], aj[4];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) ai[a] = Ai[buf][kk][ty + 16 * a];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) aj[b] = Aj[buf][kk][tx + 16 * b];
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) df_fma(S[a][b], Cc[a][b], ai[a], aj[b]);
-        }
-        __syncthreads();
-    }
-    double *out = part + (size_t)z * (m + 1) * m;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        const int r = r0 + ty + 16 * a;
-        if (r > m) continue;
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int c = c0 + tx + 16 * b;
-            if (c < m && c <= r) out[(size_t)r * m + c] = __dadd_rn((double)S[a][b], (double)Cc[a][b]);
-        }
-    }
-}
-
 // e = y - KSC beta, then Da (src/budgeted-train.c:431-457). One warp per row.
 __global__ void residual_kernel(const double *__restrict__ KSC, int l, int m, const double *__restrict__ beta,
                                 const double *__restrict__ y, double C, double M, double *__restrict__ e,
@@ -955,32 +837,6 @@ extern "C" int irwls_par_gram(const double *d_KSC, int m, const int *d_act, int 
     IRWLS_LAUNCH_CHECK("gram");
     const long long total = (long long)(m + 1) * m;
     gram_reduce_kernel<<<(int)std::min<long long>(ceil_div(total, 256), 65535), 256, 0, irwls_stream()>>>(
-        d_part, P, m, d_KC, d_K1, ldK1);
-    IRWLS_LAUNCH_CHECK("gram_reduce");
-    return 0;
-}
-
-extern "C" int irwls_par_df_lda(int m) { return ceil_div(m + 1, DT) * DT; }
-
-extern "C" int irwls_par_gram_df(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
-                                 const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part,
-                                 int P, void *d_A) {
-    const int lda = irwls_par_df_lda(m);
-    float2 *A = (float2 *)d_A;
-    const long long total = (long long)nact * lda;
-    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM);
-    if (total > 0) {
-        df_pack_kernel<<<(int)std::min<long long>(ceil_div(total, 256), 16LL * 152 * 8), 256, 0, irwls_stream()>>>(
-            d_KSC, m, d_act, nact, d_sd, d_day, A, lda);
-        IRWLS_LAUNCH_CHECK("df_pack");
-    }
-    const int T = ceil_div(m + 1, DT), Tc = ceil_div(m, DT);
-    const int chunk = nact > 0 ? ceil_div(nact, P) : 1;
-    gram_df_kernel<<<dim3(Tc, T, P), 256, 0, irwls_stream()>>>(A, lda, m, nact, chunk, d_part);
-    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_GRAM);
-    IRWLS_LAUNCH_CHECK("gram_df");
-    const long long tot = (long long)(m + 1) * m;
-    gram_reduce_kernel<<<(int)std::min<long long>(ceil_div(tot, 256), 65535), 256, 0, irwls_stream()>>>(
         d_part, P, m, d_KC, d_K1, ldK1);
     IRWLS_LAUNCH_CHECK("gram_reduce");
     return 0;

@@ -402,7 +402,7 @@ extern "C" size_t irwls_par_gram_tc_bytes(int l, int m) {
 }
 
 // K1 (column-major, leading dimension ldK1, lower part) = KC + the Gram of
-// the active rows, row m = K2, as irwls_par_gram_df gives; P bounds the
+// the active rows, row m = K2, as irwls_par_gram gives; P bounds the
 // split-K chunks (part holds at least P partials).
 extern "C" int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                                  const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part,

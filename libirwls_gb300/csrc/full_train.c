@@ -274,6 +274,13 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
         }
     }
     if (irwls_dev_d2h(beta_out, bnew, L1 * sizeof(double)) || irwls_dev_sync()) goto fail;
+    if (tcs) {
+        const int tc = irwls_tc_status();
+        if (tc) {
+            irwls_set_error(-13, "a tensor-core pipeline wait of the error update ran out (code %d)", tc);
+            goto fail;
+        }
+    }
     goto done;
 fail:
     rc = -1;

@@ -183,13 +183,6 @@ int irwls_par_first(const double *d_y, int l, double M, int *d_act, double *d_sd
 size_t irwls_par_gram_part_bytes(int m, int P);
 int irwls_par_gram(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                    const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P);
-/* Precision form of the Gram: A' packed as FP32 hi/lo pairs (d_A holds
-   nact x irwls_par_df_lda(m) pairs), double-float products and sums, FP64
-   reduction of the P partials. */
-int irwls_par_df_lda(int m);
-int irwls_par_gram_df(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
-                      const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P,
-                      void *d_A);
 /* Precision form of the Gram on the tensor cores (dev_gram_tc.cu): A' as
    exact base-64 integer digits per column scale, digit-pair products summed
    exactly in FP32 tensor memory and drained into 96-bit integers; d_ws holds
