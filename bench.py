@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
-    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned"])
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned", "linear_predict"])
     ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
@@ -865,6 +865,140 @@ def run_batch(args):
 
 
 # ----------------------------------------------------------------------------
+# linear-kernel prediction through the primal weights
+# ----------------------------------------------------------------------------
+LINP = dict(n_sv_rows=50_000, n_test=200_000, cpu_rows=20_000, seed=20240611)
+LINP_DESC = ("linear-kernel prediction: softTest of 200000 sparse test rows (d=300, 3%% nonzero, values binary or "
+             "U[0,1]) against a linear model of %d support vectors (seeded weights): the primal fast path "
+             "(irwls_set_linear_fast_path) against the per-support-vector kernel sum")
+
+
+def run_linear_predict(args):
+    import numpy as np
+
+    from libirwls_gb300 import _abi, load, synth
+
+    n_sv, n_te = LINP["n_sv_rows"], LINP["n_test"]
+    pool = synth.sparse_linear_pool(n_sv + n_te, seed=LINP["seed"])
+    cut = int(pool.indptr[n_sv])
+    tr = _abi.build_dataset(pool.indptr[:n_sv + 1], pool.indices[:cut], pool.values[:cut], pool.y[:n_sv])
+    te = _abi.build_dataset(pool.indptr[n_sv:] - cut, pool.indices[cut:], pool.values[cut:], pool.y[n_sv:])
+    rng = np.random.default_rng(LINP["seed"])
+    beta = np.ascontiguousarray(np.where(rng.random(n_sv + 1) < 0.6, rng.standard_normal(n_sv + 1), 0.0))
+    nsv = int((beta[:-1] != 0).sum())
+    prop = _abi.make_properties(gamma=1.0, C_=1.0, kernel=0)
+    pp = _abi.make_predict_properties(labels=0, soft=1)
+    metric = "linear-kernel prediction s (soft decision values of %d test rows)" % n_te
+    cfg = {"workload": LINP_DESC % nsv, "test_rows": n_te, "support_vectors": nsv, "d": 300,
+           "nnz_test": int(pool.indptr[-1] - cut), "form": "primal fast path", "parallelism": "single GPU",
+           "l2": "flushed before each call; the test set is uploaded by every call"}
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+
+    def cpu_line():
+        os.environ["OPENBLAS_NUM_THREADS"] = "1"
+        port_path = os.path.join(ROOT, "oracle", "_build", "libirwls_port.so")
+        if not os.path.exists(port_path):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+        port = _abi.load_library(port_path)
+        cores = os.cpu_count() or 1
+        k = LINP["cpu_rows"]
+        sub = _abi.build_dataset(pool.indptr[n_sv:n_sv + k + 1] - cut, pool.indices[cut:int(pool.indptr[n_sv + k])],
+                                 pool.values[cut:int(pool.indptr[n_sv + k])], pool.y[n_sv:n_sv + k])
+        # the model is packed by this library's host packing (byte-identical to
+        # the reference's calculateFULLModel, no device work, not timed)
+        from libirwls_gb300 import load as load_ours
+
+        pc = _abi.make_properties(gamma=1.0, C_=1.0, kernel=0, threads=cores)
+        mdl_c = load_ours().calculateFULLModel(pc, tr.struct, beta.ctypes.data_as(PD))
+        ppc = _abi.make_predict_properties(labels=0, soft=1, threads=cores)
+        t0 = time.perf_counter()
+        libc.free(C.cast(port.softTest(sub.struct, mdl_c, ppc), C.c_void_p))
+        dt = time.perf_counter() - t0
+        return {"value": round(dt * n_te / k, 3), "unit": "s", "cores": cores, "kind": "port",
+                "sample": "the restatement's softTest (per-support-vector kernel sum, OpenMP over test rows) on "
+                          "the first %d test rows, scaled to %d" % (k, n_te)}
+
+    if args.impl == "reference":
+        base = cpu_line()
+        print(json.dumps({"metric": metric, "value": base["value"], "unit": "s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": base["value"] * 1000,
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded generator)", "config": cfg, "cpu_baseline": base,
+                          "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    lib = load()
+    if not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    mdl = lib.calculateFULLModel(prop, tr.struct, beta.ctypes.data_as(PD))
+
+    def predict(fast):
+        lib.irwls_set_linear_fast_path(fast)
+        lib.irwls_l2_flush(512 << 20)
+        lib.irwls_dev_sync()
+        h0, d0 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
+        t0 = time.perf_counter()
+        ptr = lib.softTest(te.struct, mdl, pp)
+        dt = time.perf_counter() - t0
+        if not ptr:
+            raise SystemExit("prediction failed: " + lib.irwls_last_error_message().decode())
+        f = np.ctypeslib.as_array(ptr, shape=(n_te,)).copy()
+        libc.free(C.cast(ptr, C.c_void_p))
+        h1, d1 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
+        return dt, f, h1.value - h0.value, d1.value - d0.value
+
+    predict(0)
+    kern_s, f_kern, _, _ = predict(0)
+    for _ in range(args.warmup):
+        predict(1)
+    lib.irwls_profile_enable(1)
+    lib.irwls_profile_reset()
+    launches0 = lib.irwls_kernel_launches()
+    clocks = Clocks(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        dt, f_fast, h2d, d2h = predict(1)
+        times.append(dt)
+    clk = clocks.stop()
+    launches = lib.irwls_kernel_launches() - launches0
+    k_s = profile_read(lib, 4, args.steps)[0]
+    lib.irwls_profile_enable(0)
+    lib.irwls_set_linear_fast_path(0)
+    value = statistics.mean(times)
+    scale = float(np.abs(f_kern).max())
+    diff = float(np.abs(f_fast - f_kern).max() / scale)
+    clear = np.abs(f_kern) > 1e-10 * scale
+    labels_equal = bool(np.array_equal(np.sign(f_fast[clear]), np.sign(f_kern[clear])))
+    peaks, peak_src = measured_peaks()
+    nnz = cfg["nnz_test"]
+    # test CSR entries, row pointers and decision values, plus the model's dense
+    # rows read once to form W (nsv x 300 doubles)
+    alg = nnz * 12 + (n_te + 1) * 4 + n_te * 8 + nsv * 300 * 8
+    ach = alg / k_s / 1e9 if k_s > 0 else 0.0
+    line = {"metric": metric, "value": round(value, 4), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 2), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": cfg,
+            "e2e": {"value": round(value, 4), "unit": "s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "note": "softTest takes a host svm_dataset: every call uploads the test set and the model"},
+            "gpu_launches": int(launches // max(args.steps, 1)),
+            "roofline": {"bound": "hbm", "kernel": "linear_w_kernel + linear_dot_kernel",
+                         "achieved": round(ach, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": round(ach / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None,
+                         "traffic": None, "peak_source": peak_src, "kernel_s": round(k_s, 6),
+                         "algorithmic_bytes": alg},
+            "cpu_baseline": None if args.no_cpu else cpu_line(), "clocks": clk,
+            "kernel_sum_path_s": round(kern_s, 4), "speedup_vs_kernel_sum": round(kern_s / value, 2),
+            "parity": {"max_abs_diff_over_max_abs_f": diff, "labels_equal_where_clear": labels_equal}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
 # learned-proposal form of SGMA
 # ----------------------------------------------------------------------------
 LEARN = dict(n=1_000_000, n_test=20_000, gamma=0.5, C=10.0, trace_sets=10, trace_rows=20_000, pool=4096)
@@ -1016,6 +1150,8 @@ def main():
         run_batch(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "linear_predict":
+        run_linear_predict(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -21,17 +21,30 @@ const char *irwls_last_error_message(void);
  * device every training or prediction call fails with an error. */
 int irwls_gpu_available(void);
 
-/* Arithmetic of SGMA centroid selection:
+/* Arithmetic of the training paths:
  * IRWLS_PRECISION_FP64 (default): FP64 throughout, reference parity;
- * IRWLS_PRECISION_MIXED: the precision form -- candidate scores computed as
+ * IRWLS_PRECISION_MIXED: the precision form -- SGMA candidate scores as
  * split-BF16 tensor-core products (FP32 accumulation) on the Nystrom
  * features of the current centroids, with the K_mm factorization and its
- * solves in FP64. It can pick a different centroid where two candidates
- * score within about 1e-5 of each other; IRWLSpar stays FP64 in both forms.
- * The environment variable IRWLS_PRECISION=mixed selects it at start-up. */
+ * solves in FP64 (it can pick a different centroid where two candidates
+ * score within about 1e-5 of each other); the IRWLSpar Gram from exact
+ * integer digit products on the tensor cores (about 2^-45 of the column
+ * scales per row), its Cholesky, solves, residual and stop test in FP64;
+ * in full IRWLS, the error updates of rows away from the margin on the
+ * tensor cores. The environment variable IRWLS_PRECISION=mixed selects it
+ * at start-up. */
 enum { IRWLS_PRECISION_FP64 = 0, IRWLS_PRECISION_MIXED = 1 };
 void irwls_set_precision(int mode);
 int irwls_get_precision(void);
+
+/* Linear-kernel prediction fast path (off by default): test()/softTest() of
+ * a model with kernelType 0 evaluate b + x . W with W = sum_j w_j sv_j formed
+ * once on the device, instead of the reference's per-support-vector kernel
+ * sum (src/LIBIRWLS-predict.c:56-131); decision values then differ from the
+ * reference's in the last bits (summation order). The environment variable
+ * IRWLS_LINEAR_FAST=1 turns it on at start-up. */
+void irwls_set_linear_fast_path(int on);
+int irwls_get_linear_fast_path(void);
 
 /* A training set uploaded to the GPU once (rows l + 2 when the class-mean
  * rows exist), for repeated training without host-to-device traffic. */

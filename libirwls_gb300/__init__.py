@@ -53,6 +53,8 @@ def load() -> C.CDLL:
         "irwls_last_run_info": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "irwls_last_gram_flops": (C.c_double, []),
         "irwls_gram_tc_flops": (C.c_double, [C.c_int]),
+        "irwls_set_linear_fast_path": (None, [C.c_int]),
+        "irwls_get_linear_fast_path": (C.c_int, []),
         "irwls_full_train_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
         "irwls_budgeted_train_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                                  C.c_void_p]),

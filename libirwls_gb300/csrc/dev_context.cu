@@ -292,8 +292,9 @@ extern "C" int irwls_model_feature_width(const model *m) {
     return w;
 }
 
+// csr_only: no dense copy X (for consumers that read the rows as CSR only).
 static int upload_rows(svm_sample *const *rows, const double *q, const double *y, int n_rows, int mode,
-                       double gamma, int raw_width, int width_hint, irwls_dev_set *out) {
+                       double gamma, int raw_width, int width_hint, irwls_dev_set *out, int csr_only = 0) {
     memset(out, 0, sizeof *out);
     if (irwls_dev_init()) return -1;
     out->n_rows = n_rows;
@@ -319,13 +320,13 @@ static int upload_rows(svm_sample *const *rows, const double *q, const double *y
         irwls_set_error(-4, "dataset has %lld stored entries; the device layout indexes them with int32", nnz);
         return -4;
     }
-    const size_t xbytes = (size_t)n_rows * out->ld * sizeof(double);
+    const size_t xbytes = csr_only ? 0 : (size_t)n_rows * out->ld * sizeof(double);
     const size_t bytes = xbytes + (size_t)(n_rows + 1) * sizeof(int) + (size_t)nnz * (sizeof(int) + sizeof(double)) +
                          2 * (size_t)n_rows * sizeof(double);
     void *h = nullptr;
     if (irwls_dev_host_alloc(&h, bytes)) return -3;
     double *hX = (double *)h;
-    double *hq = hX + (size_t)n_rows * out->ld;
+    double *hq = hX + xbytes / sizeof(double);
     double *hy = hq + n_rows;
     double *hcv = hy + n_rows;
     int *hrp = (int *)(hcv + nnz);
@@ -334,14 +335,14 @@ static int upload_rows(svm_sample *const *rows, const double *q, const double *y
     long long k = 0;
     for (int i = 0; i < n_rows; ++i) {
         hrp[i] = (int)k;
-        double *row = hX + (size_t)i * out->ld;
-        if (mode == IRWLS_K_RAW_RBF) {
+        double *row = csr_only ? nullptr : hX + (size_t)i * out->ld;
+        if (row && mode == IRWLS_K_RAW_RBF) {
             // maxdim consecutive values from the row start, as src/kernels.c:93-97 reads them
             const svm_sample *p = rows[i];
             for (int t = 0; t < raw_width; ++t) row[t] = p[t].value;
         }
         for (const svm_sample *p = rows[i]; p->index != -1; ++p) {
-            if (mode != IRWLS_K_RAW_RBF) row[p->index] = p->value;
+            if (row && mode != IRWLS_K_RAW_RBF) row[p->index] = p->value;
             hci[k] = p->index;
             hcv[k] = p->value;
             ++k;
@@ -373,6 +374,13 @@ static int upload_rows(svm_sample *const *rows, const double *q, const double *y
         return rc ? rc : -3;
     }
     return 0;
+}
+
+// The rows of ds as CSR only (no dense copy): for the linear prediction path.
+extern "C" int irwls_dev_upload_csr(const svm_dataset *ds, int n_rows, int kernelType, double gamma, int width_hint,
+                                    irwls_dev_set *out) {
+    const int mode = kernelType == 0 ? IRWLS_K_LINEAR : IRWLS_K_NORM_RBF;
+    return upload_rows(ds->x, ds->quadratic_value, ds->y, n_rows, mode, gamma, ds->maxdim, width_hint, out, 1);
 }
 
 extern "C" int irwls_dev_upload(const svm_dataset *ds, int n_rows, int kernelType, double gamma, int force_norm,

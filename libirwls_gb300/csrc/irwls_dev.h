@@ -75,6 +75,10 @@ typedef struct irwls_dev_set {
  * by-index layout (so two sets share one column space). */
 int irwls_dev_upload(const svm_dataset *ds, int n_rows, int kernelType, double gamma, int force_norm,
                      int width_hint, irwls_dev_set *out);
+/* The same rows as CSR only (X holds no dense copy): for the linear
+ * prediction path. */
+int irwls_dev_upload_csr(const svm_dataset *ds, int n_rows, int kernelType, double gamma, int width_hint,
+                         irwls_dev_set *out);
 /* Same upload from the rows of a model. */
 int irwls_dev_upload_model(const model *m, int width_hint, irwls_dev_set *out);
 void irwls_dev_release(irwls_dev_set *s);
@@ -230,6 +234,9 @@ int irwls_par_dev(const irwls_dev_set *X, int l, const int *idx, properties prop
 /* ---- prediction (dev_predict.cu) ----------------------------------------- */
 int irwls_predict_soft(const irwls_dev_set *T, int n, const irwls_dev_set *S, int nSV, const double *d_w,
                        double bias, int hard, double *d_out);
+size_t irwls_predict_linear_scratch(int width, int nsv);
+int irwls_predict_linear(const irwls_dev_set *T, int n, const irwls_dev_set *S, int nSV, const double *d_w,
+                         double bias, int hard, double *d_W, double *d_out);
 
 /* ---- timing of the dominant kernels ------------------------------------- */
 void irwls_prof_enable(int on);
