@@ -37,6 +37,25 @@ enum { IRWLS_PRECISION_FP64 = 0, IRWLS_PRECISION_MIXED = 1 };
 void irwls_set_precision(int mode);
 int irwls_get_precision(void);
 
+/* The libsvm reader on the GPU: the same svm_dataset as readTrainFile
+ * (reference src/IOStructures.c:88-275) -- rows, labels, norms, the sparse
+ * flag, maxdim and the class-mean rows -- with the text tokenised and every
+ * number converted on the device (exactly as the C library's strtod/strtol).
+ * irwls_parse_libsvm parses len bytes of file content and returns 0, -20 (the
+ * reference's "Wrong file format"), -21 (a hexadecimal number, a NaN payload
+ * or a decimal of more than 19 digits too close to a rounding boundary:
+ * converted by the host reader, not by this one) or -22 (a line longer than
+ * the reference's 99999-byte line buffer), the line in the message.
+ * readTrainFileGPU reads a file, and exits with the reference's message and
+ * status 2 on an error, as readTrainFile does. IRWLS_DEVICE_PARSER=1 makes
+ * readTrainFile itself use the device reader. */
+int irwls_parse_libsvm(const char *buf, size_t len, svm_dataset *ds);
+svm_dataset readTrainFileGPU(char filename[]);
+/* Numbers one per line through the device's strtod (out[i]; status[i]: 0
+ * whole line, 1 trailing text, -1 no number, 2 not converted). Returns the
+ * line count or a negative error. */
+long long irwls_parse_doubles(const char *buf, size_t len, double *out, int *status, long long cap);
+
 /* Linear-kernel prediction fast path (off by default): test()/softTest() of
  * a model with kernelType 0 evaluate b + x . W with W = sum_j w_j sv_j formed
  * once on the device, instead of the reference's per-support-vector kernel

@@ -48,7 +48,12 @@ void freeModel(model modelo) {
  * builds rows with -1 terminators, norms in file order, the sparse flag, and
  * appends the mean of the +1 rows (row l) and of the other rows (row l+1).
  * The norm of row l+1 divides by the positive count, as the reference does. */
+svm_dataset readTrainFileGPU(char filename[]);
+
 svm_dataset readTrainFile(char filename[]) {
+    /* IRWLS_DEVICE_PARSER=1: the same dataset parsed on the GPU (dev_parse.cu) */
+    const char *dev = getenv("IRWLS_DEVICE_PARSER");
+    if (dev && dev[0] == '1') return readTrainFileGPU(filename);
     svm_dataset ds;
     char *line = (char *)malloc(LINE_MAX_CHARS);
     char *end, *tok, *idx, *val;
@@ -145,6 +150,76 @@ svm_dataset readTrainFile(char filename[]) {
     free(sum_neg);
     free(line);
     return ds;
+}
+
+/* The dataset of readTrainFile from rows parsed elsewhere (the device reader,
+ * dev_parse.cu): rows[] holds the l rows in file order, each ended by a -1
+ * entry (row i from row_start[i]); y and q are the labels and row norms. The
+ * class-mean rows l and l + 1 are formed here exactly as readTrainFile forms
+ * them (sums in row order, the negative mean's norm divided by the positive
+ * count), over the pass-1 index range 0 ... maxidx. */
+int irwls_dataset_assemble(svm_dataset *ds, int l, long long pass1_elements, int maxidx, int max_index, int sparse,
+                           const svm_sample *rows, long long row_entries, const long long *row_start,
+                           const double *y, const double *q) {
+    const int top = maxidx > max_index ? maxidx : max_index;
+    long long elements = pass1_elements > row_entries ? pass1_elements : row_entries;
+    elements += 2 * ((long long)maxidx + 2);
+    ds->l = l;
+    ds->sparse = sparse;
+    ds->y = (double *)calloc((size_t)l + 2, sizeof(double));
+    ds->quadratic_value = (double *)calloc((size_t)l + 2, sizeof(double));
+    ds->x = (svm_sample **)calloc((size_t)l + 2, sizeof(svm_sample *));
+    ds->features = (svm_sample *)calloc((size_t)elements, sizeof(svm_sample));
+    double *sum_pos = (double *)calloc((size_t)top + 1, sizeof(double));
+    double *sum_neg = (double *)calloc((size_t)top + 1, sizeof(double));
+    if (!ds->y || !ds->quadratic_value || !ds->x || !ds->features || !sum_pos || !sum_neg) {
+        free(sum_pos);
+        free(sum_neg);
+        irwls_set_error(-3, "host allocation failed while assembling the dataset");
+        return -3;
+    }
+    if (row_entries > 0) memcpy(ds->features, rows, (size_t)row_entries * sizeof(svm_sample));
+    double n_pos = 0.0, n_neg = 0.0;
+    for (int i = 0; i < l; i++) {
+        ds->x[i] = &ds->features[row_start[i]];
+        ds->y[i] = y[i];
+        ds->quadratic_value[i] = q[i];
+        if (y[i] == 1.0) n_pos = n_pos + 1;
+        else n_neg = n_neg + 1;
+        for (const svm_sample *p = ds->x[i]; p->index != -1; ++p) {
+            if (y[i] == 1.0) sum_pos[p->index] += p->value;
+            else sum_neg[p->index] += p->value;
+        }
+    }
+    long long j = row_entries;
+    ds->y[l] = 1.0;
+    ds->x[l] = &ds->features[j];
+    for (int k = 0; k <= maxidx; k++) {
+        if (sum_pos[k] != 0.0) {
+            ds->features[j].index = k;
+            ds->features[j].value = sum_pos[k] / n_pos;
+            const double v = sum_pos[k] / n_pos;
+            ds->quadratic_value[l] += v * v;
+            ++j;
+        }
+    }
+    ds->features[j++].index = -1;
+    ds->y[l + 1] = -1.0;
+    ds->x[l + 1] = &ds->features[j];
+    for (int k = 0; k <= maxidx; k++) {
+        if (sum_neg[k] != 0.0) {
+            ds->features[j].index = k;
+            ds->features[j].value = sum_neg[k] / n_neg;
+            const double v = sum_neg[k] / n_pos;
+            ds->quadratic_value[l + 1] += v * v;
+            ++j;
+        }
+    }
+    ds->features[j++].index = -1;
+    ds->maxdim = max_index;
+    free(sum_pos);
+    free(sum_neg);
+    return 0;
 }
 
 /* Labeled CSV file (src/IOStructures.c:293-493): label first, the k-th value
