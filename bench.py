@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
-    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned", "linear_predict"])
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned", "linear_predict", "parse"])
     ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
@@ -999,6 +999,131 @@ def run_linear_predict(args):
 
 
 # ----------------------------------------------------------------------------
+# the libsvm reader on the device
+# ----------------------------------------------------------------------------
+PARSE = dict(n=1_000_000, seed=20240612)
+PARSE_DESC = ("libsvm reader: readTrainFile of a %d-row file of the learned-form workload's shape (32 dense features "
+              "written with 17 significant digits, labels +-1; %.0f MB of text): the device reader "
+              "(readTrainFileGPU: file read, both strtok passes and every strtod/strtol on the GPU, class-mean rows "
+              "on the host) against the host reader")
+
+
+def run_parse(args):
+    import numpy as np
+
+    from libirwls_gb300 import _abi, load, synth
+
+    path = os.path.join(tempfile.gettempdir(), "irwls_parse_%d.libsvm" % PARSE["n"])
+    X, y = synth.gauss_mixture(PARSE["n"], seed=PARSE["seed"])
+    synth.write_libsvm(path, synth.from_dense(X, y, keep_zeros=True))
+    with open(path, "rb") as f:
+        text = f.read()
+    mb = len(text) / 1e6
+    metric = "libsvm read s (%d rows, %.0f MB)" % (PARSE["n"], mb)
+    cfg = {"workload": PARSE_DESC % (PARSE["n"], mb), "rows": PARSE["n"], "features": 32, "bytes": len(text),
+           "form": "device reader", "parallelism": "single GPU", "l2": "the text (%.0f MB) exceeds L2" % mb}
+    lib = load()
+
+    def host_read():
+        t0 = time.perf_counter()
+        ds = lib.readTrainFile(path.encode())
+        return time.perf_counter() - t0, ds
+
+    if args.impl == "reference":
+        dt, ds = host_read()
+        lib.freeDataset(ds)
+        base = {"value": round(dt, 3), "unit": "s", "cores": 1, "kind": "port",
+                "sample": "the reference's reader restated (host C, single thread, strtok/strtod as the reference) "
+                          "on the whole file"}
+        print(json.dumps({"metric": metric, "value": base["value"], "unit": "s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": base["value"] * 1000,
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded generator)", "config": cfg, "cpu_baseline": base,
+                          "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        os.unlink(path)
+        return
+    if not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    lib.readTrainFileGPU.restype = _abi.SvmDataset
+    lib.readTrainFileGPU.argtypes = [C.c_char_p]
+    lib.irwls_parse_libsvm.restype = C.c_int
+    lib.irwls_parse_libsvm.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(_abi.SvmDataset)]
+
+    def dev_read():
+        lib.irwls_dev_sync()
+        h0, d0 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
+        t0 = time.perf_counter()
+        ds = lib.readTrainFileGPU(path.encode())
+        dt = time.perf_counter() - t0
+        h1, d1 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
+        return dt, ds, h1.value - h0.value, d1.value - d0.value
+
+    def same(a, b):
+        if (a.l, a.sparse, a.maxdim) != (b.l, b.sparse, b.maxdim):
+            return False
+        ra, ya, qa = _abi.dataset_rows(a, a.l + 2)
+        rb, yb, qb = _abi.dataset_rows(b, b.l + 2)
+        return (all(np.array_equal(i1, i2) and np.array_equal(v1.view(np.int64), v2.view(np.int64))
+                    for (i1, v1), (i2, v2) in zip(ra, rb))
+                and np.array_equal(ya.view(np.int64), yb.view(np.int64))
+                and np.array_equal(qa.view(np.int64), qb.view(np.int64)))
+
+    for _ in range(args.warmup):
+        _, ds, _, _ = dev_read()
+        lib.freeDataset(ds)
+    lib.irwls_profile_enable(1)
+    lib.irwls_profile_reset()
+    launches0 = lib.irwls_kernel_launches()
+    clocks = Clocks(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        lib.irwls_l2_flush(512 << 20)
+        dt, ds, h2d, d2h = dev_read()
+        times.append(dt)
+        last = ds
+    clk = clocks.stop()
+    launches = lib.irwls_kernel_launches() - launches0
+    k_s = profile_read(lib, 8, args.steps)[0]
+    lib.irwls_profile_enable(0)
+    mem_t0 = time.perf_counter()
+    ds_mem = _abi.SvmDataset()
+    rc = lib.irwls_parse_libsvm(text, len(text), C.byref(ds_mem))
+    mem_s = time.perf_counter() - mem_t0
+    value = statistics.mean(times)
+    host_s, host_ds = host_read() if not args.no_cpu else (None, None)
+    identical = bool(same(last, host_ds)) if host_ds is not None else None
+    peaks, peak_src = measured_peaks()
+    ach = len(text) / k_s / 1e9 if k_s > 0 else 0.0
+    line = {"metric": metric, "value": round(value, 3), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 1), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (exact decimal conversion)",
+            "data": "synthetic (seeded generator)", "config": cfg,
+            "e2e": {"value": round(value, 3), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "note": "from the file name to the host svm_dataset, file read included"},
+            "gpu_launches": int(launches // max(args.steps, 1)),
+            "roofline": {"bound": "issue (byte-serial tokenising, one thread per line)", "kernel": "pass1/pass2/sparse",
+                         "achieved": round(ach, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s of text",
+                         "frac": round(ach / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None,
+                         "traffic": None, "peak_source": peak_src, "kernel_s": round(k_s, 4)},
+            "cpu_baseline": None if host_s is None else {
+                "value": round(host_s, 3), "unit": "s", "cores": 1, "kind": "port",
+                "sample": "the reference's reader restated (host C readTrainFile, single thread) on the whole file"},
+            "clocks": clk, "in_memory_parse_s": round(mem_s, 3) if rc == 0 else None,
+            "identical_to_host_reader": identical}
+    print(json.dumps(line), flush=True)
+    lib.freeDataset(last)
+    if rc == 0:
+        lib.freeDataset(ds_mem)
+    if host_ds is not None:
+        lib.freeDataset(host_ds)
+    os.unlink(path)
+
+
+# ----------------------------------------------------------------------------
 # learned-proposal form of SGMA
 # ----------------------------------------------------------------------------
 LEARN = dict(n=1_000_000, n_test=20_000, gamma=0.5, C=10.0, trace_sets=10, trace_rows=20_000, pool=4096)
@@ -1152,6 +1277,8 @@ def main():
         run_learned(args)
     elif args.workload == "linear_predict":
         run_linear_predict(args)
+    elif args.workload == "parse":
+        run_parse(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

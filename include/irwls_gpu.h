@@ -89,7 +89,8 @@ void irwls_profile_enable(int on);
 void irwls_profile_reset(void);
 /* slot: 0 SGMA score GEMM, 1 Gram update, 2 kernel row sums, 3 Cholesky
  * solve, 4 prediction, 5 SGMA candidate rows and solves, 6 SGMA selection
- * and factor/column update, 7 digit slicing of the precision form's Gram.
+ * and factor/column update, 7 digit slicing of the precision form's Gram,
+ * 8 the device libsvm reader's kernels.
  * Total milliseconds and launches since the reset. */
 void irwls_profile_read(int slot, double *ms, long long *launches);
 /* Kernel launches issued by the library since it was loaded. */

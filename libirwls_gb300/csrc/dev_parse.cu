@@ -347,10 +347,14 @@ extern "C" int irwls_parse_libsvm(const char *buf, size_t len, svm_dataset *ds) 
         rc |= irwls_dev_h2d(d_err2, &err2, sizeof(long long));
     }
     if (!rc && n > 0) {
+        if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_PARSE);
         pass1_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, d_el, d_maxidx, d_err1);
+        irwls_count_launch(1);
         rc |= irwls_check_launch("pass1");
         pass2_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, nullptr, nullptr, nullptr, nullptr, d_cnt, nullptr,
                                                        d_err2);
+        if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_PARSE);
+        irwls_count_launch(1);
         rc |= irwls_check_launch("pass2 count");
         cnt.resize(n);
         rc |= irwls_dev_d2h(&elements, d_el, sizeof elements);
@@ -396,9 +400,13 @@ extern "C" int irwls_parse_libsvm(const char *buf, size_t len, svm_dataset *ds) 
     std::vector<int> rmax;
     int sparse = 0;
     if (!rc && n > 0) {
+        if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_PARSE);
         pass2_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, d_start, d_rows, d_y, d_q, d_cnt, d_rmax, d_err2);
+        irwls_count_launch(1);
         rc |= irwls_check_launch("pass2 rows");
         sparse_kernel<<<grid, 128, 0, irwls_stream()>>>(d_rows, d_start, n, d_sparse);
+        if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_PARSE);
+        irwls_count_launch(1);
         rc |= irwls_check_launch("sparse");
         h_rows = (svm_sample *)malloc((size_t)total * sizeof(svm_sample));
         y.resize(n);
@@ -487,7 +495,8 @@ extern "C" long long irwls_parse_doubles(const char *buf, size_t len, double *ou
         if (!rc) {
             parse_doubles_kernel<<<(int)std::min<long long>((n + 127) / 128, 32LL * sms), 128, 0, irwls_stream()>>>(
                 L, n, d_out, d_st);
-            rc |= irwls_check_launch("parse_doubles");
+            irwls_count_launch(1);
+        rc |= irwls_check_launch("parse_doubles");
             rc |= irwls_dev_d2h(out, d_out, n * sizeof(double));
             rc |= irwls_dev_d2h(status, d_st, n * sizeof(int));
             rc |= irwls_dev_sync();

@@ -248,7 +248,7 @@ void irwls_prof_read(int slot, double *ms, long long *launches);
 void irwls_prof_reset(void);
 enum { IRWLS_PROF_SGMA_GEMM = 0, IRWLS_PROF_GRAM = 1, IRWLS_PROF_ROWSUM = 2, IRWLS_PROF_CHOL = 3,
        IRWLS_PROF_PREDICT = 4, IRWLS_PROF_SGMA_CAND = 5, IRWLS_PROF_SGMA_UPDATE = 6, IRWLS_PROF_GRAM_SLICE = 7,
-       IRWLS_PROF_SLOTS = 8 };
+       IRWLS_PROF_PARSE = 8, IRWLS_PROF_SLOTS = 9 };
 long long irwls_launch_count(void);
 void irwls_count_launch(int n);
 
