@@ -603,46 +603,71 @@ __global__ void residual_kernel(const double *__restrict__ KSC, int l, int m, co
     }
 }
 
-__device__ int block_exclusive_scan(int *s, int v) {
-    const int t = threadIdx.x;
-    s[t] = v;
+// Active rows (Da != 0) in ascending order with sqrt(Da) and sqrt(Da) y
+// (src/budgeted-train.c:459-474), as an ordered compaction over blocks of WB
+// rows: weights_count_kernel counts each block's active rows; each block of
+// weights_write_kernel sums the counts before it and places its rows by
+// warp-ballot prefixes, round by round in row order.
+constexpr int WB = 2048;
+
+__device__ __forceinline__ int block_sum256(int v, int *ws) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
     __syncthreads();
-    for (int o = 1; o < CT; o <<= 1) {
-        int x = (t >= o) ? s[t - o] : 0;
-        __syncthreads();
-        s[t] += x;
-        __syncthreads();
-    }
-    const int incl = s[t];
-    const int total = s[CT - 1];
+    int t = 0;
+    for (int k = 0; k < 8; ++k) t += ws[k];
     __syncthreads();
-    s[t] = incl - v;
-    __syncthreads();
-    return total;
+    return t;
 }
 
-// Active rows (Da != 0) in ascending order with sqrt(Da) and sqrt(Da) y
-// (src/budgeted-train.c:459-474).
-__global__ void __launch_bounds__(CT) weights_kernel(const double *__restrict__ Da, const double *__restrict__ y,
-                                                     int l, int *act, double *sd, double *day, int *nact) {
-    __shared__ int s_scan[CT];
-    const int ch = (l + CT - 1) / CT;
-    const int b = threadIdx.x * ch, e = min(l, b + ch);
+__global__ void __launch_bounds__(256) weights_count_kernel(const double *__restrict__ Da, int l,
+                                                            int *__restrict__ cnt) {
+    __shared__ int ws[8];
+    const int r0 = blockIdx.x * WB, r1 = min(l, r0 + WB);
     int c = 0;
-    for (int i = b; i < e; ++i) c += (Da[i] != 0.0);
-    const int total = block_exclusive_scan(s_scan, c);
-    int off = s_scan[threadIdx.x];
-    for (int i = b; i < e; ++i) {
-        const double d = Da[i];
-        if (d != 0.0) {
-            act[off] = i;
-            const double r = sqrt(d);
-            sd[off] = r;
-            day[off] = __dmul_rn(r, y[i]);
-            ++off;
+    for (int i = r0 + threadIdx.x; i < r1; i += 256) c += Da[i] != 0.0;
+    const int t = block_sum256(c, ws);
+    if (threadIdx.x == 0) cnt[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(256) weights_write_kernel(const double *__restrict__ Da, const double *__restrict__ y,
+                                                            int l, const int *__restrict__ cnt, int nb,
+                                                            int *__restrict__ act, double *__restrict__ sd,
+                                                            double *__restrict__ day, int *__restrict__ nact) {
+    __shared__ int ws[8];
+    __shared__ int woff[8];
+    int part = 0;
+    for (int k = threadIdx.x; k < (int)blockIdx.x; k += 256) part += cnt[k];
+    int base = block_sum256(part, ws);
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) nact[0] = base + cnt[nb - 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = blockIdx.x * WB, r1 = min(l, r0 + WB);
+    for (int i0 = r0; i0 < r1; i0 += 256) {
+        const int i = i0 + threadIdx.x;
+        const double d = i < r1 ? Da[i] : 0.0;
+        const bool on = d != 0.0;
+        const unsigned bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) ws[warp] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int k = 0; k < 8; ++k) {
+                woff[k] = t;
+                t += ws[k];
+            }
+            ws[0] = t;  // this round's total, read below after the barrier
         }
+        __syncthreads();
+        if (on) {
+            const int pos = base + woff[warp] + __popc(bal & ((1u << lane) - 1u));
+            act[pos] = i;
+            const double r = sqrt(d);
+            sd[pos] = r;
+            day[pos] = __dmul_rn(r, y[i]);
+        }
+        base += ws[0];
+        __syncthreads();
     }
-    if (threadIdx.x == 0) nact[0] = total;
 }
 
 // First IRWLSpar pass: every row, unscaled, with Day = y M (src/budgeted-train.c:348-352).
@@ -852,8 +877,13 @@ extern "C" int irwls_par_residual(const double *d_KSC, int l, int m, const doubl
 
 extern "C" int irwls_par_weights(const double *d_Da, const double *d_y, int l, int *d_act, double *d_sd,
                                  double *d_day, int *d_nact) {
-    weights_kernel<<<1, CT, 0, irwls_stream()>>>(d_Da, d_y, l, d_act, d_sd, d_day, d_nact);
-    IRWLS_LAUNCH_CHECK("weights");
+    const int nb = std::max(1, ceil_div(l, WB));
+    int *cnt = (int *)irwls_ctx_scratch(2, (size_t)nb * sizeof(int));
+    if (!cnt) return -3;
+    weights_count_kernel<<<nb, 256, 0, irwls_stream()>>>(d_Da, l, cnt);
+    IRWLS_LAUNCH_CHECK("weights_count");
+    weights_write_kernel<<<nb, 256, 0, irwls_stream()>>>(d_Da, d_y, l, cnt, nb, d_act, d_sd, d_day, d_nact);
+    IRWLS_LAUNCH_CHECK("weights_write");
     return 0;
 }
 
