@@ -71,22 +71,25 @@ __global__ void __launch_bounds__(256) gram_colmax_kernel(const double *__restri
     const int c = blockIdx.x * 256 + threadIdx.x;
     if (c > m) return;
     const int p0 = blockIdx.y * GCM, p1 = min(nact, p0 + GCM);
-    double mx[8];
+    // |v| and the maximum on the bit patterns (integer operations): only the
+    // product itself uses the FP64 pipe
+    unsigned long long mx[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) mx[u] = 0.0;
+    for (int u = 0; u < 8; ++u) mx[u] = 0ULL;
     for (int p = p0; p < p1; p += 8) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const int pp = p + u;
             if (pp < p1) {
                 const double v = c < m ? __dmul_rn(sd[pp], KSC[(size_t)act[pp] * m + c]) : day[pp];
-                mx[u] = fmax(mx[u], fabs(v));
+                const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+                mx[u] = a > mx[u] ? a : mx[u];
             }
         }
     }
 #pragma unroll
-    for (int u = 1; u < 8; ++u) mx[0] = fmax(mx[0], mx[u]);
-    if (p1 > p0) atomicMax(cmax + c, (unsigned long long)__double_as_longlong(mx[0]));
+    for (int u = 1; u < 8; ++u) mx[0] = mx[u] > mx[0] ? mx[u] : mx[0];
+    if (p1 > p0) atomicMax(cmax + c, mx[0]);
 }
 
 // sigma_c = 2^e_c, the smallest power of two >= the column maximum (e = -1100:
