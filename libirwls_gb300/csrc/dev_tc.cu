@@ -720,9 +720,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
     __shared__ volatile int abort_flag;
     unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
     float *ca = (float *)(smem + NS * S::BYTES);
-    unsigned char *xs = (unsigned char *)(ca + 64 * X.ld);  // xs_bytes of staged tile rows
-    __shared__ int srp[TC_BM + 1];
-    __shared__ float sq[TC_BM];
+    // two buffers of xs_bytes: the rows of the tile being scored and of the next
+    unsigned char *xs = (unsigned char *)(ca + 64 * X.ld);
+    __shared__ int srp[2][TC_BM + 1];
+    __shared__ float sq[2][TC_BM];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntiles = (l + TC_BM - 1) / TC_BM;
     const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -808,11 +809,17 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
         // 32 g ... 32 g + 31 of epilogue group g
         const int ew = warp & 3, g = (warp - 4) >> 2;
         const int et = threadIdx.x - 128;
+        // the rows of tile j + 1 are copied in while tile j is scored
+        auto stage = [&](int jt) {
+            const int m0 = ((int)blockIdx.x + jt * (int)gridDim.x) * TC_BM;
+            return stage_tile_rows(X, m0, min(TC_BM, l - m0), xs + (jt & 1) * xs_bytes, xs_bytes, srp[jt & 1],
+                                   sq[jt & 1], et);
+        };
+        TileRows T = {};
+        if (my_tiles > 0) T = stage(0);
         for (int j = 0; j < my_tiles; ++j) {
             const int b = j & 1, tile = (int)blockIdx.x + j * (int)gridDim.x;
             const int m0 = tile * TC_BM, r = 32 * ew + lane, row = m0 + r;
-            // the tile's rows are copied in while its accumulator fills
-            const TileRows T = stage_tile_rows(X, m0, min(TC_BM, l - m0), xs, xs_bytes, srp, sq, et);
             const bool acc_ok = mbar_wait(smem_u32(&accf[b]), (uint32_t)(j / 2) & 1u);
             asm volatile("cp.async.wait_all;\n" ::);
             // one decision for all 256 epilogue threads (an OR over them), so
@@ -828,6 +835,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
                 abort_flag = 1;
                 break;
             }
+            // the other buffer was last read by tile j - 1, which every epilogue
+            // thread finished before the barriers that closed it
+            const TileRows Tn = j + 1 < my_tiles ? stage(j + 1) : T;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
             for (int c0 = 32 * g; c0 < 32 * g + 32; c0 += 8) {
                 float v[8], kv[8];
@@ -853,6 +863,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
                 part[(size_t)tile * 64 + et] = (w[0] + w[32]) + (w[64] + w[96]);
             }
             asm volatile("bar.sync 1, 256;\n" ::);
+            T = Tn;
         }
     }
     if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
@@ -1021,7 +1032,7 @@ extern "C" void irwls_f32_mirror_free(void *h) {
 
 extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qb,
                                    int ldq, const void *Wb, int s, float *d_part) {
-    constexpr size_t LIMIT = 220 * 1024, XS = 32 * 1024;
+    constexpr size_t LIMIT = 220 * 1024, XS = 24 * 1024;  // XS: one of the two row-staging buffers
     const int kst = (s + WS_BK - 1) / WS_BK;
     if (kst * WS_BK > ldq || ldq % WS_BK) {
         irwls_set_error(-12, "Q leading dimension %d does not hold order %d in 32-column blocks", ldq, s);
@@ -1034,10 +1045,10 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
         return -12;
     }
     // row staging when it leaves room for at least four ring stages
-    const size_t xs = fixed + XS + 4 * stage <= LIMIT ? XS : 0;
+    const size_t xs = fixed + 2 * XS + 4 * stage <= LIMIT ? XS : 0;
     int ns = 8;
-    while (ns > 2 && fixed + xs + (size_t)ns * stage > LIMIT) ns = ns == 8 ? 6 : ns - 2;
-    const size_t smem = fixed + xs + (size_t)ns * stage;
+    while (ns > 2 && fixed + 2 * xs + (size_t)ns * stage > LIMIT) ns = ns == 8 ? 6 : ns - 2;
+    const size_t smem = fixed + 2 * xs + (size_t)ns * stage;
     const int ntiles = ceil_div(l, TC_BM);
     const int grid = std::max(1, std::min(ntiles, irwls_num_sms() > 0 ? irwls_num_sms() : 148));
     const KViewF kv = kviewf(X, (const F32Mirror *)F);
