@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--budget", type=int, default=BUDGET)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
-    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned", "linear_predict", "parse"])
+    ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned", "linear_predict", "parse", "model_io"])
     ap.add_argument("--form", default="both", choices=["both", "plain", "mixed"],
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
@@ -1124,6 +1124,123 @@ def run_parse(args):
 
 
 # ----------------------------------------------------------------------------
+# models on the device: packing, the model file
+# ----------------------------------------------------------------------------
+MODEL_IO_DESC = ("model I/O: a full-IRWLS model of %d support vectors packed from the 200000-row budgeted workload "
+                 "(d=54 sparse; seeded weights, half of them zero), stored to a model file and read back: "
+                 "on the device (irwls_dmodel_full / _store / _read) against the host "
+                 "(calculateFULLModel / storeModel / readModel)")
+
+
+def run_model_io(args):
+    import numpy as np
+
+    from libirwls_gb300 import _abi, load
+
+    lib = load()
+    hd = workload(N_ROWS)
+    rng = np.random.default_rng(20240613)
+    beta = np.ascontiguousarray(np.where(rng.random(hd.l + 1) < 0.5, rng.standard_normal(hd.l + 1), 0.0))
+    nsv = int((beta[:-1] != 0).sum())
+    prop = _abi.make_properties(gamma=GAMMA, C_=COST, kernel=1)
+    metric = "model pack + store + read s (%d support vectors)" % nsv
+    cfg = {"workload": MODEL_IO_DESC % nsv, "support_vectors": nsv, "rows": hd.l, "form": "device model",
+           "parallelism": "single GPU", "l2": "the model (%.0f MB) exceeds L2" % (16 * (nsv + 13 * nsv) / 1e6)}
+    d = tempfile.mkdtemp()
+    path_h, path_d = os.path.join(d, "host.model"), os.path.join(d, "dev.model")
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+
+    def host_path():
+        t0 = time.perf_counter()
+        mdl = lib.calculateFULLModel(prop, hd.struct, beta.ctypes.data_as(PD))
+        fp = libc.fopen(path_h.encode(), b"wb")
+        lib.storeModel(C.byref(mdl), C.c_void_p(fp))
+        libc.fclose(C.c_void_p(fp))
+        m2 = _abi.Model()
+        fp = libc.fopen(path_h.encode(), b"rb")
+        lib.readModel(C.byref(m2), C.c_void_p(fp))
+        libc.fclose(C.c_void_p(fp))
+        dt = time.perf_counter() - t0
+        lib.freeModel(mdl)
+        lib.freeModel(m2)
+        return dt
+
+    if args.impl == "reference":
+        dt = host_path()
+        base = {"value": round(dt, 3), "unit": "s", "cores": 1, "kind": "port",
+                "sample": "the reference's model packing and model file I/O restated (host C, single thread)"}
+        print(json.dumps({"metric": metric, "value": base["value"], "unit": "s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": base["value"] * 1000,
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded generator)", "config": cfg, "cpu_baseline": base,
+                          "e2e": {"value": base["value"], "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    if not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    lib.irwls_dmodel_full.restype = C.c_void_p
+    lib.irwls_dmodel_full.argtypes = [C.c_void_p, _abi.Properties, PD]
+    lib.irwls_dmodel_read.restype = C.c_void_p
+    lib.irwls_dmodel_read.argtypes = [C.c_char_p]
+    lib.irwls_dmodel_store.argtypes = [C.c_void_p, C.c_char_p]
+    lib.irwls_dmodel_free.argtypes = [C.c_void_p]
+    res = lib.irwls_resident_upload(hd.struct, prop, 0)
+
+    def dev_path():
+        lib.irwls_dev_sync()
+        h0, d0 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h0), C.byref(d0))
+        t0 = time.perf_counter()
+        dm = lib.irwls_dmodel_full(res, prop, beta.ctypes.data_as(PD))
+        if not dm or lib.irwls_dmodel_store(dm, path_d.encode()) != 0:
+            raise SystemExit("device model failed: " + lib.irwls_last_error_message().decode())
+        dm2 = lib.irwls_dmodel_read(path_d.encode())
+        lib.irwls_dev_sync()
+        dt = time.perf_counter() - t0
+        h1, d1 = C.c_longlong(), C.c_longlong()
+        lib.irwls_transfer_bytes(C.byref(h1), C.byref(d1))
+        lib.irwls_dmodel_free(dm)
+        lib.irwls_dmodel_free(dm2)
+        return dt, h1.value - h0.value, d1.value - d0.value
+
+    for _ in range(args.warmup):
+        dev_path()
+    launches0 = lib.irwls_kernel_launches()
+    clocks = Clocks(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        dt, h2d, d2h = dev_path()
+        times.append(dt)
+    clk = clocks.stop()
+    launches = lib.irwls_kernel_launches() - launches0
+    host_s = host_path()
+    identical = open(path_h, "rb").read() == open(path_d, "rb").read()
+    value = statistics.mean(times)
+    line = {"metric": metric, "value": round(value, 4), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(value * 1000, 2), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": cfg,
+            "e2e": {"value": round(value, 4), "unit": "s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "note": "from the resident dataset and host weights to a file "
+                                                            "and back to a device model, file writes included"},
+            "gpu_launches": int(launches // max(args.steps, 1)),
+            "roofline": {"bound": "file I/O and host-device copies", "kernel": None, "achieved": None, "peak": None,
+                         "unit": None, "frac": None, "traffic": None},
+            "cpu_baseline": {"value": round(host_s, 4), "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "the reference's model packing and model file I/O restated (host C)"},
+            "clocks": clk, "model_file_bytes": os.path.getsize(path_d), "identical_model_files": bool(identical)}
+    print(json.dumps(line), flush=True)
+    lib.irwls_resident_free(res)
+    os.unlink(path_h)
+    os.unlink(path_d)
+    os.rmdir(d)
+
+
+# ----------------------------------------------------------------------------
 # learned-proposal form of SGMA
 # ----------------------------------------------------------------------------
 LEARN = dict(n=1_000_000, n_test=20_000, gamma=0.5, C=10.0, trace_sets=10, trace_rows=20_000, pool=4096)
@@ -1279,6 +1396,8 @@ def main():
         run_linear_predict(args)
     elif args.workload == "parse":
         run_parse(args)
+    elif args.workload == "model_io":
+        run_model_io(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

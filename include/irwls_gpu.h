@@ -76,6 +76,28 @@ int irwls_resident_budgeted(irwls_resident *r, properties props, int *centroids,
 /* Full IRWLS on a resident set; fills beta[l + 1]. 0 on success. */
 int irwls_resident_full(irwls_resident *r, properties props, double *beta);
 
+/* Models on the GPU (reference calculateFULLModel / calculateBudgetedModel,
+ * src/full-train.c:779-839, src/budgeted-train.c:519-570; storeModel /
+ * readModel, src/IOStructures.c:773-825): the support vectors are packed,
+ * read, stored and used for prediction on the device, without host
+ * svm_sample arrays. irwls_dmodel_full packs the rows with beta != 0 of a
+ * resident dataset (beta: l + 1 weights, the last one the bias),
+ * irwls_dmodel_budgeted the given centroids (the resident set needs its
+ * class-mean rows when a centroid is one of them); irwls_dmodel_store writes
+ * the bytes storeModel writes for the same model; irwls_dmodel_read reads
+ * that format; irwls_dmodel_predict is test (soft = 0) or softTest (soft = 1)
+ * with the device model, printing the accuracy line when props.Labels == 1.
+ * NULL / a nonzero return on an error (irwls_last_error_message). */
+typedef struct irwls_dmodel irwls_dmodel;
+irwls_dmodel *irwls_dmodel_full(const irwls_resident *r, properties props, const double *beta);
+irwls_dmodel *irwls_dmodel_budgeted(const irwls_resident *r, properties props, const int *centroids,
+                                    const double *weights);
+irwls_dmodel *irwls_dmodel_read(const char *path);
+int irwls_dmodel_store(const irwls_dmodel *m, const char *path);
+double *irwls_dmodel_predict(const irwls_dmodel *m, svm_dataset ds, predictProperties props, int soft);
+void irwls_dmodel_info(const irwls_dmodel *m, int *nSVs, int *nElem, double *bias);
+void irwls_dmodel_free(irwls_dmodel *m);
+
 /* Python-module dataset builders (reference python-package/pythonmodule.c):
  * dense row-major n x d doubles, every non-zero stored as feature j+1,
  * sparse = 1 when any value is non-zero (:213-263). The _with_means variant

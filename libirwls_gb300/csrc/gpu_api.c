@@ -34,6 +34,10 @@ irwls_resident *irwls_resident_upload(svm_dataset dataset, properties props, int
     return r;
 }
 
+/* The device rows and the host dataset of a resident set (dev_model.cu). */
+const irwls_dev_set *irwls_resident_devset(const irwls_resident *r) { return &r->X; }
+const svm_dataset *irwls_resident_dataset(const irwls_resident *r) { return &r->ds; }
+
 void irwls_resident_free(irwls_resident *r) {
     if (!r) return;
     irwls_dev_release(&r->X);
