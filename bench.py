@@ -1145,7 +1145,9 @@ def run_model_io(args):
     prop = _abi.make_properties(gamma=GAMMA, C_=COST, kernel=1)
     metric = "model pack + store + read s (%d support vectors)" % nsv
     cfg = {"workload": MODEL_IO_DESC % nsv, "support_vectors": nsv, "rows": hd.l, "form": "device model",
-           "parallelism": "single GPU", "l2": "the model (%.0f MB) exceeds L2" % (16 * (nsv + 13 * nsv) / 1e6)}
+           "parallelism": "single GPU",
+           "l2": "not flushed: the model (about %.0f MB) fits in L2, and the file writes dominate" %
+                 (16 * (nsv + 13 * nsv) / 1e6)}
     d = tempfile.mkdtemp()
     path_h, path_d = os.path.join(d, "host.model"), os.path.join(d, "dev.model")
     libc = C.CDLL(None)
