@@ -12,7 +12,8 @@ One step = one complete training (SGMA + IRWLSpar) of that workload. Both
 forms are timed in the same run, on the same resident dataset:
   plain FP64 : the reference's arithmetic, the form the parity tests pin;
   precision  : SGMA scores in split BF16 on the tensor cores, IRWLSpar's Gram
-               in double-float FP32 pairs, factors/solves/residuals in FP64.
+               from exact integer digit products on the tensor cores,
+               factors/solves/residuals in FP64.
   value : train seconds per step of the precision form when it meets the
           accuracy bars against the plain run of the same job (relative primal
           objective difference <= 1e-4, held-out accuracy change <= 0.1%),
@@ -21,9 +22,9 @@ forms are timed in the same run, on the same resident dataset:
   e2e   : the same form through the reference-facing C ABI (SGMA() +
           IRWLSpar() on the host svm_dataset), host-to-device copies of the
           dataset and device-to-host copies of the results included.
-  roofline: the dominant kernel of that form (double-float Gram: FP32-issue
-          bound at 12 instructions per product-sum, against a live FP32 FMA
-          probe; plain form: the FP64 SGMA GEMM against a live FP64 probe).
+  roofline: the dominant kernel of that form (tensor-core Gram: bf16 digit
+          products against the measured sustained bf16 peak; plain form: the
+          FP64 SGMA GEMM against a live FP64 probe).
   kernels : the other measured kernel rooflines of both forms.
   cpu_baseline: the CPU restatement of the reference (oracle/irwls_port.c,
           reference arithmetic and BLAS/LAPACK calls) on all host cores, on a

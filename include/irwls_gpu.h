@@ -188,7 +188,7 @@ void irwls_set_sgma_proposer(void *mlp, int pool);
  * precision-form SGMA run (RBF), or -1. */
 double irwls_last_nystrom_residual(void);
 /* FP32 FMA throughput of the device (TFLOP/s, one FMA = 2 flops), measured
- * the same way: the denominator of the precision form's double-float Gram. */
+ * the same way. */
 double irwls_fp32_peak_tflops(int reps);
 
 /* Cholesky factorization and solve of one system on the GPU that allocates

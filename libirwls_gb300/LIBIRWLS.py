@@ -125,8 +125,9 @@ def budgeted_train(data, labels, gamma=1.0, C=1.0, threads=1, size=10, algorithm
 
 def set_precision(mode):
     """Budgeted training's arithmetic for this process: "fp64" (the
-    reference's, the default) or "mixed" (tensor-core SGMA scores and a
-    double-float IRWLS Gram; same loops and random draws). Not part of the
+    reference's, the default) or "mixed" (tensor-core SGMA scores and an
+    IRWLS Gram from exact integer digit products on the tensor cores; same
+    loops and random draws). Not part of the
     reference module."""
     modes = {"fp64": 0, "mixed": 1}
     if mode not in modes:

@@ -546,8 +546,7 @@ __global__ void fp32_probe_kernel(float *out, int iters) {
 }  // namespace
 
 // FP32 FMA throughput in TFLOP/s (one FMA = 2 flops), best of `reps` timed
-// launches: the denominator of the double-float Gram, whose product-sum costs
-// twelve FP32 instructions.
+// launches: the FP32-issue ceiling reported beside the tensor-core kernels.
 extern "C" double irwls_fp32_peak_tflops(int reps) {
     if (irwls_dev_init()) return 0.0;
     const int blocks = 4 * g_num_sms, threads = 256, iters = 100000;

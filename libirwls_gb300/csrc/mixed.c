@@ -7,14 +7,15 @@
  *         Q w on the tensor cores in split BF16 (Q = K_nm L^-T, kept in FP32
  *         and as bf16 hi/lo), candidate kernel rows of the score epilogue in
  *         FP32.
- *   IRWLSpar (budgeted_train.c, irwls_par_dev) accumulates its Gram in
- *   double-float FP32 pairs; its factor, solves, residuals and convergence
- *   test stay FP64. Its system K1 = KC + K_nm^T D_a K_nm carries weights up
- *   to 1e4 against a 1e-5 jitter, so its condition number reaches ~1e13: a
- *   Gram accumulated from 16-bit-mantissa products (relative error ~1e-5)
- *   turns it indefinite (measured on 200000 rows and 1000 centroids, that
- *   variant's primal objective was off by a factor of 4e6), while the
- *   double-float Gram's ~1e-14 relative error keeps it definite.
+ *   IRWLSpar (budgeted_train.c, irwls_par_dev) forms its Gram on the tensor
+ *   cores from exact integer digits of its operand (dev_gram_tc.cu); its
+ *   factor, solves, residuals and convergence test stay FP64. Its system
+ *   K1 = KC + K_nm^T D_a K_nm carries weights up to 1e4 against a 1e-5
+ *   jitter, so its condition number reaches ~1e13: a Gram accumulated from
+ *   16-bit-mantissa products (relative error ~1e-5) turns it indefinite
+ *   (measured on 200000 rows and 1000 centroids, that variant's primal
+ *   objective was off by a factor of 4e6), while the digit products' error
+ *   (about 2^-45 of the column scales per row) keeps it definite.
  * Selected with irwls_set_precision(IRWLS_PRECISION_MIXED) or the
  * environment variable IRWLS_PRECISION=mixed; plain FP64 is the default.
  */

@@ -7,9 +7,10 @@ scores differ from the FP64 form by about 1e-5 relative, so it may pick a
 different centroid where two candidates score within that margin; on the
 seeded reference cases below every step's argmax agrees with the reference.
 
-IRWLSpar: the Gram K1 = KC + A'^T A' is accumulated in double-float (FP32
-pairs, about 48 significant bits) instead of FP64; the factor, solves,
-residual and convergence test stay FP64. Its weights therefore differ from
+IRWLSpar: the Gram K1 = KC + A'^T A' is formed on the tensor cores from
+exact integer digits of A' (48-bit fixed point per column, about 2^-45 of
+the column scales per row) instead of FP64; the factor, solves, residual and
+convergence test stay FP64. Its weights therefore differ from
 the reference's by the solve's sensitivity to that rounding; the bar is the
 objective the weights reach and the labels they predict."""
 import numpy as np
