@@ -599,7 +599,13 @@ __global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__re
 // leaves its loop (the epilogue warps decide together at their named
 // barrier), the MMA thread waits for its last commit and the producer for
 // its copies before the tensor memory is released.
-constexpr int WS_THREADS = 384, WS_BK = 32;
+constexpr int WS_BK = 32;
+// Epilogue groups: 2 (8 epilogue warps, 384 threads). Four groups (640
+// threads, 96 registers) were measured at 200000 rows: 4 % faster at order
+// 32, 3 % slower at orders 512-992, slower over a whole training -- the
+// epilogue is bound by shared-memory traffic (staged rows and candidate
+// gathers), which more warps do not reduce.
+constexpr int WS_EG = 2;
 
 __device__ __forceinline__ void cp_async4(uint32_t saddr, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(saddr), "l"(gmem));
@@ -624,7 +630,7 @@ struct TileRows {
 // Issues the staging copies of rows m0 ... m0 + nr - 1 (threads et = 0 ... 255
 // of the epilogue); the caller waits for them (cp.async.wait_all + barrier).
 __device__ __forceinline__ TileRows stage_tile_rows(const KViewF &X, int m0, int nr, unsigned char *buf, int buf_bytes,
-                                                    int *srp, float *sq, int et) {
+                                                    int *srp, float *sq, int et, int nthr) {
     TileRows t;
     t.kind = 0;
     t.lds = 0;
@@ -638,7 +644,7 @@ __device__ __forceinline__ TileRows stage_tile_rows(const KViewF &X, int m0, int
         if (nr * lds * 4 <= buf_bytes) {
             t.kind = 2;
             const int n = nr * X.width;
-            for (int k = et; k < n; k += 256) {
+            for (int k = et; k < n; k += nthr) {
                 const int r = k / X.width, c = k - r * X.width;
                 cp_async4(smem_u32(x + r * lds + c), X.X + (size_t)(m0 + r) * X.ld + c);
             }
@@ -651,12 +657,12 @@ __device__ __forceinline__ TileRows stage_tile_rows(const KViewF &X, int m0, int
     float *cv = (float *)(buf + (buf_bytes / 8) * 4);
     t.ci = ci;
     t.cv = cv;
-    for (int k = et; k <= nr; k += 256) srp[k] = X.rp[m0 + k] - p0;
+    for (int k = et; k <= nr; k += nthr) srp[k] = X.rp[m0 + k] - p0;
     if (X.mode == IRWLS_K_NORM_RBF)
-        for (int k = et; k < nr; k += 256) sq[k] = X.q[m0 + k];
+        for (int k = et; k < nr; k += nthr) sq[k] = X.q[m0 + k];
     if (nnz <= buf_bytes / 8) {
         t.kind = 1;
-        for (int k = et; k < nnz; k += 256) {
+        for (int k = et; k < nnz; k += nthr) {
             cp_async4(smem_u32(ci + k), X.ci + p0 + k);
             cp_async4(smem_u32(cv + k), X.cv + p0 + k);
         }
@@ -706,8 +712,10 @@ __device__ __forceinline__ void kentry8_tile(const KViewF &B, const TileRows &T,
     for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
 }
 
-template <int NS>
-__global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
+// EG epilogue groups of four warps (warps 4 ... 4 EG + 3), each scoring 64 / EG
+// of the candidates for all 128 rows of a tile.
+template <int NS, int EG>
+__global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     KViewF X, int l, const int *__restrict__ cand, const __nv_bfloat16 *__restrict__ Qb, int kbn,
     const __nv_bfloat16 *__restrict__ Wb, int kst, float *__restrict__ part, int xs_bytes, int *flags) {
     using S = TcRing<64, 2, WS_BK>;
@@ -716,7 +724,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
     __shared__ __align__(8) uint64_t full[NS], empty[NS], accf[2], acce[2], done;
     __shared__ uint32_t tmem_slot;
     __shared__ float qc[64];
-    __shared__ float wred[8][32];
+    constexpr int EPI = 128 * EG, CPG = 64 / EG;  // epilogue threads, candidates per group
+    __shared__ float wred[4 * EG][CPG];
     __shared__ volatile int abort_flag;
     unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
     float *ca = (float *)(smem + NS * S::BYTES);
@@ -734,13 +743,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&accf[b], 1);
-            mbar_init(&acce[b], 8);
+            mbar_init(&acce[b], 4 * EG);
         }
         mbar_init(&done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
         abort_flag = 0;
     }
-    for (int t = threadIdx.x; t < 64 * X.ld; t += WS_THREADS) {
+    for (int t = threadIdx.x; t < 64 * X.ld; t += blockDim.x) {
         const int c = t / X.ld, k = t % X.ld;
         ca[t] = X.X[(size_t)cand[c] * X.ld + k];
     }
@@ -813,7 +822,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
         auto stage = [&](int jt) {
             const int m0 = ((int)blockIdx.x + jt * (int)gridDim.x) * TC_BM;
             return stage_tile_rows(X, m0, min(TC_BM, l - m0), xs + (jt & 1) * xs_bytes, xs_bytes, srp[jt & 1],
-                                   sq[jt & 1], et);
+                                   sq[jt & 1], et, EPI);
         };
         TileRows T = {};
         if (my_tiles > 0) T = stage(0);
@@ -822,15 +831,15 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
             const int m0 = tile * TC_BM, r = 32 * ew + lane, row = m0 + r;
             const bool acc_ok = mbar_wait(smem_u32(&accf[b]), (uint32_t)(j / 2) & 1u);
             asm volatile("cp.async.wait_all;\n" ::);
-            // one decision for all 256 epilogue threads (an OR over them), so
+            // one decision for all epilogue threads (an OR over them), so
             // that none is left at a named barrier that the others skip; the
             // barrier also publishes the staged rows
             const int bad = (!acc_ok || abort_flag) ? 1 : 0;
             int any;
             asm volatile(
-                "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, 1, 256, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+                "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, 1, %2, p;\nselp.s32 %0, 1, 0, q;\n}\n"
                 : "=r"(any)
-                : "r"(bad));
+                : "r"(bad), "r"(EPI));
             if (any) {
                 abort_flag = 1;
                 break;
@@ -839,7 +848,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
             // thread finished before the barriers that closed it
             const TileRows Tn = j + 1 < my_tiles ? stage(j + 1) : T;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-            for (int c0 = 32 * g; c0 < 32 * g + 32; c0 += 8) {
+            for (int c0 = CPG * g; c0 < CPG * g + CPG; c0 += 8) {
                 float v[8], kv[8];
                 tc_ld8_lanes(tmem + b * 64, 32 * ew, c0, v);
                 if (row < l) kentry8_tile(X, T, ca + (size_t)c0 * X.ld, X.ld, qc + c0, r, row, kv);
@@ -852,17 +861,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1) sgma_tc_score_ws_kernel(
                     }
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-                    if (lane == 0) wred[4 * g + ew][c0 - 32 * g + jj] = r2;
+                    if (lane == 0) wred[4 * g + ew][c0 - CPG * g + jj] = r2;
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
             if (lane == 0) mbar_arrive(&acce[b]);  // this warp's reads of accumulator b are done
-            asm volatile("bar.sync 1, 256;\n" ::);
+            asm volatile("bar.sync 1, %0;\n" ::"r"(EPI));
             if (et < 64) {
-                const float *w = &wred[4 * (et >> 5)][et & 31];
-                part[(size_t)tile * 64 + et] = (w[0] + w[32]) + (w[64] + w[96]);
+                // the candidate's four row-quarter sums, in a fixed order
+                const float *w = &wred[4 * (et / CPG)][et % CPG];
+                part[(size_t)tile * 64 + et] = (w[0] + w[CPG]) + (w[2 * CPG] + w[3 * CPG]);
             }
-            asm volatile("bar.sync 1, 256;\n" ::);
+            asm volatile("bar.sync 1, %0;\n" ::"r"(EPI));
             T = Tn;
         }
     }
@@ -1055,15 +1065,15 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
     const __nv_bfloat16 *qb = (const __nv_bfloat16 *)Qb, *wb = (const __nv_bfloat16 *)Wb;
     auto launch = [&](auto kern) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kern<<<grid, WS_THREADS, smem, irwls_stream()>>>(kv, l, d_cand, qb, ldq / 32, wb, kst, d_part, (int)xs,
-                                                         irwls_dev_flags());
+        kern<<<grid, 128 + 128 * WS_EG, smem, irwls_stream()>>>(kv, l, d_cand, qb, ldq / 32, wb, kst, d_part,
+                                                                (int)xs, irwls_dev_flags());
     };
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
     switch (ns) {
-        case 8: launch(sgma_tc_score_ws_kernel<8>); break;
-        case 6: launch(sgma_tc_score_ws_kernel<6>); break;
-        case 4: launch(sgma_tc_score_ws_kernel<4>); break;
-        default: launch(sgma_tc_score_ws_kernel<2>); break;
+        case 8: launch(sgma_tc_score_ws_kernel<8, WS_EG>); break;
+        case 6: launch(sgma_tc_score_ws_kernel<6, WS_EG>); break;
+        case 4: launch(sgma_tc_score_ws_kernel<4, WS_EG>); break;
+        default: launch(sgma_tc_score_ws_kernel<2, WS_EG>); break;
     }
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_GEMM);
     IRWLS_LAUNCH_CHECK("sgma_tc_score");
