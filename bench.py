@@ -480,7 +480,16 @@ def run_ours(args):
     # roofline: the dominant kernel of the headline form
     if head == 1:
         k = kernels["gram_tc_kernel (precision form, exact base-64 digit products on tcgen05)"]
-        roofline = dict(k, kernel="gram_tc_kernel", traffic=None)
+        # DRAM traffic of one launch from a full-size, one-pass ncu capture (the
+        # last IRWLSpar iteration of this workload, 62357 active rows):
+        # profiles/gram_tc_kernel_50k_m300.md; its algorithmic bytes are the digit
+        # slices read once (62368 padded rows x 1024 columns x 8 digits x 2 B)
+        # plus the FP64 partials
+        roofline = dict(k, kernel="gram_tc_kernel", traffic=1022239488 + 3406592,
+                        traffic_launch={"launch": "last of 42 (active rows 62357)", "duration_ms": 2.495,
+                                        "algorithmic_bytes": 62368 * 1024 * 16 + 2 * 4004000,
+                                        "source": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,"
+                                                  "gpu__time_duration.sum (one pass)"})
     else:
         k = kernels["sgma_gemm_kernel (plain FP64)"]
         roofline = dict(k, kernel="sgma_gemm_kernel", traffic=None,
