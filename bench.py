@@ -482,7 +482,7 @@ def run_ours(args):
         k = kernels["gram_tc_kernel (precision form, exact base-64 digit products on tcgen05)"]
         # DRAM traffic of one launch from a full-size, one-pass ncu capture (the
         # last IRWLSpar iteration of this workload, 62357 active rows):
-        # profiles/gram_tc_kernel_50k_m300.md; its algorithmic bytes are the digit
+        # profiles/gram_tc_kernel_200k_m1000_traffic.md; its algorithmic bytes are the digit
         # slices read once (62368 padded rows x 1024 columns x 8 digits x 2 B)
         # plus the FP64 partials
         roofline = dict(k, kernel="gram_tc_kernel", traffic=1022239488 + 3406592,
