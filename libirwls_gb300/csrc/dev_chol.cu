@@ -18,6 +18,8 @@
 // one launch applies the rank-32 update to the lower trailing matrix.
 #include <math.h>
 
+#include <cooperative_groups.h>
+
 #include "dev_common.cuh"
 
 namespace {
@@ -228,6 +230,64 @@ __global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
 
 // Enqueues the whole factorization (and the solve when has_b) on `st`, with
 // Dinv holding ceil(n/32) blocks of 32x32 doubles.
+// The same backward sweep on several CTAs (a cooperative launch): thread t
+// of CTA k owns row 256 k + t of z, which is row n of M updated in place.
+// Per 32-row block from the bottom, every CTA forms x_b = D_b^-T y_b in
+// shared memory from the block's rows of z (final since the previous block),
+// CTA 0 stores it, and the owners of the rows above subtract L_b^T x_b; every
+// value takes the single-CTA sweep's FMAs in the same order, so the results
+// are the same bits. A grid barrier closes each block.
+__global__ void __launch_bounds__(256) chol_backsolve_coop_kernel(double *__restrict__ M, int n, int ld,
+                                                                  const double *__restrict__ Dinv,
+                                                                  double *__restrict__ x) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    __shared__ double Di[NB][NB + 1];
+    __shared__ double yb[NB];
+    __shared__ double xb[NB];
+    const int tid = threadIdx.x;
+    const int r = blockIdx.x * blockDim.x + tid;
+    double *z = M + n;  // z[c] at z[c * ld]
+    const int nblk = (n + NB - 1) / NB;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int r0 = b * NB, r1 = min(n, r0 + NB);
+        for (int t = tid; t < NB * NB; t += blockDim.x) Di[t / NB][t % NB] = Dinv[(size_t)b * NB * NB + t];
+        if (tid < NB) yb[tid] = (r0 + tid < r1) ? z[(size_t)(r0 + tid) * ld] : 0.0;
+        __syncthreads();
+        if (tid < r1 - r0) {
+            double v = 0.0;
+            for (int c = tid; c < r1 - r0; ++c) v = fma(Di[c][tid], yb[c], v);
+            xb[tid] = v;
+            if (blockIdx.x == 0) x[r0 + tid] = v;
+        }
+        __syncthreads();
+        if (r < r0) {
+            double v = z[(size_t)r * ld];
+            const double *col = M + (size_t)r * ld;
+#pragma unroll 8
+            for (int c = r0; c < r1; ++c) v = fma(-col[c], xb[c - r0], v);
+            z[(size_t)r * ld] = v;
+        }
+        grid.sync();
+    }
+}
+
+// CTAs of the cooperative sweep for order n, or 0 when they cannot all be
+// resident at once (the single-CTA sweep is used then).
+int coop_backsolve_ctas(int n) {
+    static int cap = -1;
+    if (cap < 0) {
+        int dev = 0, coop = 0, per_sm = 0;
+        cap = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_backsolve_coop_kernel, 256, 0) == cudaSuccess)
+            cap = per_sm * (irwls_num_sms() > 0 ? irwls_num_sms() : 0);
+        cudaGetLastError();
+    }
+    const int g = (n + 255) / 256;
+    return g <= cap ? g : 0;
+}
+
 int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Dinv, cudaStream_t st) {
     const int has_b = d_x != nullptr;
     const int nrows = n + has_b;
@@ -248,6 +308,18 @@ int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Di
         }
     }
     if (has_b) {
+        const int g = coop_backsolve_ctas(n);
+        if (g > 0) {
+            void *args[] = {&d_M, &n, &ld, &Dinv, &d_x};
+            const cudaError_t e = cudaLaunchCooperativeKernel((const void *)chol_backsolve_coop_kernel, dim3(g),
+                                                              dim3(256), args, 0, st);
+            if (e != cudaSuccess) {
+                irwls_set_error(-2, "CUDA error in chol_backsolve (cooperative): %s", cudaGetErrorString(e));
+                return -2;
+            }
+            irwls_count_launch(1);
+            return 0;
+        }
         const size_t smem = (size_t)n * sizeof(double);
         if (smem > 48 * 1024) {
             if (smem > 160 * 1024) {
