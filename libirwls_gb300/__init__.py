@@ -55,6 +55,16 @@ def load() -> C.CDLL:
         "irwls_gram_tc_flops": (C.c_double, [C.c_int]),
         "irwls_set_linear_fast_path": (None, [C.c_int]),
         "irwls_get_linear_fast_path": (C.c_int, []),
+        "irwls_parse_libsvm": (C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(_abi.SvmDataset)]),
+        "readTrainFileGPU": (_abi.SvmDataset, [C.c_char_p]),
+        "irwls_parse_doubles": (C.c_longlong, [C.c_char_p, C.c_size_t, PD, PI, C.c_longlong]),
+        "irwls_dmodel_full": (C.c_void_p, [C.c_void_p, _abi.Properties, PD]),
+        "irwls_dmodel_budgeted": (C.c_void_p, [C.c_void_p, _abi.Properties, PI, PD]),
+        "irwls_dmodel_read": (C.c_void_p, [C.c_char_p]),
+        "irwls_dmodel_store": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "irwls_dmodel_predict": (PD, [C.c_void_p, _abi.SvmDataset, _abi.PredictProperties, C.c_int]),
+        "irwls_dmodel_info": (None, [C.c_void_p, PI, PI, PD]),
+        "irwls_dmodel_free": (None, [C.c_void_p]),
         "irwls_full_train_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
         "irwls_budgeted_train_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                                  C.c_void_p]),
