@@ -10,6 +10,12 @@ A' = [sd * KSC[act, :], day], from exact base-64 integer digits.
   FP64 product: |G - G_ref|_ij <= 2^-40 sigma_i sigma_j sqrt(nact), sigma the
   column scales (the dropped digit levels weigh 2^-45 sigma_i sigma_j per row
   and carry random signs).
+- Bit for bit on real-valued data: every step of the kernel is exact or
+  correctly rounded, so K1 must equal the host model of its arithmetic
+  (tests/gram_digits.py) -- RBF-like columns with weights over six decades;
+  and columns that hit the edge cases: ties of the fixed-point rounding, a
+  power-of-two and a just-above maximum, a zero column, subnormal entries,
+  tiny columns, and a constant column whose integer sum passes 2^63.
 - No active rows: K1 = KC.
 """
 import ctypes as C
@@ -17,6 +23,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import gram_digits as gd
 from libirwls_gb300 import load
 
 pytestmark = pytest.mark.gpu
@@ -132,3 +139,46 @@ def test_gram_tc_no_active_rows():
     low = _lower(G[:m])
     assert np.array_equal(G[:m][low], KC[low])
     assert np.all(G[m] == 0.0)
+
+
+def _rbf_case(rng):
+    l, m, nact = 6000, 300, 5200
+    X = rng.standard_normal((l, 12))
+    Cn = X[rng.choice(l, m, replace=False)]
+    KSC = np.exp(-0.1 * ((X[:, None, :] - Cn[None, :, :]) ** 2).sum(-1))
+    act = np.sort(rng.choice(l, nact, replace=False))
+    sd = 10.0 ** rng.uniform(-3, 3, nact)
+    day = rng.standard_normal(nact) * sd
+    KC = np.exp(-0.1 * ((Cn[:, None, :] - Cn[None, :, :]) ** 2).sum(-1))
+    return KSC, act, sd, day, KC
+
+
+def _edge_case(rng):
+    l, m, nact = 3000, 129, 2500
+    act = np.sort(rng.choice(l, nact, replace=False))
+    KSC = rng.uniform(-1, 1, (l, m))
+    KSC[:, 0] = 1.0                                          # constant: T(0, 0) = 2500 * 2^52 > 2^63
+    KSC[:, 1] = (2 * rng.integers(-2 ** 20, 2 ** 20, l) + 1) * 2.0 ** -49  # ties at sigma = 1/2
+    KSC[act[0], 1] = 0.5                                     # power-of-two maximum
+    KSC[:, 2] = 0.0                                          # zero column
+    KSC[:, 3] *= 2.0 ** -200                                 # tiny column
+    KSC[::7, 3] = 1e-310                                     # subnormal entries
+    KSC[:, 4] = np.clip(KSC[:, 4], -0.5, 0.5)
+    KSC[act[5], 4] = np.nextafter(0.5, 1.0)                  # maximum just above a power of two
+    sd = np.ones(nact)
+    day = rng.standard_normal(nact)
+    KC = rng.standard_normal((m, m))
+    return KSC, act, sd, day, KC
+
+
+@pytest.mark.parametrize("P", [1, 4])
+@pytest.mark.parametrize("make", [_rbf_case, _edge_case])
+def test_gram_tc_bit_exact_against_host_model(make, P):
+    KSC, act, sd, day, KC = make(np.random.default_rng(11))
+    G = _gram(KSC, act, sd, day, KC, P)
+    # the split-K chunks: the same on any part with at least P x tiles SMs
+    ref = gd.gram(KSC, act, sd, day, KC, P, 1 << 30)
+    low = _lower(G)
+    assert np.array_equal(np.isnan(ref), ~low)
+    assert np.array_equal(G[low].view(np.int64), ref[low].view(np.int64)), int(
+        np.sum(G[low].view(np.int64) != ref[low].view(np.int64)))

@@ -1,0 +1,81 @@
+"""The host model of the tensor-core Gram's arithmetic (tests/gram_digits.py),
+checked on the CPU before it is used to pin the kernel bit for bit:
+
+- the balanced base-64 digits rebuild N exactly and stay within +-33, so every
+  digit product is exact in bf16 and a 1024-row level sum stays below 2^24;
+- the fixed-point conversion rounds ties away from zero and drops subnormals;
+- on integer columns below 2^20 the model is the exact integer product;
+- on RBF-like columns with weights over six decades it is within the stated
+  bound of the FP64 product, and the split-K chunking does not change it by
+  more than the final roundings.
+"""
+import numpy as np
+
+import gram_digits as gd
+
+BIG = 1 << 30  # SM count: any part with at least P x tiles SMs chunks alike
+
+
+def test_digits_rebuild_and_range():
+    rng = np.random.default_rng(1)
+    N = rng.integers(-(1 << 47), (1 << 47) + 1, size=20000)
+    N[:4] = [1 << 47, -(1 << 47), (1 << 47) - 1, 0]
+    d = gd.digits(N)
+    back = sum(d[s] * (np.int64(64) ** s) for s in range(gd.GS))
+    assert np.array_equal(back, N)
+    for s in range(gd.GS - 1):
+        assert d[s].min() >= -32 and d[s].max() <= 31
+    assert np.abs(d[gd.GS - 1]).max() <= 33
+    # a level over 1024 rows: at most 8 pairs of products <= 33^2
+    assert 8 * 1024 * 33 * 33 < 1 << 24
+
+
+def test_fixed47_rounding():
+    e = 0
+    q = 2.0 ** -48  # half a unit of the 47-bit fixed point at sigma = 1
+    v = np.array([3 * q, -3 * q, 5 * q, -5 * q, q, 1.0, -1.0, 0.0, 1e-310, 2.0 ** -47])
+    assert list(gd.fixed47(v, e)) == [2, -2, 3, -3, 1, 1 << 47, -(1 << 47), 0, 0, 1]
+    assert list(gd.fixed47(v, None)) == [0] * len(v)
+
+
+def test_column_exponents():
+    A = np.array([[0.5, 0.0, -0.75, 1e-310, 3.0], [-0.25, 0.0, 0.1, 0.0, -4.0]])
+    assert gd.column_exponents(A) == [-1, None, 0, None, 2]
+
+
+def test_model_is_exact_on_integers():
+    rng = np.random.default_rng(2)
+    l, m, nact = 900, 70, 700
+    KSC = rng.integers(-(1 << 20), 1 << 20, size=(l, m)).astype(np.float64)
+    act = np.sort(rng.choice(l, nact, replace=False))
+    day = rng.integers(-(1 << 20), 1 << 20, size=nact).astype(np.float64)
+    KC = rng.integers(-1000, 1000, size=(m, m)).astype(np.float64)
+    G = gd.gram(KSC, act, np.ones(nact), day, KC, 3, BIG)
+    A = np.concatenate([KSC[act].astype(np.int64), day.astype(np.int64)[:, None]], axis=1)
+    ref = (A.T @ A)[:, :m].astype(np.float64)
+    ref[:m] += KC
+    low = ~np.isnan(G)
+    assert np.array_equal(G[low], ref[low])
+
+
+def test_model_accuracy_and_chunking():
+    rng = np.random.default_rng(3)
+    l, m, nact = 1500, 90, 1300
+    X = rng.standard_normal((l, 6))
+    Cn = X[rng.choice(l, m, replace=False)]
+    KSC = np.exp(-0.2 * ((X[:, None, :] - Cn[None, :, :]) ** 2).sum(-1))
+    act = np.sort(rng.choice(l, nact, replace=False))
+    sd = 10.0 ** rng.uniform(-3, 3, nact)
+    day = rng.standard_normal(nact) * sd
+    KC = np.zeros((m, m))
+    G1 = gd.gram(KSC, act, sd, day, KC, 1, BIG)
+    G4 = gd.gram(KSC, act, sd, day, KC, 4, BIG)
+    assert gd.chunking(nact, m, 4, BIG)[0] == 4
+    A = gd.column_values(KSC, act, sd, day)
+    ref = (A.T @ A)[:, :m]
+    sig = 2.0 ** np.ceil(np.log2(np.abs(A).max(0)))
+    bound = 2.0 ** -40 * np.outer(sig, sig[:m]) * np.sqrt(nact)
+    low = ~np.isnan(G1)
+    assert np.all(np.abs(G1 - ref)[low] <= bound[low])
+    # the chunks differ from one sum only by the roundings of the partials
+    assert np.all(np.abs(G4 - G1)[low] <= 4 * 2.0 ** -52 * np.abs(ref)[low] + bound[low] * 2.0 ** -10)
