@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rows", type=int, default=N_ROWS)
     ap.add_argument("--budget", type=int, default=BUDGET)
+    ap.add_argument("--parse-rows", type=int, default=None,
+                    help="rows of the parse workload's file (default 1000000; smaller only for profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
     ap.add_argument("--workload", default="budgeted", choices=["budgeted", "full", "full784", "batch", "learned", "linear_predict", "parse", "model_io"])
@@ -1023,16 +1025,19 @@ def run_parse(args):
 
     from libirwls_gb300 import _abi, load, synth
 
-    path = os.path.join(tempfile.gettempdir(), "irwls_parse_%d.libsvm" % PARSE["n"])
-    X, y = synth.gauss_mixture(PARSE["n"], seed=PARSE["seed"])
+    lib = load()
+    if args.impl != "reference" and not lib.irwls_gpu_available():
+        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
+    n = args.parse_rows or PARSE["n"]
+    path = os.path.join(tempfile.gettempdir(), "irwls_parse_%d.libsvm" % n)
+    X, y = synth.gauss_mixture(n, seed=PARSE["seed"])
     synth.write_libsvm(path, synth.from_dense(X, y, keep_zeros=True))
     with open(path, "rb") as f:
         text = f.read()
     mb = len(text) / 1e6
-    metric = "libsvm read s (%d rows, %.0f MB)" % (PARSE["n"], mb)
-    cfg = {"workload": PARSE_DESC % (PARSE["n"], mb), "rows": PARSE["n"], "features": 32, "bytes": len(text),
+    metric = "libsvm read s (%d rows, %.0f MB)" % (n, mb)
+    cfg = {"workload": PARSE_DESC % (n, mb), "rows": n, "features": 32, "bytes": len(text),
            "form": "device reader", "parallelism": "single GPU", "l2": "the text (%.0f MB) exceeds L2" % mb}
-    lib = load()
 
     def host_read():
         t0 = time.perf_counter()
@@ -1053,8 +1058,6 @@ def run_parse(args):
                                   "d2h_bytes_per_step": 0}}), flush=True)
         os.unlink(path)
         return
-    if not lib.irwls_gpu_available():
-        raise SystemExit("no CUDA device: " + lib.irwls_last_error_message().decode())
     lib.readTrainFileGPU.restype = _abi.SvmDataset
     lib.readTrainFileGPU.argtypes = [C.c_char_p]
     lib.irwls_parse_libsvm.restype = C.c_int

@@ -40,9 +40,11 @@
 #include "irwls_gpu.h"
 #include "numparse.cuh"
 
-extern "C" int irwls_dataset_assemble(svm_dataset *ds, int l, long long pass1_elements, int maxidx, int max_index,
-                                      int sparse, const svm_sample *rows, long long row_entries,
-                                      const long long *row_start, const double *y, const double *q);
+extern "C" int irwls_dataset_alloc(svm_dataset *ds, int l, long long pass1_elements, int maxidx,
+                                   long long row_entries);
+extern "C" int irwls_dataset_finish(svm_dataset *ds, int l, int maxidx, int max_index, int sparse,
+                                    long long row_entries, const long long *row_start, const double *y,
+                                    const double *q);
 
 namespace {
 
@@ -136,15 +138,17 @@ __device__ __forceinline__ void line_range(const LineSet &L, long long i, long l
 }
 
 // Pass 1 of the reference (elements and the largest index) and the line
-// length check.
+// length check. lcnt[i] = the line's index:value tokens, the slot that pass 2
+// writes the line's entries into (pass 2 checks that the counts agree).
 __global__ void pass1_kernel(LineSet L, long long nlines, unsigned long long *__restrict__ elements,
-                             int *__restrict__ maxidx, int *__restrict__ err) {
+                             int *__restrict__ maxidx, int *__restrict__ err, int *__restrict__ lcnt) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nlines;
          i += (long long)gridDim.x * blockDim.x) {
         long long ls, le0;
         line_range(L, i, ls, le0);
         if (le0 - ls > LINE_CHARS) {
             atomicMin(err, -3);  // the reference would split the line into several rows
+            lcnt[i] = 0;
             continue;
         }
         const char *b = L.b + ls;
@@ -164,15 +168,21 @@ __global__ void pass1_kernel(LineSet L, long long nlines, unsigned long long *__
         }
         atomicAdd(elements, el);
         atomicMax(maxidx, mx);
+        lcnt[i] = (int)min(el - 1, (unsigned long long)LINE_CHARS);
     }
 }
 
 // Pass 2 of the reference: the checks, the entry count per line, and (when
 // rows != null) the entries, the label, the row norm and the row's largest
 // index. err: the first failing line * 4 + kind (1 format, 2 unsupported).
+// Line i's entries and terminator go to the slot [row_start[i],
+// row_start[i + 1]); writes stay inside it, and a line whose entry count is
+// not the slot's sets *mismatch (the rows are then laid out again from this
+// pass's counts).
 __global__ void pass2_kernel(LineSet L, long long nlines, const long long *__restrict__ row_start,
                              svm_sample *__restrict__ rows, double *__restrict__ y, double *__restrict__ q,
-                             int *__restrict__ cnt, int *__restrict__ rmax, long long *__restrict__ err) {
+                             int *__restrict__ cnt, int *__restrict__ rmax, long long *__restrict__ err,
+                             int *__restrict__ mismatch) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nlines;
          i += (long long)gridDim.x * blockDim.x) {
         long long ls, le0;
@@ -192,6 +202,7 @@ __global__ void pass2_kernel(LineSet L, long long nlines, const long long *__res
         int n = 0, row_max = -1;
         double qq = 0.0;
         const long long base = rows ? row_start[i] : 0;
+        const int cap = rows ? (int)(row_start[i + 1] - base - 1) : 0;
         while (!kind) {
             const bool hi = next_tok(b, pos, le, D_COLON, is, ie);
             if (!next_tok(b, pos, le, D_SPTAB, ts, te)) break;
@@ -214,7 +225,7 @@ __global__ void pass2_kernel(LineSet L, long long nlines, const long long *__res
                 break;
             }
             qq = __dadd_rn(qq, __dmul_rn(v, v));
-            if (rows) {
+            if (rows && n < cap) {
                 rows[base + n].index = k;
                 rows[base + n].value = v;
             }
@@ -226,8 +237,9 @@ __global__ void pass2_kernel(LineSet L, long long nlines, const long long *__res
         }
         cnt[i] = n;
         if (rows) {
-            rows[base + n].index = -1;
-            rows[base + n].value = 0.0;
+            if (n != cap) atomicExch(mismatch, 1);
+            rows[base + min(n, cap)].index = -1;
+            rows[base + min(n, cap)].value = 0.0;
             y[i] = label;
             q[i] = qq;
             rmax[i] = row_max;
@@ -321,6 +333,7 @@ extern "C" int irwls_parse_libsvm(const char *buf, size_t len, svm_dataset *ds) 
     long long *d_nl = nullptr, *d_start = nullptr;
     unsigned long long *d_el = nullptr;
     int *d_maxidx = nullptr, *d_err1 = nullptr, *d_cnt = nullptr, *d_rmax = nullptr, *d_sparse = nullptr;
+    int *d_mis = nullptr;
     long long *d_err2 = nullptr;
     svm_sample *d_rows = nullptr;
     double *d_y = nullptr, *d_q = nullptr;
@@ -348,25 +361,76 @@ extern "C" int irwls_parse_libsvm(const char *buf, size_t len, svm_dataset *ds) 
     }
     if (!rc && n > 0) {
         if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_PARSE);
-        pass1_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, d_el, d_maxidx, d_err1);
-        irwls_count_launch(1);
-        rc |= irwls_check_launch("pass1");
-        pass2_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, nullptr, nullptr, nullptr, nullptr, d_cnt, nullptr,
-                                                       d_err2);
+        pass1_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, d_el, d_maxidx, d_err1, d_cnt);
         if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_PARSE);
         irwls_count_launch(1);
-        rc |= irwls_check_launch("pass2 count");
+        rc |= irwls_check_launch("pass1");
         cnt.resize(n);
         rc |= irwls_dev_d2h(&elements, d_el, sizeof elements);
         rc |= irwls_dev_d2h(&maxidx, d_maxidx, sizeof maxidx);
         rc |= irwls_dev_d2h(&err1, d_err1, sizeof err1);
-        rc |= irwls_dev_d2h(&err2, d_err2, sizeof err2);
         rc |= irwls_dev_d2h(cnt.data(), d_cnt, n * sizeof(int));
         rc |= irwls_dev_sync();
     }
     if (!rc && err1 < 0) {
         irwls_set_error(-22, "a line is longer than the reference's 99999-byte line buffer");
         rc = -22;
+    }
+    if (!rc) {
+        rc |= irwls_dev_malloc((void **)&d_start, (n + 1) * sizeof(long long));
+        rc |= irwls_dev_malloc((void **)&d_y, (n > 0 ? n : 1) * sizeof(double));
+        rc |= irwls_dev_malloc((void **)&d_q, (n > 0 ? n : 1) * sizeof(double));
+        rc |= irwls_dev_malloc((void **)&d_rmax, (n > 0 ? n : 1) * sizeof(int));
+        rc |= irwls_dev_malloc((void **)&d_sparse, sizeof(int));
+        rc |= irwls_dev_malloc((void **)&d_mis, sizeof(int));
+        rc |= irwls_dev_memset(d_sparse, 0, sizeof(int));
+    }
+    // The rows are laid out from pass 1's entry counts and written by one
+    // pass 2. On every line that pass 2 accepts the two passes stop at the
+    // same token, so the counts agree; should a line's count differ all the
+    // same, the layout is redone from pass 2's own counts (its count run,
+    // then the write again).
+    long long total = 0;
+    for (int attempt = 0; !rc; ++attempt) {
+        if (attempt == 1 && n > 0) {
+            if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_PARSE);
+            pass2_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, nullptr, nullptr, nullptr, nullptr, d_cnt, nullptr,
+                                                           d_err2, nullptr);
+            if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_PARSE);
+            irwls_count_launch(1);
+            rc |= irwls_check_launch("pass2 count");
+            rc |= irwls_dev_d2h(cnt.data(), d_cnt, n * sizeof(int));
+            rc |= irwls_dev_sync();
+            if (rc) break;
+        }
+        start.assign(n + 1, 0);
+        total = 0;
+        for (long long i = 0; i < n; ++i) {
+            start[i] = total;
+            total += cnt[i] + 1;  // entries and the -1 terminator
+        }
+        start[n] = total;
+        irwls_dev_free(d_rows);
+        d_rows = nullptr;
+        rc |= irwls_dev_malloc((void **)&d_rows, (total > 0 ? total : 1) * sizeof(svm_sample));
+        rc |= irwls_dev_h2d(d_start, start.data(), (n + 1) * sizeof(long long));
+        rc |= irwls_dev_memset(d_mis, 0, sizeof(int));
+        if (rc || n == 0) break;
+        int mis = 0;
+        if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_PARSE);
+        pass2_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, d_start, d_rows, d_y, d_q, d_cnt, d_rmax, d_err2,
+                                                       d_mis);
+        if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_PARSE);
+        irwls_count_launch(1);
+        rc |= irwls_check_launch("pass2 rows");
+        rc |= irwls_dev_d2h(&err2, d_err2, sizeof err2);
+        rc |= irwls_dev_d2h(&mis, d_mis, sizeof mis);
+        rc |= irwls_dev_sync();
+        if (rc || err2 != 0x7fffffffffffffffLL || !mis) break;
+        if (attempt == 1) {
+            irwls_set_error(-1, "libsvm reader: entry counts of pass 2 disagree between its two runs");
+            rc = -1;
+        }
     }
     if (!rc && err2 != 0x7fffffffffffffffLL) {
         const long long line = err2 / 4 + 1;
@@ -378,59 +442,44 @@ extern "C" int irwls_parse_libsvm(const char *buf, size_t len, svm_dataset *ds) 
             rc = -21;
         }
     }
-    long long total = 0;
-    if (!rc) {
-        start.resize(n + 1);
-        for (long long i = 0; i < n; ++i) {
-            start[i] = total;
-            total += cnt[i] + 1;  // entries and the -1 terminator
-        }
-        start[n] = total;
-        rc |= irwls_dev_malloc((void **)&d_start, (n + 1) * sizeof(long long));
-        rc |= irwls_dev_malloc((void **)&d_rows, (total > 0 ? total : 1) * sizeof(svm_sample));
-        rc |= irwls_dev_malloc((void **)&d_y, (n > 0 ? n : 1) * sizeof(double));
-        rc |= irwls_dev_malloc((void **)&d_q, (n > 0 ? n : 1) * sizeof(double));
-        rc |= irwls_dev_malloc((void **)&d_rmax, (n > 0 ? n : 1) * sizeof(int));
-        rc |= irwls_dev_malloc((void **)&d_sparse, sizeof(int));
-        rc |= irwls_dev_memset(d_sparse, 0, sizeof(int));
-        if (!rc) rc |= irwls_dev_h2d(d_start, start.data(), (n + 1) * sizeof(long long));
-    }
-    svm_sample *h_rows = nullptr;
     std::vector<double> y, q;
     std::vector<int> rmax;
     int sparse = 0;
+    bool held = false;  // *ds holds host arrays
     if (!rc && n > 0) {
         if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_PARSE);
-        pass2_kernel<<<grid, 128, 0, irwls_stream()>>>(L, n, d_start, d_rows, d_y, d_q, d_cnt, d_rmax, d_err2);
-        irwls_count_launch(1);
-        rc |= irwls_check_launch("pass2 rows");
         sparse_kernel<<<grid, 128, 0, irwls_stream()>>>(d_rows, d_start, n, d_sparse);
         if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_PARSE);
         irwls_count_launch(1);
         rc |= irwls_check_launch("sparse");
-        h_rows = (svm_sample *)malloc((size_t)total * sizeof(svm_sample));
+    }
+    if (!rc) {
+        // the rows go straight into the dataset's features array
+        rc = irwls_dataset_alloc(ds, (int)n, (long long)elements, maxidx, total);
+        held = rc == 0;
+    }
+    if (!rc && n > 0) {
         y.resize(n);
         q.resize(n);
         rmax.resize(n);
-        if (!h_rows) rc = -3;
-        if (!rc) {
-            rc |= irwls_dev_d2h(h_rows, d_rows, (size_t)total * sizeof(svm_sample));
-            rc |= irwls_dev_d2h(y.data(), d_y, n * sizeof(double));
-            rc |= irwls_dev_d2h(q.data(), d_q, n * sizeof(double));
-            rc |= irwls_dev_d2h(rmax.data(), d_rmax, n * sizeof(int));
-            rc |= irwls_dev_d2h(&sparse, d_sparse, sizeof(int));
-            rc |= irwls_dev_sync();
-        }
+        rc |= irwls_dev_d2h(ds->features, d_rows, (size_t)total * sizeof(svm_sample));
+        rc |= irwls_dev_d2h(y.data(), d_y, n * sizeof(double));
+        rc |= irwls_dev_d2h(q.data(), d_q, n * sizeof(double));
+        rc |= irwls_dev_d2h(rmax.data(), d_rmax, n * sizeof(int));
+        rc |= irwls_dev_d2h(&sparse, d_sparse, sizeof(int));
+        rc |= irwls_dev_sync();
     }
-    void *bufs[] = {d_text, d_nl, d_start, d_el, d_maxidx, d_err1, d_cnt, d_rmax, d_sparse, d_err2, d_rows, d_y, d_q};
+    void *bufs[] = {d_text, d_nl, d_start, d_el, d_maxidx, d_err1, d_cnt, d_rmax, d_sparse, d_err2, d_rows, d_y, d_q,
+                    d_mis};
     for (void *p : bufs) irwls_dev_free(p);
     if (!rc) {
         int max_index = 0;
         for (long long i = 0; i < n; ++i) max_index = std::max(max_index, rmax[i]);
-        rc = irwls_dataset_assemble(ds, (int)n, (long long)elements, maxidx, max_index, sparse, h_rows, total,
-                                    start.data(), y.data(), q.data());
+        rc = irwls_dataset_finish(ds, (int)n, maxidx, max_index, sparse, total, start.data(), y.data(), q.data());
+    } else if (held) {
+        freeDataset(*ds);
+        memset(ds, 0, sizeof *ds);
     }
-    free(h_rows);
     return rc;
 }
 

@@ -157,28 +157,46 @@ svm_dataset readTrainFile(char filename[]) {
  * entry (row i from row_start[i]); y and q are the labels and row norms. The
  * class-mean rows l and l + 1 are formed here exactly as readTrainFile forms
  * them (sums in row order, the negative mean's norm divided by the positive
- * count), over the pass-1 index range 0 ... maxidx. */
-int irwls_dataset_assemble(svm_dataset *ds, int l, long long pass1_elements, int maxidx, int max_index, int sparse,
-                           const svm_sample *rows, long long row_entries, const long long *row_start,
-                           const double *y, const double *q) {
-    const int top = maxidx > max_index ? maxidx : max_index;
+ * count), over the pass-1 index range 0 ... maxidx.
+ *
+ * In two steps for a caller that copies the rows itself:
+ * irwls_dataset_alloc allocates the arrays (features sized as readTrainFile
+ * sizes them, zeroed), the caller writes the rows to features[0,
+ * row_entries), and irwls_dataset_finish sets the row pointers, labels and
+ * norms and appends the class-mean rows. Either step frees what it holds on
+ * failure and returns -3; irwls_dataset_assemble is the two with a copy of
+ * rows[] between them. */
+int irwls_dataset_alloc(svm_dataset *ds, int l, long long pass1_elements, int maxidx, long long row_entries) {
     long long elements = pass1_elements > row_entries ? pass1_elements : row_entries;
     elements += 2 * ((long long)maxidx + 2);
     ds->l = l;
-    ds->sparse = sparse;
     ds->y = (double *)calloc((size_t)l + 2, sizeof(double));
     ds->quadratic_value = (double *)calloc((size_t)l + 2, sizeof(double));
     ds->x = (svm_sample **)calloc((size_t)l + 2, sizeof(svm_sample *));
     ds->features = (svm_sample *)calloc((size_t)elements, sizeof(svm_sample));
-    double *sum_pos = (double *)calloc((size_t)top + 1, sizeof(double));
-    double *sum_neg = (double *)calloc((size_t)top + 1, sizeof(double));
-    if (!ds->y || !ds->quadratic_value || !ds->x || !ds->features || !sum_pos || !sum_neg) {
-        free(sum_pos);
-        free(sum_neg);
+    if (!ds->y || !ds->quadratic_value || !ds->x || !ds->features) {
+        freeDataset(*ds);
+        memset(ds, 0, sizeof *ds);
         irwls_set_error(-3, "host allocation failed while assembling the dataset");
         return -3;
     }
-    if (row_entries > 0) memcpy(ds->features, rows, (size_t)row_entries * sizeof(svm_sample));
+    return 0;
+}
+
+int irwls_dataset_finish(svm_dataset *ds, int l, int maxidx, int max_index, int sparse, long long row_entries,
+                         const long long *row_start, const double *y, const double *q) {
+    const int top = maxidx > max_index ? maxidx : max_index;
+    double *sum_pos = (double *)calloc((size_t)top + 1, sizeof(double));
+    double *sum_neg = (double *)calloc((size_t)top + 1, sizeof(double));
+    if (!sum_pos || !sum_neg) {
+        free(sum_pos);
+        free(sum_neg);
+        freeDataset(*ds);
+        memset(ds, 0, sizeof *ds);
+        irwls_set_error(-3, "host allocation failed while assembling the dataset");
+        return -3;
+    }
+    ds->sparse = sparse;
     double n_pos = 0.0, n_neg = 0.0;
     for (int i = 0; i < l; i++) {
         ds->x[i] = &ds->features[row_start[i]];
@@ -220,6 +238,15 @@ int irwls_dataset_assemble(svm_dataset *ds, int l, long long pass1_elements, int
     free(sum_pos);
     free(sum_neg);
     return 0;
+}
+
+int irwls_dataset_assemble(svm_dataset *ds, int l, long long pass1_elements, int maxidx, int max_index, int sparse,
+                           const svm_sample *rows, long long row_entries, const long long *row_start,
+                           const double *y, const double *q) {
+    int rc = irwls_dataset_alloc(ds, l, pass1_elements, maxidx, row_entries);
+    if (rc) return rc;
+    if (row_entries > 0) memcpy(ds->features, rows, (size_t)row_entries * sizeof(svm_sample));
+    return irwls_dataset_finish(ds, l, maxidx, max_index, sparse, row_entries, row_start, y, q);
 }
 
 /* Labeled CSV file (src/IOStructures.c:293-493): label first, the k-th value

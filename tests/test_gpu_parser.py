@@ -1,7 +1,8 @@
 """The libsvm reader on the GPU (irwls_parse_libsvm / readTrainFileGPU,
 libirwls_gb300/csrc/dev_parse.cu) against the reference's reader:
 
-- the golden reader fixtures: the reference's own parse of two files;
+- the golden reader fixtures: the reference's own parse of two files, with
+  the rows laid out from pass 1's entry counts and written by one pass 2;
 - randomised files (tabs, repeated and trailing blanks, CRLF, exponents,
   17-digit and subnormal values, signs, ragged and dense rows) against the
   host readTrainFile, field by field and bit for bit, class-mean rows
@@ -81,8 +82,12 @@ def _host(lib, text):
 def test_golden_files(key):
     lib = _lib()
     g = np.load(os.path.join(H.GOLDEN, "reader.npz"))
+    n0 = lib.irwls_kernel_launches()
     rc, ds = _parse(lib, g[key + "_text"].tobytes())
     assert rc == 0, lib.irwls_last_error_message()
+    # one pass 2: the rows laid out from pass 1's counts (newline count and
+    # write, pass 1, pass 2, the sparse flag)
+    assert lib.irwls_kernel_launches() - n0 == 5
     assert ds.l == int(g[key + "_l"]) and ds.sparse == int(g[key + "_sparse"])
     assert ds.maxdim == int(g[key + "_maxdim"])
     rows, y, q = _abi.dataset_rows(ds, ds.l + 2)
@@ -132,8 +137,10 @@ def _file(rng, n, d, dense):
 def test_random_files_equal_host_reader(seed, n, d, dense):
     lib = _lib()
     text = _file(random.Random(seed), n, d, dense)
+    n0 = lib.irwls_kernel_launches()
     rc, dev = _parse(lib, text)
     assert rc == 0, lib.irwls_last_error_message()
+    assert lib.irwls_kernel_launches() - n0 == 5  # pass 1's counts were pass 2's on every line
     host, path = _host(lib, text)
     try:
         _same(dev, host)
