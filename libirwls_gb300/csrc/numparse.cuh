@@ -6,6 +6,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include "pow5_table.cuh"
+
 #ifdef __CUDACC__
 #define NP_HD __host__ __device__
 #else
@@ -149,7 +151,96 @@ NP_HD uint64_t bi_extract(const Big &a, int sh, int &half, int &sticky) {
 
 NP_HD inline int bitlen64(uint64_t v) { return v ? 64 - np_clzll(v) : 0; }
 
-// w * 10^q rounded to nearest even (w >= 1), as a positive double.
+// ---- the interval step --------------------------------------------------------
+
+// a * b as two 64-bit halves.
+NP_HD inline void np_mul64(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo) {
+#ifdef __CUDA_ARCH__
+    lo = a * b;
+    hi = __umul64hi(a, b);
+#else
+    const unsigned __int128 p = (unsigned __int128)a * b;
+    lo = (uint64_t)p;
+    hi = (uint64_t)(p >> 64);
+#endif
+}
+
+// Y 2^k rounded to nearest even (subnormals and overflow included), Y the
+// 256-bit integer y[3] .. y[0] with at least 54 significant bits. Returns
+// false for a shorter Y.
+NP_HD bool np_round_limbs(const uint64_t y[4], int k, double *out) {
+    int L = 0;
+    for (int i = 3; i >= 0 && !L; --i)
+        if (y[i]) L = 64 * i + bitlen64(y[i]);
+    if (L < 54) return false;
+    int sh = L - 53;                       // lowest kept bit
+    if (sh < -1074 - k) sh = -1074 - k;    // below the subnormal grid
+    if (sh > L) {                          // under half the smallest subnormal
+        *out = 0.0;
+        return true;
+    }
+    const int i = sh >> 6, o = sh & 63;
+    uint64_t m = i < 4 ? y[i] >> o : 0;
+    if (o && i + 1 < 4) m |= y[i + 1] << (64 - o);
+    const int hb = sh - 1, hi = hb >> 6, ho = hb & 63;
+    const int half = (int)((y[hi] >> ho) & 1u);
+    int sticky = (y[hi] & ((1ULL << ho) - 1)) != 0;
+    for (int j = 0; j < hi && !sticky; ++j) sticky = y[j] != 0;
+    if (half && (sticky || (m & 1))) ++m;
+    *out = ldexp((double)m, sh + k);  // m <= 2^53: exact, or the overflow to infinity
+    return true;
+}
+
+// w 10^q rounded to nearest even for w >= 1, through the table of 5^q:
+// w 10^q = X 2^(q - lz + E_q - 127) with X = (w << lz) 5^q 2^(127 - E_q)
+// (lz the leading zeros of w), and X lies in [A, A + (w << lz)), A =
+// (w << lz) T_q, because 5^q 2^(127 - E_q) lies in [T_q, T_q + 1) (exactly
+// T_q for 0 <= q <= 55). Rounding is monotone, so when both ends of that
+// interval round to the same double, so does X. Returns false when they do
+// not (X within 2^-73 of its rounding unit of a rounding boundary, or an
+// exact tie) and for q outside the table.
+NP_HD bool np_interval_round(uint64_t w, int q, double *out) {
+    if (q < NP_POW5_QMIN || q > NP_POW5_QMAX) return false;
+    const int t = q - NP_POW5_QMIN;
+#ifdef __CUDA_ARCH__
+    const uint64_t th = NP_POW5_D[t][0], tl = NP_POW5_D[t][1];
+    const int e5 = NP_POW5_D_E[t];
+#else
+    const uint64_t th = NP_POW5_H[t][0], tl = NP_POW5_H[t][1];
+    const int e5 = NP_POW5_H_E[t];
+#endif
+    const int lz = np_clzll(w);
+    const uint64_t wn = w << lz;
+    uint64_t p1h, p1l, p2h, p2l;
+    np_mul64(wn, tl, p1h, p1l);
+    np_mul64(wn, th, p2h, p2l);  // p2h <= 2^64 - 2
+    uint64_t a[4], b[4];
+    a[0] = p1l;
+    a[1] = p1h + p2l;
+    a[2] = p2h + (a[1] < p2l ? 1 : 0);
+    a[3] = 0;
+    const int k = q - lz + e5 - 127;
+    double ra, rb;
+    if (!np_round_limbs(a, k, &ra)) return false;
+    if (q >= 0 && q <= 55) {  // T_q is 5^q 2^(127 - E_q) itself: X = A
+        *out = ra;
+        return true;
+    }
+    b[0] = a[0] + wn;
+    uint64_t c = b[0] < wn ? 1 : 0;
+    b[1] = a[1] + c;
+    c = (c && b[1] == 0) ? 1 : 0;
+    b[2] = a[2] + c;
+    c = (c && b[2] == 0) ? 1 : 0;
+    b[3] = c;
+    if (!np_round_limbs(b, k, &rb) || ra != rb) return false;
+    *out = ra;
+    return true;
+}
+
+// w * 10^q rounded to nearest even (w >= 1), as a positive double: the
+// exact-double product or quotient when w and 10^|q| are exact (Clinger's
+// fast path), else the interval step, else big-integer arithmetic.
 NP_HD double dec_to_double(uint64_t w, int q) {
     if (q > 310) return np_bits_to_double(0x7ff0000000000000LL);
     if (q < -380) return 0.0;
@@ -158,6 +249,8 @@ NP_HD double dec_to_double(uint64_t w, int q) {
         for (int k = 0; k < (q < 0 ? -q : q); ++k) p = np_mul(p, 10.0);  // 10^k < 2^53 * 2^k: exact
         return q < 0 ? np_div((double)w, p) : np_mul((double)w, p);
     }
+    double r;
+    if (np_interval_round(w, q, &r)) return r;
     if (q >= 0) {
         Big N;
         bi_set(N, w);
