@@ -88,10 +88,24 @@ __device__ int line_end(const char *b, int ls, int le) {
 
 constexpr int CHUNK = 16384;  // bytes per block when searching newlines
 
+// Newline bytes of a 4-byte word: __vcmpeq4 sets 0xff in each matching byte.
+__device__ __forceinline__ int nl_in_word(uint32_t w) { return __popc(__vcmpeq4(w, 0x0a0a0a0au)) >> 3; }
+
+// Newlines per chunk. A whole chunk on a 16-byte boundary is read in 16-byte
+// loads; the last, partial chunk byte by byte, so no load passes the end of
+// the text.
 __global__ void nl_count_kernel(const char *__restrict__ b, long long len, int *__restrict__ cnt) {
     const long long c0 = (long long)blockIdx.x * CHUNK;
     int n = 0;
-    for (long long p = c0 + threadIdx.x; p < min(len, c0 + CHUNK); p += blockDim.x) n += b[p] == '\n';
+    if (len - c0 >= CHUNK && ((uintptr_t)(b + c0) & 15) == 0) {
+        const uint4 *p4 = (const uint4 *)(b + c0);
+        for (int j = threadIdx.x; j < CHUNK / 16; j += blockDim.x) {
+            const uint4 v = p4[j];
+            n += nl_in_word(v.x) + nl_in_word(v.y) + nl_in_word(v.z) + nl_in_word(v.w);
+        }
+    } else {
+        for (long long p = c0 + threadIdx.x; p < min(len, c0 + CHUNK); p += blockDim.x) n += b[p] == '\n';
+    }
     for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
     __shared__ int ws[32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = n;
@@ -104,13 +118,31 @@ __global__ void nl_count_kernel(const char *__restrict__ b, long long len, int *
 }
 
 // Newline positions of each chunk, in order: thread k scans the chunk's k-th
-// slice of CHUNK / blockDim bytes.
+// slice of CHUNK / blockDim bytes. A 64-byte slice inside the text (on a
+// 16-byte boundary) is held in registers from four 16-byte loads; the slice
+// holding the end of the text is read byte by byte.
 __global__ void nl_write_kernel(const char *__restrict__ b, long long len, const long long *__restrict__ off,
                                 long long *__restrict__ nl) {
     const int per = CHUNK / blockDim.x;
     const long long s0 = (long long)blockIdx.x * CHUNK + (long long)threadIdx.x * per;
+    const bool whole = per == 64 && len - s0 >= 64 && ((uintptr_t)(b + s0) & 15) == 0;
+    uint32_t wv[16];
     int n = 0;
-    for (long long p = s0; p < min(len, s0 + per); ++p) n += b[p] == '\n';
+    if (whole) {
+        const uint4 *p4 = (const uint4 *)(b + s0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint4 v = p4[j];
+            wv[4 * j] = v.x;
+            wv[4 * j + 1] = v.y;
+            wv[4 * j + 2] = v.z;
+            wv[4 * j + 3] = v.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) n += nl_in_word(wv[j]);
+    } else {
+        for (long long p = s0; p < min(len, s0 + per); ++p) n += b[p] == '\n';
+    }
     __shared__ int pre[1024];
     pre[threadIdx.x] = n;
     __syncthreads();
@@ -121,8 +153,20 @@ __global__ void nl_write_kernel(const char *__restrict__ b, long long len, const
         __syncthreads();
     }
     long long k = off[blockIdx.x] + pre[threadIdx.x] - n;
-    for (long long p = s0; p < min(len, s0 + per); ++p)
-        if (b[p] == '\n') nl[k++] = p;
+    if (whole) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            uint32_t m = __vcmpeq4(wv[j], 0x0a0a0a0au);  // little-endian: byte i is bits 8i .. 8i + 7
+            while (m) {
+                const int bit = __ffs(m) - 1;
+                nl[k++] = s0 + 4 * j + (bit >> 3);
+                m &= ~(0xffu << bit);
+            }
+        }
+    } else {
+        for (long long p = s0; p < min(len, s0 + per); ++p)
+            if (b[p] == '\n') nl[k++] = p;
+    }
 }
 
 struct LineSet {
