@@ -13,10 +13,26 @@
 extern "C" {
 #endif
 
-/* Status of the last call that can fail on the device: 0 = success. Training
- * and prediction functions return NULL after a failure and set this. */
+/* Status of the last call that can fail on the device: 0 = success, < 0 =
+ * an error, > 0 = a warning. Training and prediction functions return NULL
+ * after an error and set this; a warning leaves the result in place.
+ * Errors: -1 no device, -2 CUDA error, -3 allocation failed, -4 invalid
+ * dataset (negative feature index, non-finite value or label, too many
+ * entries) or arguments, -5 width/file limits, -6 solve limits, -7 to -12
+ * limits of particular paths (see the message), -13 a tensor-core pipeline
+ * wait ran out, -14 a CUDA error was already pending (allocation-free solve),
+ * -20 to -22 the device libsvm reader. Warnings: IRWLS_WARN_PIVOT. */
 int irwls_last_error(void);
 const char *irwls_last_error_message(void);
+/* ParallelLinearSystem / ParallelChol met a pivot that is not positive. The
+ * reference (LAPACK dpotrf) reports it in an info value it ignores; this
+ * library factors on as the reference's solve does and reports it here. */
+enum { IRWLS_WARN_PIVOT = 1 };
+/* Test hook, no counterpart in the reference: arms an injected failure of the
+ * n-th device or pinned-host allocation the library makes from now on (n <= 0
+ * disarms). The call that meets it fails with -3, as when the runtime refuses
+ * memory, and the library stays usable. */
+void irwls_debug_fail_alloc(long long n);
 /* 1 when a CUDA device is usable. The library has no CPU path: without a
  * device every training or prediction call fails with an error. */
 int irwls_gpu_available(void);
@@ -200,6 +216,7 @@ double irwls_fp32_peak_tflops(int reps);
  * d_M: column-major n x n matrix in device memory, leading dimension
  * ld >= n + 1 (row n holds the right-hand side); overwritten by its lower
  * Cholesky factor (a non-positive pivot is stored as LAPACK dpotrf leaves it).
+ * Row n is scratch: its contents on return are unspecified.
  * d_b: right-hand side (n doubles, device) copied into row n, or NULL if row n
  * already holds it. d_x: solution (n doubles, device), or NULL to factor only.
  * d_info: NULL, or a device int that receives the first failed pivot
@@ -207,7 +224,9 @@ double irwls_fp32_peak_tflops(int reps);
  * stream; the call only enqueues work on it.
  *
  * Limit: n <= 4096; larger orders are rejected (-11, see
- * irwls_last_error_message). Scratch: one 1 MiB array in the library's
+ * irwls_last_error_message). A CUDA error already pending in the calling
+ * thread when the call starts is left in place and the call returns -14
+ * without enqueueing anything. Scratch: one 1 MiB array in the library's
  * device memory, held by every GPU that loads the library until the process
  * exits. All calls share it and it keeps the last call's contents, so calls
  * that overlap on the GPU (on different streams) race; serialize them. The
@@ -216,6 +235,9 @@ double irwls_fp32_peak_tflops(int reps);
  * Returns 0 on success. */
 int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double *d_b, double *d_x, int *d_info,
                              void *stream);
+/* CTAs of the cooperative backward sweep that a solve of order n uses on the
+ * current device (0: the single-CTA sweep); no counterpart in the reference. */
+int irwls_chol_sweep_ctas(int n);
 
 #ifdef __cplusplus
 }

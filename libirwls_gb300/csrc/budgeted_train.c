@@ -256,7 +256,7 @@ static int budget_rows(const svm_dataset *ds, const int *idx, int m) {
 int *SGMA(svm_dataset dataset, properties props) {
     irwls_clear_error();
     irwls_dev_set X;
-    if (irwls_dev_upload(&dataset, dataset.l + 2, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
+    if (irwls_check_labels(&dataset, dataset.l) || irwls_dev_upload(&dataset, dataset.l + 2, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
     int *cent = (int *)malloc((size_t)(props.size > 0 ? props.size : 1) * sizeof(int));
     if (irwls_sgma_dev(&X, &dataset, props, cent)) {
         free(cent);
@@ -270,7 +270,7 @@ double *IRWLSpar(svm_dataset dataset, int *indexes, properties props) {
     irwls_clear_error();
     irwls_dev_set X;
     const int rows = budget_rows(&dataset, indexes, props.size);
-    if (irwls_dev_upload(&dataset, rows, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
+    if (irwls_check_labels(&dataset, dataset.l) || irwls_dev_upload(&dataset, rows, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
     double *w = (double *)malloc((size_t)(props.size > 0 ? props.size : 1) * sizeof(double));
     if (irwls_par_dev(&X, dataset.l, indexes, props, w)) {
         free(w);

@@ -42,7 +42,7 @@ int default_workers() { return g_tuned_workers > 0 ? g_tuned_workers : 16; }
 // One full-IRWLS SVM in the calling thread's context.
 int train_full_one(const svm_dataset &ds, const properties &p, unsigned seed, double **beta) {
     irwls_dev_set X;
-    if (irwls_dev_upload(&ds, ds.l, p.kernelType, p.Kgamma, 0, 0, &X)) return -1;
+    if (irwls_check_labels(&ds, ds.l) || irwls_dev_upload(&ds, ds.l, p.kernelType, p.Kgamma, 0, 0, &X)) return -1;
     double *b = (double *)malloc((size_t)(ds.l + 1) * sizeof(double));
     irwls_srand(seed);
     const int rc = b ? irwls_full_train_dev(&X, ds.l, p, b) : -3;
@@ -62,7 +62,7 @@ int train_budgeted_one(const svm_dataset &ds, const properties &p, unsigned seed
     *w = nullptr;
     irwls_srand(seed);
     irwls_dev_set X;
-    if (irwls_dev_upload(&ds, ds.l + 2, p.kernelType, p.Kgamma, 0, 0, &X)) return -1;
+    if (irwls_check_labels(&ds, ds.l) || irwls_dev_upload(&ds, ds.l + 2, p.kernelType, p.Kgamma, 0, 0, &X)) return -1;
     const int m = p.size > 0 ? p.size : 1;
     int *c = nullptr;
     int rc = 0;

@@ -18,6 +18,8 @@
 // one launch applies the rank-32 update to the lower trailing matrix.
 #include <math.h>
 
+#include <atomic>
+
 #include <cooperative_groups.h>
 
 #include "dev_common.cuh"
@@ -229,7 +231,9 @@ __global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
 }
 
 // Enqueues the whole factorization (and the solve when has_b) on `st`, with
-// Dinv holding ceil(n/32) blocks of 32x32 doubles.
+// Dinv holding ceil(n/32) blocks of 32x32 doubles. Row n of M (the
+// right-hand side) is scratch on return: which backward sweep runs decides
+// what it holds.
 // The same backward sweep on several CTAs (a cooperative launch): thread t
 // of CTA k owns row 256 k + t of z, which is row n of M updated in place.
 // Per 32-row block from the bottom, every CTA forms x_b = D_b^-T y_b in
@@ -271,21 +275,35 @@ __global__ void __launch_bounds__(256) chol_backsolve_coop_kernel(double *__rest
     }
 }
 
-// CTAs of the cooperative sweep for order n, or 0 when they cannot all be
-// resident at once (the single-CTA sweep is used then).
+// CTAs of the cooperative sweep for order n on the current device, or 0 when
+// they cannot all be resident at once (the single-CTA sweep is used then).
+// The capacity is computed per device from the device's own attributes (the
+// library context need not exist: the allocation-free solve runs without it)
+// and published only once computed; concurrent first calls compute the same
+// value. Only errors of these queries are cleared, never one the caller left.
 int coop_backsolve_ctas(int n) {
-    static int cap = -1;
-    if (cap < 0) {
-        int dev = 0, coop = 0, per_sm = 0;
-        cap = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_backsolve_coop_kernel, 256, 0) == cudaSuccess)
-            cap = per_sm * (irwls_num_sms() > 0 ? irwls_num_sms() : 0);
+    constexpr int kDevices = 64;
+    static std::atomic<int> cap_plus1[kDevices];  // 0: not computed yet
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
+        return 0;
+    }
+    if (dev < 0 || dev >= kDevices) return 0;
+    int c = cap_plus1[dev].load(std::memory_order_acquire);
+    if (c == 0) {
+        int coop = 0, per_sm = 0, sms = 0, cap = 0;
+        if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_backsolve_coop_kernel, 256, 0) != cudaSuccess)
+            cudaGetLastError();
+        else if (coop)
+            cap = per_sm * sms;
+        c = cap + 1;
+        cap_plus1[dev].store(c, std::memory_order_release);
     }
     const int g = (n + 255) / 256;
-    return g <= cap ? g : 0;
+    return g <= c - 1 ? g : 0;
 }
 
 int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Dinv, cudaStream_t st) {
@@ -373,6 +391,19 @@ extern "C" int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_
     return 0;
 }
 
+extern "C" int irwls_chol_sweep_ctas(int n) { return coop_backsolve_ctas(n); }
+
+extern "C" int irwls_dev_pivot_status(int *info) {
+    *info = 0;
+    cudaError_t e = cudaMemcpyAsync(info, irwls_dev_flags(), sizeof(int), cudaMemcpyDeviceToHost, irwls_stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(irwls_stream());
+    if (e != cudaSuccess) {
+        irwls_set_error(-2, "CUDA error reading the pivot status: %s", cudaGetErrorString(e));
+        return -2;
+    }
+    return 0;
+}
+
 namespace {
 // out = A v (trans = 0) or out = A^T v (trans = 1) for a column-major size x
 // size matrix; one warp per output entry.
@@ -427,6 +458,15 @@ static double *g_noalloc_addr[IRWLS_NOALLOC_DEVICES];  // device address of the 
 extern "C" int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double *d_b, double *d_x, int *d_info,
                                         void *stream) {
     irwls_clear_error();
+    // A CUDA error the caller left pending would be taken for one of this
+    // call's launches (each launch is checked with cudaGetLastError, which
+    // clears it): refuse instead, and leave the caller's error in place.
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        irwls_set_error(-14, "irwls_chol_solve_noalloc: a CUDA error is already pending (%s); not cleared",
+                        cudaGetErrorString(pending));
+        return -14;
+    }
     if (n <= 0) return 0;
     if (n > IRWLS_NOALLOC_MAX_ORDER) {
         irwls_set_error(-11, "irwls_chol_solve_noalloc: order %d exceeds its limit of %d", n, IRWLS_NOALLOC_MAX_ORDER);

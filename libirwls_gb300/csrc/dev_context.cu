@@ -9,6 +9,7 @@
 // trainings run concurrently on separate streams. Device memory is allocated
 // stream-ordered (cudaMallocAsync / cudaFreeAsync on the context's stream),
 // so that no thread's free waits for the whole device.
+#include <math.h>
 #include <stdarg.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -78,7 +79,18 @@ std::atomic<long long> g_launches{0};
 
 extern "C" void irwls_set_error(int code, const char *fmt, ...) {
     Ctx *c = cur();
-    if (c->err) return;  // keep the first error
+    if (c->err < 0) return;  // keep the first error (an error replaces a warning)
+    c->err = code;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->msg, sizeof c->msg, fmt, ap);
+    va_end(ap);
+}
+// A warning (positive code): the call returns its result, and the condition
+// is reported unless an error or an earlier warning is already recorded.
+extern "C" void irwls_set_warning(int code, const char *fmt, ...) {
+    Ctx *c = cur();
+    if (c->err) return;
     c->err = code;
     va_list ap;
     va_start(ap, fmt);
@@ -187,6 +199,18 @@ extern "C" void irwls_rand_sequence(unsigned seed, int n, int *out) {
     for (int i = 0; i < n; ++i) out[i] = g.next();
 }
 
+// Allocation-failure injection for tests of the error paths: armed with
+// n > 0, the n-th device or pinned-host allocation of the library from then
+// on fails as if the runtime had refused it (nothing is allocated).
+static std::atomic<long long> g_fail_alloc{0};
+extern "C" void irwls_debug_fail_alloc(long long n) { g_fail_alloc.store(n > 0 ? n : 0); }
+static bool injected_alloc_failure() {
+    long long v = g_fail_alloc.load();
+    while (v > 0)
+        if (g_fail_alloc.compare_exchange_weak(v, v - 1)) return v == 1;
+    return false;
+}
+
 // Grow-only scratch buffer `slot` of the current context (stream-ordered).
 extern "C" void *irwls_ctx_scratch(int slot, size_t bytes) {
     Ctx *c = cur();
@@ -194,6 +218,10 @@ extern "C" void *irwls_ctx_scratch(int slot, size_t bytes) {
         if (c->scratch[slot]) cudaFreeAsync(c->scratch[slot], c->stream);
         c->scratch[slot] = nullptr;
         c->scratch_bytes[slot] = 0;
+        if (injected_alloc_failure()) {
+            irwls_set_error(-3, "device scratch of %zu bytes failed (injected failure)", bytes);
+            return nullptr;
+        }
         if (cudaMallocAsync(&c->scratch[slot], bytes, c->stream) != cudaSuccess) {
             cudaGetLastError();
             irwls_set_error(-3, "device scratch of %zu bytes failed", bytes);
@@ -213,6 +241,10 @@ extern "C" int irwls_dev_sync(void) {
 extern "C" int irwls_dev_malloc(void **p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
+    if (injected_alloc_failure()) {
+        irwls_set_error(-3, "device allocation of %zu bytes failed (injected failure)", bytes);
+        return -3;
+    }
     cudaError_t e = cudaMallocAsync(p, bytes, cur()->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -250,6 +282,11 @@ extern "C" int irwls_dev_memset(void *d, int byte, size_t bytes) {
     return e == cudaSuccess ? 0 : cuda_fail(e, "memset");
 }
 extern "C" int irwls_dev_host_alloc(void **p, size_t bytes) {
+    if (injected_alloc_failure()) {
+        *p = nullptr;
+        irwls_set_error(-3, "pinned host allocation of %zu bytes failed (injected failure)", bytes);
+        return -3;
+    }
     cudaError_t e = cudaMallocHost(p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
         *p = nullptr;
@@ -292,6 +329,17 @@ extern "C" int irwls_model_feature_width(const model *m) {
     return w;
 }
 
+// Training needs finite labels (prediction does not read them, so its
+// datasets are not checked).
+extern "C" int irwls_check_labels(const svm_dataset *ds, int n_rows) {
+    for (int i = 0; i < n_rows; ++i)
+        if (!isfinite(ds->y[i])) {
+            irwls_set_error(-4, "non-finite label %g in row %d", ds->y[i], i);
+            return -4;
+        }
+    return 0;
+}
+
 // csr_only: no dense copy X (for consumers that read the rows as CSR only).
 static int upload_rows(svm_sample *const *rows, const double *q, const double *y, int n_rows, int mode,
                        double gamma, int raw_width, int width_hint, irwls_dev_set *out, int csr_only = 0) {
@@ -307,6 +355,10 @@ static int upload_rows(svm_sample *const *rows, const double *q, const double *y
             ++nnz;
             if (p->index < 0) {
                 irwls_set_error(-4, "negative feature index %d in row %d", p->index, i);
+                return -4;
+            }
+            if (!isfinite(p->value)) {
+                irwls_set_error(-4, "non-finite value %g of feature %d in row %d", p->value, p->index, i);
                 return -4;
             }
             if (p->index + 1 > width) width = p->index + 1;

@@ -64,7 +64,7 @@ double *subIRWLS(svm_dataset dataset, properties props, double *GIN, double *e, 
     irwls_clear_error();
     const int l = dataset.l;
     irwls_dev_set X;
-    if (irwls_dev_upload(&dataset, l, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
+    if (irwls_check_labels(&dataset, l) || irwls_dev_upload(&dataset, l, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
     irwls_sub_ws ws;
     double *out = NULL;
     if (irwls_sub_alloc(&ws, l > 0 ? l : 1)) goto done_x;
@@ -302,7 +302,7 @@ double *trainFULL(svm_dataset dataset, properties props) {
     irwls_clear_error();
     if (props.verbose == 1) printf("\n");
     irwls_dev_set X;
-    if (irwls_dev_upload(&dataset, dataset.l, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
+    if (irwls_check_labels(&dataset, dataset.l) || irwls_dev_upload(&dataset, dataset.l, props.kernelType, props.Kgamma, 0, 0, &X)) return NULL;
     double *beta = (double *)malloc((size_t)(dataset.l + 1) * sizeof(double));
     if (irwls_full_train_dev(&X, dataset.l, props, beta)) {
         free(beta);

@@ -27,7 +27,7 @@ irwls_resident *irwls_resident_upload(svm_dataset dataset, properties props, int
     r->ds = dataset;
     r->kernelType = props.kernelType;
     const int rows = dataset.l + (with_mean_rows ? 2 : 0);
-    if (irwls_dev_upload(&dataset, rows, props.kernelType, props.Kgamma, 0, 0, &r->X)) {
+    if (irwls_check_labels(&dataset, dataset.l) || irwls_dev_upload(&dataset, rows, props.kernelType, props.Kgamma, 0, 0, &r->X)) {
         free(r);
         return NULL;
     }

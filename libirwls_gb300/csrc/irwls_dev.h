@@ -21,6 +21,13 @@ void irwls_set_error(int code, const char *fmt, ...);
 int irwls_get_error(void);
 const char *irwls_get_error_message(void);
 void irwls_clear_error(void);
+/* A warning (positive code): recorded unless an error or a warning already is. */
+void irwls_set_warning(int code, const char *fmt, ...);
+/* First failed pivot (1-based) of the last Cholesky on the current context's
+ * stream, 0 if none; synchronizes the stream. Returns 0 or an error. */
+int irwls_dev_pivot_status(int *info);
+/* -4 (and the error set) when one of the first n_rows labels is not finite. */
+int irwls_check_labels(const svm_dataset *ds, int n_rows);
 
 /* ---- context ------------------------------------------------------------ */
 int irwls_dev_init(void);                     /* idempotent; creates the stream */

@@ -54,6 +54,13 @@ static int block_solve(double *matrix, int r, int ro, int co, int n, const doubl
         if (b) rc |= irwls_dev_d2h(x, dx, n * sizeof(double));
         rc |= irwls_dev_sync();
     }
+    int info = 0;
+    if (!rc) rc |= irwls_dev_pivot_status(&info);
+    if (!rc && info)
+        irwls_set_warning(IRWLS_WARN_PIVOT,
+                          "pivot %d of the order-%d system is not positive: it is stored without its square root "
+                          "and the factorization goes on, as LAPACK dpotrf leaves it for the reference's solve",
+                          info, n);
     if (!rc)
         for (int c = 0; c < n; c++) memcpy(matrix + (size_t)(co + c) * r + ro, h + (size_t)c * ld, n * sizeof(double));
     irwls_dev_free(d);

@@ -265,7 +265,8 @@ int irwls_sgma_traces(svm_dataset dataset, properties props, float *feat, float 
     g_trace_feat = feat;
     g_trace_score = score;
     irwls_dev_set X;
-    int rc = irwls_dev_upload(&dataset, dataset.l + 2, props.kernelType, props.Kgamma, 0, 0, &X);
+    int rc = irwls_check_labels(&dataset, dataset.l);
+    if (!rc) rc = irwls_dev_upload(&dataset, dataset.l + 2, props.kernelType, props.Kgamma, 0, 0, &X);
     if (!rc) {
         int *cent = (int *)malloc((size_t)props.size * sizeof(int));
         rc = irwls_sgma_mixed_dev(&X, &dataset, props, cent);

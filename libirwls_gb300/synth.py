@@ -217,3 +217,20 @@ def write_libsvm(path: str, data: Sparse, labeled: bool = True) -> None:
             for k in range(ip[i], ip[i + 1]):
                 parts.append("%d:%.17g" % (ix[k], vv[k]))
             f.write(" ".join(parts) + "\n")
+
+
+def dataset_digest(hd) -> str:
+    """SHA-256 of a dataset exactly as the library reads it: the feature
+    array (index/value pairs with their -1 terminators, class-mean rows
+    included), every row's offset, the labels, the norms and the header
+    fields. Two machines that rebuild a seeded workload agree on it only if
+    every number the training sees is the same."""
+    import hashlib
+
+    h = hashlib.sha256()
+    h.update(np.array([hd.l, hd.sparse, hd.maxdim, hd.n_rows], dtype=np.int64).tobytes())
+    h.update(np.ascontiguousarray(hd.features).tobytes())
+    h.update(np.ascontiguousarray(hd.row_start, dtype=np.int64).tobytes())
+    h.update(np.ascontiguousarray(hd.y, dtype=np.float64).tobytes())
+    h.update(np.ascontiguousarray(hd.q, dtype=np.float64).tobytes())
+    return h.hexdigest()

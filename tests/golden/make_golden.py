@@ -26,6 +26,9 @@ import numpy as np
 # the reference links a single-threaded BLAS; keep OpenBLAS serial so the
 # factorizations follow one fixed order
 os.environ["OPENBLAS_NUM_THREADS"] = "1"
+# the reference's library functions run their OpenMP loops at the default team
+# size unless a CLI calls omp_set_num_threads; one thread is the -t 1 run
+os.environ["OMP_NUM_THREADS"] = "1"
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
