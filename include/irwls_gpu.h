@@ -33,6 +33,18 @@ enum { IRWLS_WARN_PIVOT = 1 };
  * disarms). The call that meets it fails with -3, as when the runtime refuses
  * memory, and the library stays usable. */
 void irwls_debug_fail_alloc(long long n);
+/* Test hook, no counterpart in the reference: the poll limit of every bounded
+ * wait of the precision form's full-IRWLS error-update kernel (<= 0: the
+ * default, 2^26 polls) and a stall switch with which that kernel's MMA thread
+ * issues no MMA and never completes an accumulator, so that the epilogue's
+ * wait runs out with no copy or MMA in flight. The training then fails with
+ * -13 and the next one runs normally. */
+void irwls_debug_tc_wait(long long limit, int stall);
+/* Operand pieces (1 or 3) the last precision-form full-IRWLS training used:
+ * 1 when every value of the set is exactly a bf16 after a scale of 1 or 255
+ * (binary and 8-bit data; the products are then exact), else 3 (hi + mid +
+ * lo of the FP32 value). */
+int irwls_last_tc_pieces(void);
 /* 1 when a CUDA device is usable. The library has no CPU path: without a
  * device every training or prediction call fails with an error. */
 int irwls_gpu_available(void);
@@ -226,7 +238,7 @@ double irwls_fp32_peak_tflops(int reps);
  * Limit: n <= 4096; larger orders are rejected (-11, see
  * irwls_last_error_message). A CUDA error already pending in the calling
  * thread when the call starts is left in place and the call returns -14
- * without enqueueing anything. Scratch: one 1 MiB array in the library's
+ * without enqueueing anything. Scratch: one array of about 1.06 MiB in the library's
  * device memory, held by every GPU that loads the library until the process
  * exits. All calls share it and it keeps the last call's contents, so calls
  * that overlap on the GPU (on different streams) race; serialize them. The
@@ -238,6 +250,12 @@ int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double *d_b, doub
 /* CTAs of the cooperative backward sweep that a solve of order n uses on the
  * current device (0: the single-CTA sweep); no counterpart in the reference. */
 int irwls_chol_sweep_ctas(int n);
+/* Test hook, no counterpart in the reference: which Cholesky factorization
+ * the solves use. 0 (default): one cooperative launch scheduled by data flow
+ * where the device allows it, else the multi-launch panel sequence; 1: the
+ * multi-launch sequence; 2: the data-flow launch only. Both give the same
+ * bits. */
+void irwls_debug_chol_path(int mode);
 
 #ifdef __cplusplus
 }

@@ -230,6 +230,196 @@ __global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same factorization in one cooperative launch, scheduled by data flow.
+//
+// The lower blocked matrix (32 x 32 tiles (i, j), i >= j, the right-hand-side
+// row n included as a row) is a list of tasks in column-major order; task t
+// belongs to CTA t mod G, and each CTA runs its tasks in order, keeping its
+// tile in shared memory. A tile takes the updates of panels k = 0 ... j - 1
+// as soon as their tiles L(i, k) and L(j, k) are published, then either
+// factors and inverts itself (i == j) or solves against the published inverse
+// of diagonal block j; it then publishes itself (a release store of a ready
+// word after its data; readers poll with acquire loads and read the data
+// from L2). Every dependency of a task has a smaller index, and all CTAs are
+// resident (cooperative launch), so the smallest unfinished task can always
+// run: no wait is circular. There are no grid-wide barriers, so a panel's
+// diagonal block is factored as soon as its last update lands while other
+// CTAs are still applying earlier panels elsewhere.
+//
+// Every element gets the multi-launch path's operations in the same order:
+// per panel, acc = sum over the panel's 32 columns by FMA from zero, then
+// M - acc; the diagonal blocks through factor_invert_block; the panel solves
+// as products with the inverted block. The results are the same bits.
+//
+// The waits are bounded: one that runs out (which needs a fault in this
+// schedule) sets the pivot status to -1 and the tensor-core status word to
+// CHOL_WAIT_CODE, and the CTA stops; the others then run out too.
+// ---------------------------------------------------------------------------
+constexpr long long DF_WAIT_LIMIT = 1LL << 22;
+constexpr int CHOL_WAIT_CODE = 0x40000000;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 polls *p until it is nonzero (or `abort` is set elsewhere); the
+// CTA learns the outcome at the barrier. False if the wait ran out.
+__device__ bool df_wait(const unsigned *p, const volatile int *abort, int *ok_sh) {
+    if (threadIdx.x == 0) {
+        int ok = 0;
+        for (long long it = 0; it < DF_WAIT_LIMIT; ++it) {
+            if (ld_acquire_u32(p)) {
+                ok = 1;
+                break;
+            }
+            if (*abort) break;
+            __nanosleep(64);
+        }
+        *ok_sh = ok;
+    }
+    __syncthreads();
+    return *ok_sh != 0;
+}
+
+// Publishes the tile just stored by the whole CTA.
+__device__ __forceinline__ void df_publish(unsigned *p) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_u32(p, 1u);
+    }
+}
+
+// ready: diag[j] at ready[j] (j < nbc), tile L(i, j) at ready[nbc + j * nbr + i].
+__global__ void __launch_bounds__(256) chol_df_kernel(double *__restrict__ M, int n, int ld, int nrows,
+                                                      int *__restrict__ flags, double *__restrict__ Dinv,
+                                                      unsigned *__restrict__ ready, int *__restrict__ abort) {
+    __shared__ double T[NB][NB + 1], Li[NB][NB + 1], Lj[NB][NB + 1];
+    __shared__ int failed_at, ok_sh;
+    const int tid = threadIdx.x;
+    const int nbc = (n + NB - 1) / NB, nbr = (nrows + NB - 1) / NB;
+    int t = 0;
+    for (int j = 0; j < nbc; ++j) {
+        for (int i = j; i < nbr; ++i, ++t) {
+            if (t % (int)gridDim.x != (int)blockIdx.x) continue;
+            const int r0 = NB * i, c0 = NB * j;
+            const int nr = min(NB, nrows - r0), nc = min(NB, n - c0);
+            for (int e = tid; e < NB * NB; e += 256) {
+                const int r = e % NB, c = e / NB;
+                T[r][c] = (r < nr && c < nc && (i != j || c <= r)) ? __ldcg(M + (size_t)(c0 + c) * ld + r0 + r) : 0.0;
+            }
+            for (int k = 0; k < j; ++k) {
+                const int kc = NB * k;
+                if (!df_wait(ready + nbc + (size_t)k * nbr + i, abort, &ok_sh) ||
+                    !df_wait(ready + nbc + (size_t)k * nbr + j, abort, &ok_sh))
+                    goto fail;
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int r = e % NB, kk = e / NB;
+                    Li[r][kk] = r < nr ? __ldcg(M + (size_t)(kc + kk) * ld + r0 + r) : 0.0;
+                    Lj[r][kk] = r < nc ? __ldcg(M + (size_t)(kc + kk) * ld + c0 + r) : 0.0;
+                }
+                __syncthreads();
+                const int r = tid % NB;
+                for (int cc = tid / NB; cc < NB; cc += 8) {
+                    if (r >= nr || cc >= nc || (i == j && cc > r)) continue;
+                    double acc = 0.0;
+#pragma unroll 8
+                    for (int kk = 0; kk < NB; ++kk) acc = fma(Li[r][kk], Lj[cc][kk], acc);
+                    T[r][cc] = T[r][cc] - acc;
+                }
+                __syncthreads();
+            }
+            if (i == j) {
+                // rows >= n of this tile (the right-hand side) wait in Lj
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int r = e % NB, c = e / NB;
+                    Lj[r][c] = (r >= nc && r < nr && c < nc) ? T[r][c] : 0.0;
+                    if (r >= nc || c > r) T[r][c] = 0.0;
+                }
+                __syncthreads();
+                factor_invert_block(T, Li, nc, c0, flags, &failed_at);
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int r = e / NB, c = e % NB;
+                    if (r < nc && c <= r) M[(size_t)(c0 + c) * ld + c0 + r] = T[r][c];
+                    Dinv[(size_t)j * NB * NB + e] = Li[r][c];
+                }
+                // the right-hand-side row: x_c = sum_{t <= c} Di[c][t] a_t
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int c = e / NB, r = e % NB;
+                    if (r < nc || r >= nr || c >= nc) continue;
+                    double x = 0.0;
+                    for (int q = 0; q <= c; ++q) x = fma(Li[c][q], Lj[r][q], x);
+                    M[(size_t)(c0 + c) * ld + r0 + r] = x;
+                }
+                df_publish(ready + j);
+                if (nr > nc) df_publish(ready + nbc + (size_t)j * nbr + i);
+            } else {
+                if (!df_wait(ready + j, abort, &ok_sh)) goto fail;
+                for (int e = tid; e < NB * NB; e += 256) Li[e / NB][e % NB] = __ldcg(Dinv + (size_t)j * NB * NB + e);
+                __syncthreads();
+                const int c = tid / 8;
+                for (int r = tid % 8; r < NB; r += 8) {
+                    if (c >= nc || r >= nr) continue;
+                    double x = 0.0;
+                    for (int q = 0; q <= c; ++q) x = fma(Li[c][q], T[r][q], x);
+                    M[(size_t)(c0 + c) * ld + r0 + r] = x;
+                }
+                df_publish(ready + nbc + (size_t)j * nbr + i);
+            }
+            __syncthreads();
+        }
+    }
+    return;
+fail:
+    if (tid == 0) {
+        *(volatile int *)abort = 1;
+        atomicExch(flags, -1);
+        atomicExch(flags + 1, CHOL_WAIT_CODE | (int)blockIdx.x);
+    }
+}
+
+// CTAs of the data-flow factorization on the current device (one per SM at
+// most, all resident), or 0 when a cooperative launch is not possible.
+// Computed per device and published once, as for the backward sweep.
+int df_capacity() {
+    constexpr int kDevices = 64;
+    static std::atomic<int> cap_plus1[kDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (dev < 0 || dev >= kDevices) return 0;
+    int c = cap_plus1[dev].load(std::memory_order_acquire);
+    if (c == 0) {
+        int coop = 0, per_sm = 0, sms = 0, cap = 0;
+        if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_df_kernel, 256, 0) != cudaSuccess)
+            cudaGetLastError();
+        else if (coop && per_sm > 0)
+            cap = sms;
+        c = cap + 1;
+        cap_plus1[dev].store(c, std::memory_order_release);
+    }
+    return c - 1;
+}
+
+int g_chol_path = 0;  // 0: data flow when possible, 1: multi-launch, 2: data flow only
+
+// Words of the ready list for order n (with the right-hand-side row): one per
+// diagonal block, one per tile, one abort word.
+size_t df_ready_words(int n, int has_b) {
+    const size_t nbc = (size_t)(n + NB - 1) / NB, nbr = (size_t)(n + has_b + NB - 1) / NB;
+    return nbc + nbc * nbr + 1;
+}
+
 // Enqueues the whole factorization (and the solve when has_b) on `st`, with
 // Dinv holding ceil(n/32) blocks of 32x32 doubles. Row n of M (the
 // right-hand side) is scratch on return: which backward sweep runs decides
@@ -306,9 +496,45 @@ int coop_backsolve_ctas(int n) {
     return g <= c - 1 ? g : 0;
 }
 
-int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Dinv, cudaStream_t st) {
+int chol_enqueue_panels(double *d_M, int n, int ld, int nrows, int *flags, double *Dinv, cudaStream_t st);
+int chol_enqueue_backsolve(double *d_M, int n, int ld, double *d_x, double *Dinv, cudaStream_t st);
+
+// ready: the data-flow path's list (df_ready_words words), or NULL for the
+// multi-launch path.
+int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Dinv, cudaStream_t st,
+                 unsigned *ready = nullptr) {
     const int has_b = d_x != nullptr;
     const int nrows = n + has_b;
+    const int G = ready && g_chol_path != 1 ? df_capacity() : 0;
+    if (G > 0) {
+        // one cooperative launch of the data-flow factorization
+        const size_t words = df_ready_words(n, has_b);
+        cudaError_t e = cudaMemsetAsync(ready, 0, words * sizeof(unsigned), st);
+        const int nbc = (n + NB - 1) / NB, nbr = (nrows + NB - 1) / NB;
+        const int tasks = nbc * (2 * nbr - nbc + 1) / 2;
+        int grid = std::min(G, tasks);
+        int *abort = (int *)(ready + words - 1);
+        void *args[] = {&d_M, &n, &ld, (void *)&nrows, &flags, &Dinv, &ready, &abort};
+        if (e == cudaSuccess)
+            e = cudaLaunchCooperativeKernel((const void *)chol_df_kernel, dim3(grid), dim3(256), args, 0, st);
+        if (e != cudaSuccess) {
+            irwls_set_error(-2, "CUDA error in chol_df (cooperative): %s", cudaGetErrorString(e));
+            return -2;
+        }
+        irwls_count_launch(1);
+    } else if (g_chol_path == 2) {
+        irwls_set_error(-2, "the data-flow Cholesky needs a cooperative launch");
+        return -2;
+    } else {
+        const int rc = chol_enqueue_panels(d_M, n, ld, nrows, flags, Dinv, st);
+        if (rc) return rc;
+    }
+    return has_b ? chol_enqueue_backsolve(d_M, n, ld, d_x, Dinv, st) : 0;
+}
+
+// The multi-launch factorization: per panel a solve launch and an update
+// launch (whose tile (0, 0) factors the next diagonal block).
+int chol_enqueue_panels(double *d_M, int n, int ld, int nrows, int *flags, double *Dinv, cudaStream_t st) {
     chol_factor0_kernel<<<1, 256, 0, st>>>(d_M, n, ld, flags, Dinv);
     IRWLS_LAUNCH_CHECK("chol_factor0");
     for (int k0 = 0; k0 < n; k0 += NB) {
@@ -325,7 +551,12 @@ int chol_enqueue(double *d_M, int n, int ld, double *d_x, int *flags, double *Di
             IRWLS_LAUNCH_CHECK("chol_update");
         }
     }
-    if (has_b) {
+    return 0;
+}
+
+// The backward sweep L^T x = z (z in row n of M).
+int chol_enqueue_backsolve(double *d_M, int n, int ld, double *d_x, double *Dinv, cudaStream_t st) {
+    {
         const int g = coop_backsolve_ctas(n);
         if (g > 0) {
             void *args[] = {&d_M, &n, &ld, &Dinv, &d_x};
@@ -384,14 +615,21 @@ extern "C" int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_
     // factored diagonal blocks: the context's grow-only scratch slot 0
     double *diag = (double *)irwls_ctx_scratch(0, (size_t)npanel * NB * NB * sizeof(double));
     if (!diag) return -3;
+    // ready list of the data-flow path: the context's grow-only slot 3
+    unsigned *ready = (unsigned *)irwls_ctx_scratch(3, df_ready_words(n, d_x != nullptr) * sizeof(unsigned));
+    if (!ready) return -3;
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_CHOL);
-    int rc = chol_enqueue(d_M, n, ld, d_x, flags, diag, irwls_stream());
+    int rc = chol_enqueue(d_M, n, ld, d_x, flags, diag, irwls_stream(), ready);
     if (rc) return rc;
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_CHOL);
     return 0;
 }
 
 extern "C" int irwls_chol_sweep_ctas(int n) { return coop_backsolve_ctas(n); }
+
+// Test hook: 0 = the data-flow factorization where a cooperative launch is
+// possible (default), 1 = the multi-launch factorization, 2 = data flow only.
+extern "C" void irwls_debug_chol_path(int mode) { g_chol_path = mode >= 0 && mode <= 2 ? mode : 0; }
 
 extern "C" int irwls_dev_pivot_status(int *info) {
     *info = 0;
@@ -443,14 +681,19 @@ extern "C" int irwls_dev_gemv(const double *d_A, const double *d_v, double *d_ou
 // file-scope array below, which every GPU that loads this library holds until
 // the process exits.
 //
-// The scratch keeps the inverted 32x32 diagonal blocks (one per panel) and
-// the pivot status word, which sizes it for matrices of order up to
-// IRWLS_NOALLOC_MAX_ORDER (4096: 1 MiB of blocks).
+// The scratch keeps the inverted 32x32 diagonal blocks (one per panel), the
+// status words and the ready list of the data-flow factorization, which
+// sizes it for matrices of order up to IRWLS_NOALLOC_MAX_ORDER (4096: 1 MiB
+// of blocks and 65 KiB of ready words, about 1.06 MiB in all).
 // ---------------------------------------------------------------------------
 #define IRWLS_NOALLOC_MAX_ORDER 4096
 #define IRWLS_NOALLOC_PANELS (IRWLS_NOALLOC_MAX_ORDER / NB)
+// ready words of the data-flow factorization at the largest order (with the
+// right-hand-side row), rounded up to whole doubles
+#define IRWLS_NOALLOC_READY (IRWLS_NOALLOC_PANELS + IRWLS_NOALLOC_PANELS * (IRWLS_NOALLOC_PANELS + 1) + 1)
 
-static __device__ __align__(256) double g_noalloc_scratch[IRWLS_NOALLOC_PANELS * NB * NB + 32];
+static __device__ __align__(256) double
+    g_noalloc_scratch[IRWLS_NOALLOC_PANELS * NB * NB + 32 + (IRWLS_NOALLOC_READY + 1) / 2];
 
 #define IRWLS_NOALLOC_DEVICES 64
 static double *g_noalloc_addr[IRWLS_NOALLOC_DEVICES];  // device address of the array, per device
@@ -495,6 +738,7 @@ extern "C" int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double
     }
     double *diag = g_noalloc_addr[dev];
     int *flags = (int *)(diag + IRWLS_NOALLOC_PANELS * NB * NB);
+    unsigned *ready = (unsigned *)(diag + IRWLS_NOALLOC_PANELS * NB * NB + 32);
     cudaStream_t st = (cudaStream_t)stream;
     // the pivot status must start at zero; the diagonal blocks are fully
     // rewritten before they are read
@@ -511,7 +755,7 @@ extern "C" int irwls_chol_solve_noalloc(double *d_M, int n, int ld, const double
         }
     }
     // order <= 4096: the backward sweep's vector fits the default 48 KiB
-    const int rc = chol_enqueue(d_M, n, ld, d_x, flags, diag, st);
+    const int rc = chol_enqueue(d_M, n, ld, d_x, flags, diag, st, ready);
     if (rc) return rc;
     if (d_info && (e = cudaMemcpyAsync(d_info, flags, sizeof(int), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) {
         irwls_set_error(-2, "irwls_chol_solve_noalloc: %s", cudaGetErrorString(e));

@@ -876,10 +876,12 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
             T = Tn;
         }
     }
-    if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    // after the barrier: every role has finished, so a timeout any of them
+    // met is in abort_flag
+    if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
 }
 
@@ -1110,121 +1112,353 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
 // ===========================================================================
 // Precision form of full IRWLS: the error update over every training row,
 //   e_i <- (e_i - sum_j cb_j k(x_i, x_{b_j})) - tail,   j over the working set,
-// with the kernel values from dot products on the tensor cores: each value is
-// split into three bf16 pieces hi + mid + lo (24 significant bits) and the six
-// piece products down to 2^-24 are accumulated in FP32, then
+// with the kernel values from dot products on the tensor cores, then
 // k = exp(-gamma (q_i + q_j - 2 x_i . x_j)) (RBF, the norm form) or x_i . x_j
-// (linear). The error update is incremental, so its per-entry error has to
-// stay near FP32 rounding: the two-piece (16-bit) split's 1e-5 moved the
-// errors across the classification threshold within a few updates. The
-// dataset is kept once per training as a dense three-piece copy (K padded to
-// 64); the working-set rows are gathered into B before each update. A CTA
-// owns 128 rows and walks the working set in passes of 128 columns through
-// one tensor-memory accumulator; each row's sum is Kahan-compensated FP32 in
-// a fixed column order.
+// (linear). The update is incremental, so its per-entry error has to stay
+// near FP32 rounding (a two-piece, 16-bit split moved errors across the
+// classification threshold within a few updates). Two operand forms:
+//  - P = 3 pieces: every value (rounded to FP32) is split into hi + mid + lo
+//    bf16 (24 significant bits) and the six piece products down to 2^-24 of
+//    the product are accumulated in FP32;
+//  - P = 1 piece: when every value of the set is exactly a bf16 after a scale
+//    S = 1 (binary data, small integers, values with <= 8 significant bits) or
+//    S = 255 (8-bit data k / 255), the scaled values are the operands and
+//    every product is exact; the dot product is multiplied by 1 / S^2.
+// Both keep only the FP32 accumulation error.
+//
+// Layout: the dataset is copied once per training into a blocked array in
+// which every (128-row tile, 32-column block) holds its P pieces as the
+// shared-memory image of one tcgen05 operand stage (core matrices of 8 rows
+// x 16 bytes, 128 bytes apart along K and 512 bytes apart along rows), and
+// the working-set rows are gathered before each update into the same layout
+// in 256-row chunks. A stage is then one bulk copy of the tile's block and P
+// bulk copies of the chunk's rows.
+//
+// Kernel: persistent, one CTA per SM walking (tile, chunk) items; warp 0
+// streams stages through an NS-deep ring, one thread of warp 1 issues the
+// MMAs (M = 128 rows, N = the chunk's columns rounded to 16, K = 16) into
+// one of two 256-column FP32 accumulators in tensor memory, and warps 4-11
+// run the epilogue of the previous item: warp w reads lanes 32 (w % 4) ...
+// (its rows), warps 4-7 the chunk's first 128 columns and warps 8-11 the
+// rest, and each thread keeps a Kahan-compensated FP32 sum of its row over
+// its columns in a fixed order; the two halves are added in FP64 at the end
+// of the tile. Each A tile is read from memory once per 256 working-set
+// columns. Every wait is bounded; on a timeout the device flag word 1 is
+// set, every role leaves its loop, and no copy or MMA is in flight when the
+// tensor memory is released.
 // ===========================================================================
 
 namespace {
 
-constexpr int KR_BN = 128, KR_P = 3, KR_BK = 32, KR_NS = 4;
+constexpr int RS_BM = 128, RS_BN = 256, RS_BK = 32;
+constexpr int RS_APIECE = RS_BM * RS_BK, RS_BPIECE = RS_BN * RS_BK;  // elements per piece of a stage
+constexpr int RS_EPI = 256;                                          // epilogue threads (warps 4-11)
+constexpr int RS_THREADS = 128 + RS_EPI;
+constexpr long long RS_WAIT_DEFAULT = 1LL << 26;
 
-struct Pieces {
-    const __nv_bfloat16 *p[KR_P];
+// element offset of row r, column c (c < 32) inside one piece of a stage
+__device__ __forceinline__ size_t rs_core(int r, int c) {
+    return (size_t)(r >> 3) * 256 + (c >> 3) * 64 + (r & 7) * 8 + (c & 7);
+}
+
+template <int P>
+struct RsStage {
+    static constexpr int A_BYTES = P * RS_APIECE * 2;
+    static constexpr int B_BYTES = P * RS_BPIECE * 2;
+    static constexpr int BYTES = A_BYTES + B_BYTES;
 };
 
-__global__ void __launch_bounds__(TC_THREADS) tc_kernel_rowsum_kernel(
-    Pieces Ap, int lda, int M, const float *__restrict__ qa, Pieces Bp, int ldb, const int *__restrict__ d_n, int nmax,
-    const float *__restrict__ qb, const double *__restrict__ cb, int kst, int rbf, float ng,
-    const double *init, const double *__restrict__ tail, double *out, int *flags) {
-    extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ __align__(8) uint64_t mbar[KR_NS];
-    __shared__ uint32_t tmem_slot;
-    __shared__ float qs[KR_BN], cs[KR_BN];
-    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
-    const int N = min(*d_n, nmax);  // the gathered rows held in B
-    const int m0 = blockIdx.x * TC_BM;
-    const int row = m0 + threadIdx.x;
-    const float qi = row < M ? qa[row] : 0.f;
-    float sum = 0.f, comp = 0.f;
-    tc_setup_ring<KR_BN, KR_NS>(mbar, &tmem_slot);
-    const uint32_t tmem = tmem_slot;
-    uint32_t used[KR_NS] = {};
-    bool ok = true;
-    for (int n0 = 0; n0 < N && ok; n0 += KR_BN) {
-        for (int t = threadIdx.x; t < KR_BN; t += TC_THREADS) {
-            const int j = n0 + t;
-            qs[t] = j < N ? qb[j] : 0.f;
-            cs[t] = j < N ? (float)cb[j] : 0.f;
-        }
-        ok = tc_mainloop_ring<KR_BN, KR_P, KR_BK, KR_NS>(smem, mbar, tmem, Ap.p, lda, m0, M, Bp.p, ldb, n0, N, 0, kst,
-                                                         used);
-        if (!ok) break;
-        const int ncol = min(KR_BN, N - n0);
-        for (int c0 = 0; c0 < ncol; c0 += 8) {
-            float v[8];
-            tc_ld8(tmem, c0, v);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int c = c0 + j;
-                if (c < ncol) {
-                    const float k = rbf ? expf(ng * fmaxf(qi + qs[c] - 2.f * v[j], 0.f)) : v[j];
-                    const float y = __fsub_rn(__fmul_rn(cs[c], k), comp);
-                    const float t = __fadd_rn(sum, y);
-                    comp = __fsub_rn(__fsub_rn(t, sum), y);
-                    sum = t;
-                }
-            }
-        }
-        // the next pass overwrites the accumulator and qs/cs
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
-        __syncthreads();
-    }
-    if (!ok && threadIdx.x == 0) atomicExch(flags + 1, 1);
-    if (ok && row < M) out[row] = __dsub_rn(__dsub_rn(init[row], (double)sum - (double)comp), tail ? tail[0] : 0.0);
-    tc_teardown<KR_BN>(tmem);
+template <int P>
+constexpr int rs_stages() {
+    return P == 1 ? 8 : 3;  // 192 KB and 216 KB of ring
 }
 
-// B rows j < *d_n: the dense split rows idx[j] of the set, and their norms.
-__global__ void tc_gather_rows_kernel(Pieces X, int ld, const float *__restrict__ q, const int *__restrict__ idx,
-                                      const int *__restrict__ d_n, int nmax, __nv_bfloat16 *B0, __nv_bfloat16 *B1,
-                                      __nv_bfloat16 *B2, float *qb) {
-    const int n = min(*d_n, nmax);
-    const int per = ld / 8;  // 16-byte pieces per row
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * per;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(t / per), c = (int)(t % per);
-        const size_t src = (size_t)idx[j] * ld + (size_t)c * 8, dst = (size_t)j * ld + (size_t)c * 8;
-        *(uint4 *)(B0 + dst) = *(const uint4 *)(X.p[0] + src);
-        *(uint4 *)(B1 + dst) = *(const uint4 *)(X.p[1] + src);
-        *(uint4 *)(B2 + dst) = *(const uint4 *)(X.p[2] + src);
-        if (c == 0) qb[j] = q[idx[j]];
+__device__ __forceinline__ bool mbar_wait_lim(uint32_t mbar, uint32_t parity, long long limit) {
+    uint32_t done = 0;
+    for (long long it = 0; it < limit && !done; ++it) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity));
     }
+    return done != 0;
 }
 
-// Three-piece split of the first `cols` columns of a row-major FP64 matrix
-// (rounded to FP32 first), zero up to ldo.
-__global__ void split3_kernel(const double *__restrict__ X, long long rows, int cols, int ldx, __nv_bfloat16 *p0,
-                              __nv_bfloat16 *p1, __nv_bfloat16 *p2, int ldo) {
-    const long long total = rows * (long long)ldo;
+// bad[0] |= some value is not exactly a bf16; bad[1] |= some value is not
+// k / 255 for an integer |k| <= 256 (so that 255 x is exactly a bf16).
+__global__ void rs_quant_check_kernel(const double *__restrict__ X, int rows, int cols, int ldx, int *bad) {
+    int b0 = 0, b1 = 0;
+    const long long total = (long long)rows * cols;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const long long r = t / ldo;
-        const int c = (int)(t % ldo);
-        const float x = c < cols ? __double2float_rn(X[r * ldx + c]) : 0.f;
-        const __nv_bfloat16 h = __float2bfloat16_rn(x);
-        const float r1 = x - __bfloat162float(h);
-        const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-        p0[t] = h;
-        p1[t] = m;
-        p2[t] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+        const double v = X[(t / cols) * ldx + t % cols];
+        const float f = __double2float_rn(v);
+        if ((double)f != v || __bfloat162float(__float2bfloat16_rn(f)) != f) b0 = 1;
+        const double k = rint(v * 255.0);
+        if (!(fabs(k) <= 256.0) || k / 255.0 != v) b1 = 1;
     }
+    b0 = __any_sync(0xffffffffu, b0);
+    b1 = __any_sync(0xffffffffu, b1);
+    if ((threadIdx.x & 31) == 0) {
+        if (b0) atomicOr(bad, 1);
+        if (b1) atomicOr(bad + 1, 1);
+    }
+}
+
+// The blocked P-piece copy of rows x cols of a row-major FP64 matrix, scaled
+// by `scale`; rows padded to tiles of 128 and columns to kbn blocks of 32
+// with zeros. P = 3: hi, mid, lo of the FP32 value; P = 1: the value itself
+// (exact by the check above).
+template <int P>
+__global__ void rs_split_kernel(const double *__restrict__ X, int rows, int cols, int ldx, int kbn, double scale,
+                                __nv_bfloat16 *__restrict__ A) {
+    const int ld = kbn * RS_BK;
+    const long long total = (long long)((rows + RS_BM - 1) / RS_BM) * RS_BM * ld;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(t / ld), c = (int)(t % ld);
+        const double v = (r < rows && c < cols) ? X[(size_t)r * ldx + c] * scale : 0.0;
+        const size_t base = ((size_t)(r >> 7) * kbn + (c >> 5)) * P * RS_APIECE + rs_core(r & 127, c & 31);
+        if (P == 1) {
+            A[base] = __float2bfloat16_rn(__double2float_rn(v));
+        } else {
+            const float x = __double2float_rn(v);
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            const float r1 = x - __bfloat162float(h);
+            const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+            A[base] = h;
+            A[base + RS_APIECE] = m;
+            A[base + 2 * RS_APIECE] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+        }
+    }
+}
+
+// Working-set row j < *d_n becomes row j of the blocked B (256-row chunks):
+// its 16-byte groups copied from the blocked A row idx[j]; qb[j] = q[idx[j]].
+template <int P>
+__global__ void rs_gather_kernel(const __nv_bfloat16 *__restrict__ A, int kbn, const float *__restrict__ q,
+                                 const int *__restrict__ idx, const int *__restrict__ d_n, int nmax,
+                                 __nv_bfloat16 *__restrict__ B, float *__restrict__ qb) {
+    const int n = min(*d_n, nmax);
+    const long long total = (long long)n * kbn * P * 4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(t & 3);
+        long long rest = t >> 2;
+        const int p = (int)(rest % P);
+        rest /= P;
+        const int k = (int)(rest % kbn);
+        const int j = (int)(rest / kbn);
+        const int i = idx[j];
+        const size_t src = ((size_t)(i >> 7) * kbn + k) * P * RS_APIECE + (size_t)p * RS_APIECE + rs_core(i & 127, 8 * g);
+        const size_t dst = ((size_t)(j >> 8) * kbn + k) * P * RS_BPIECE + (size_t)p * RS_BPIECE + rs_core(j & 255, 8 * g);
+        *(uint4 *)(B + dst) = *(const uint4 *)(A + src);
+        if (k == 0 && p == 0 && g == 0) qb[j] = q[i];
+    }
+}
+
+// MODE 0 (row sums): out_i = (init_i - sum_j cb_j k_ij) - tail[0].
+// MODE 1 (prediction): out_i = bias + sum_j cb_j k_ij, or its sign (>= 0 ->
+// +1) when `hard`.
+template <int P, int NS, int MODE>
+__global__ void __launch_bounds__(RS_THREADS, 1) tc_rowsum_ws_kernel(
+    const __nv_bfloat16 *__restrict__ A, int M, int kbn, const float *__restrict__ qa,
+    const __nv_bfloat16 *__restrict__ B, const int *__restrict__ d_n, int nmax, const float *__restrict__ qb,
+    const double *__restrict__ cb, int rbf, float ng, float dscale, const double *init,
+    const double *__restrict__ tail, double *out, double bias, int hard, int *flags, long long wait_limit,
+    int stall) {
+    using S = RsStage<P>;
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t full[NS], empty[NS], accf[2], acce[2], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    __shared__ float2 half_sum[RS_BM];
+    unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int N = max(0, min(*d_n, nmax));
+    const int nch = (N + RS_BN - 1) / RS_BN;
+    const int ntiles = (M + RS_BM - 1) / RS_BM;
+    const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int items = my_tiles * nch;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NS; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], RS_EPI / 32);
+        }
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+        abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(2 * RS_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const uint32_t tmem = tmem_slot;
+    // columns of chunk h, rounded up to the MMA's N granularity
+    auto chunk_rows = [&](int h) { return ((min(RS_BN, N - h * RS_BN) + 15) / 16) * 16; };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint32_t base = smem_u32(smem);
+            int u = 0;
+            for (int it = 0; it < items && !abort_flag; ++it) {
+                const int j = it / nch, h = it % nch;
+                const size_t tile = (size_t)blockIdx.x + (size_t)j * gridDim.x;
+                const uint32_t bbytes = (uint32_t)chunk_rows(h) * 64u;
+                for (int k = 0; k < kbn; ++k, ++u) {
+                    const int slot = u % NS;
+                    if (u >= NS && !mbar_wait_lim(smem_u32(&empty[slot]), (uint32_t)(u / NS - 1) & 1u, wait_limit))
+                        abort_flag = 1;
+                    if (abort_flag) break;
+                    const uint32_t sb = base + slot * S::BYTES, fb = smem_u32(&full[slot]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb),
+                                 "r"((uint32_t)S::A_BYTES + P * bbytes));
+                    bulk_g2s(sb, A + (tile * kbn + k) * P * RS_APIECE, S::A_BYTES, fb);
+                    for (int p = 0; p < P; ++p)
+                        bulk_g2s(sb + S::A_BYTES + p * RS_BPIECE * 2,
+                                 B + (((size_t)h * kbn + k) * P + p) * RS_BPIECE, bbytes, fb);
+                }
+            }
+            // no copy is left in flight: the last NS stages issued have landed
+            for (int v = u > NS ? u - NS : 0; v < u; ++v)
+                if (!mbar_wait_lim(smem_u32(&full[v % NS]), (uint32_t)(v / NS) & 1u, wait_limit)) abort_flag = 1;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int u = 0;
+            bool issued = false;  // tcgen05.commit only follows issued MMAs
+            for (int it = 0; it < items && !abort_flag; ++it) {
+                const int b = it & 1, h = it % nch;
+                if (it >= 2 && !mbar_wait_lim(smem_u32(&acce[b]), (uint32_t)(it / 2 - 1) & 1u, wait_limit)) {
+                    abort_flag = 1;
+                    break;
+                }
+                const uint32_t idesc = tc_idesc(RS_BM, chunk_rows(h));
+                for (int k = 0; k < kbn; ++k, ++u) {
+                    const int slot = u % NS;
+                    if (!mbar_wait_lim(smem_u32(&full[slot]), (uint32_t)(u / NS) & 1u, wait_limit)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    if (stall) {
+                        // test mode: no MMA is issued and the accumulator is
+                        // never completed, so the epilogue's wait runs out
+                        mbar_arrive(&empty[slot]);
+                        continue;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::);
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                    const uint32_t sa = smem_u32(smem + slot * S::BYTES), sbb = sa + S::A_BYTES;
+                    bool first = k == 0;
+#pragma unroll
+                    for (int kk = 0; kk < RS_BK / 16; ++kk)
+#pragma unroll
+                        for (int pi = 0; pi < P; ++pi)
+#pragma unroll
+                            for (int pj = 0; pj < P - pi; ++pj) {
+                                mma_bf16(tmem + b * RS_BN, tc_desc_sbo(sa + pi * RS_APIECE * 2 + kk * 256, 512),
+                                         tc_desc_sbo(sbb + pj * RS_BPIECE * 2 + kk * 256, 512), idesc, first ? 0u : 1u);
+                                first = false;
+                            }
+                    tc_commit(&empty[slot]);
+                    issued = true;
+                }
+                if (!abort_flag && !stall) tc_commit(&accf[b]);
+            }
+            // every MMA issued has completed before the tensor memory is released
+            if (issued) tc_commit(&done);
+            else mbar_arrive(&done);
+            if (!mbar_wait_lim(smem_u32(&done), 0u, wait_limit)) abort_flag = 1;
+        }
+        __syncwarp();
+    } else if (warp >= 4) {
+        const int ew = warp & 3, g = (warp - 4) >> 2, r = 32 * ew + lane;
+        int it = 0;
+        bool aborted = false;
+        for (int j = 0; j < my_tiles && !aborted; ++j) {
+            const int row = ((int)blockIdx.x + j * (int)gridDim.x) * RS_BM + r;
+            const float qi = row < M ? qa[row] : 0.f;
+            float sum = 0.f, comp = 0.f;
+            for (int h = 0; h < nch; ++h, ++it) {
+                const int b = it & 1;
+                const bool acc_ok = mbar_wait_lim(smem_u32(&accf[b]), (uint32_t)(it / 2) & 1u, wait_limit);
+                // one decision for all epilogue threads (an OR over them)
+                const int bad = (!acc_ok || abort_flag) ? 1 : 0;
+                int any;
+                asm volatile(
+                    "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.or.pred q, 1, %2, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+                    : "=r"(any)
+                    : "r"(bad), "r"(RS_EPI));
+                if (any) {
+                    abort_flag = 1;
+                    aborted = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                const int c_base = h * RS_BN + 128 * g;
+                const int ncol = min(128, N - c_base);
+                for (int c0 = 0; c0 < ncol; c0 += 8) {
+                    float v[8];
+                    tc_ld8_lanes(tmem + b * RS_BN + 128 * g, 32 * ew, c0, v);
+#pragma unroll
+                    for (int jj = 0; jj < 8; ++jj) {
+                        const int c = c0 + jj;
+                        if (c < ncol) {
+                            const float dot = v[jj] * dscale;
+                            const float k =
+                                rbf ? expf(ng * fmaxf(qi + __ldg(qb + c_base + c) - 2.f * dot, 0.f)) : dot;
+                            const float y = __fsub_rn(__fmul_rn((float)__ldg(cb + c_base + c), k), comp);
+                            const float t = __fadd_rn(sum, y);
+                            comp = __fsub_rn(__fsub_rn(t, sum), y);
+                            sum = t;
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+                if (lane == 0) mbar_arrive(&acce[b]);  // this warp's reads of accumulator b are done
+            }
+            if (aborted) break;
+            // the two column halves of the row, added in FP64 in a fixed order
+            if (g == 1) half_sum[r] = make_float2(sum, comp);
+            asm volatile("bar.sync 2, %0;\n" ::"r"(RS_EPI));
+            if (g == 0 && row < M) {
+                const float2 o = half_sum[r];
+                const double tot = ((double)sum - (double)comp) + ((double)o.x - (double)o.y);
+                if (MODE == 0) {
+                    out[row] = __dsub_rn(__dsub_rn(init[row], tot), tail ? tail[0] : 0.0);
+                } else {
+                    const double f = __dadd_rn(bias, tot);
+                    out[row] = hard ? (f >= 0.0 ? 1.0 : -1.0) : f;
+                }
+            }
+            asm volatile("bar.sync 2, %0;\n" ::"r"(RS_EPI));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    // after the barrier: every role has finished, so a timeout any of them
+    // met is in abort_flag
+    if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * RS_BN));
 }
 
 struct TcSet {
-    __nv_bfloat16 *X[KR_P], *B[KR_P];
+    __nv_bfloat16 *A, *B;
     float *q, *qb;
-    int rows, ld, wmax, rbf;
-    float ng;
+    int *bad;   // two words: the operand-form check, then the gathered-row count of a prediction
+    int *nbuf;
+    int rows, kbn, wmax, rbf, pieces;
+    float ng, dscale;
     double kbound;
 };
 
@@ -1242,32 +1476,79 @@ __global__ void __launch_bounds__(1024) max_q_kernel(const float *__restrict__ q
     if (threadIdx.x == 0) out[0] = red[0];
 }
 
+long long g_rs_wait_limit = RS_WAIT_DEFAULT;
+int g_rs_stall = 0;
+int g_rs_last_pieces = 0;
+
 }  // namespace
 
-// Dense split copy of rows 0..rows-1 of a device set for the precision form
-// of full IRWLS, with room for `wmax` gathered working-set rows.
-extern "C" void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax) {
+// Test hook of the bounded waits of the full-IRWLS error update (no
+// counterpart in the reference): the poll limit of every wait (<= 0: the
+// default 2^26) and a stall switch with which the MMA thread issues nothing
+// and never completes an accumulator, so that the epilogue's wait runs out
+// with no copy or MMA in flight.
+extern "C" void irwls_debug_tc_wait(long long limit, int stall) {
+    g_rs_wait_limit = limit > 0 ? limit : RS_WAIT_DEFAULT;
+    g_rs_stall = stall ? 1 : 0;
+}
+// Operand pieces of the last precision-form full-IRWLS set (1 or 3).
+extern "C" int irwls_last_tc_pieces(void) { return g_rs_last_pieces; }
+
+namespace {
+// Operand-form flags of rows 0..rows-1 of a set: bad[0] (not every value is
+// a bf16), bad[1] (not every value is k / 255 with |k| <= 256).
+int rs_check(const irwls_dev_set *X, int rows, int *d_bad, int bad[2]) {
+    bad[0] = bad[1] = 0;
+    if (rows <= 0) return 0;
+    int rc = irwls_dev_memset(d_bad, 0, 2 * sizeof(int));
+    const long long total = (long long)rows * X->width;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 8 * 1024));
+    rs_quant_check_kernel<<<blocks, 256, 0, irwls_stream()>>>(X->X, rows, X->width, X->ld, d_bad);
+    irwls_count_launch(1);
+    rc |= irwls_dev_d2h(bad, d_bad, 2 * sizeof(int));
+    rc |= irwls_dev_sync();
+    return rc;
+}
+
+// The operand form for flags of one or two sets: 1 piece with scale 1 or
+// 255 when every value qualifies, else 3 pieces with scale 1.
+void rs_form(const int *bad, int n, int *pieces, double *scale) {
+    int b0 = 0, b1 = 0;
+    for (int k = 0; k < n; ++k) {
+        b0 |= bad[2 * k];
+        b1 |= bad[2 * k + 1];
+    }
+    *pieces = (!b0 || !b1) ? 1 : 3;
+    *scale = !b0 ? 1.0 : (!b1 ? 255.0 : 1.0);
+}
+
+// The blocked copy of rows 0..rows-1 in a given operand form, kbn blocks of
+// 32 columns, with room for wmax gathered rows.
+TcSet *rs_set_make(const irwls_dev_set *X, int rows, int wmax, int kbn, int P, double scale) {
     TcSet *t = (TcSet *)calloc(1, sizeof(TcSet));
     if (!t) return nullptr;
     t->rows = rows;
-    t->ld = ceil_div(X->width, TC_BK) * TC_BK;
+    t->kbn = kbn;
     t->wmax = wmax;
     t->rbf = X->mode != IRWLS_K_LINEAR;
     t->ng = (float)X->neg_gamma;
-    int rc = 0;
-    const size_t xb = (size_t)(rows > 0 ? rows : 1) * t->ld * sizeof(__nv_bfloat16);
-    const size_t bb = (size_t)(wmax > 0 ? wmax : 1) * t->ld * sizeof(__nv_bfloat16);
-    for (int k = 0; k < KR_P; ++k) {
-        rc |= irwls_dev_malloc((void **)&t->X[k], xb);
-        rc |= irwls_dev_malloc((void **)&t->B[k], bb);
-    }
+    t->pieces = P;
+    t->dscale = (float)(1.0 / (scale * scale));
+    int rc = irwls_dev_malloc((void **)&t->bad, 4 * sizeof(int));
+    t->nbuf = t->bad + 2;
+    const size_t ab = (size_t)ceil_div(rows > 0 ? rows : 1, RS_BM) * RS_BM * t->kbn * RS_BK * P * sizeof(__nv_bfloat16);
+    const size_t bb = (size_t)ceil_div(wmax > 0 ? wmax : 1, RS_BN) * RS_BN * t->kbn * RS_BK * P * sizeof(__nv_bfloat16);
+    rc |= irwls_dev_malloc((void **)&t->A, ab);
+    rc |= irwls_dev_malloc((void **)&t->B, bb);
     rc |= irwls_dev_malloc((void **)&t->q, (size_t)(rows > 0 ? rows : 1) * sizeof(float));
     rc |= irwls_dev_malloc((void **)&t->qb, (size_t)(wmax > 0 ? wmax : 1) * sizeof(float));
     if (!rc && rows > 0) {
-        const long long total = (long long)rows * t->ld;
+        const long long total = (long long)ceil_div(rows, RS_BM) * RS_BM * t->kbn * RS_BK;
         const int blocks = (int)std::min<long long>((total + 255) / 256, 65535);
-        split3_kernel<<<blocks, 256, 0, irwls_stream()>>>(X->X, rows, X->width, X->ld, t->X[0], t->X[1], t->X[2],
-                                                           t->ld);
+        if (P == 1)
+            rs_split_kernel<1><<<blocks, 256, 0, irwls_stream()>>>(X->X, rows, X->width, X->ld, t->kbn, scale, t->A);
+        else
+            rs_split_kernel<3><<<blocks, 256, 0, irwls_stream()>>>(X->X, rows, X->width, X->ld, t->kbn, scale, t->A);
         irwls_count_launch(1);
         to_f32_kernel<<<ceil_div(rows, 256), 256, 0, irwls_stream()>>>(X->q, rows, t->q);
         irwls_count_launch(1);
@@ -1289,43 +1570,121 @@ extern "C" void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax)
     }
     return t;
 }
+}  // namespace
+
+// Blocked copy of rows 0..rows-1 of a device set for the precision form, in
+// the operand form its values allow, with room for `wmax` gathered rows.
+extern "C" void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax) {
+    int *d_bad = nullptr, bad[2] = {1, 1};
+    if (irwls_dev_malloc((void **)&d_bad, 2 * sizeof(int))) return nullptr;
+    const int rc = rs_check(X, rows, d_bad, bad);
+    irwls_dev_free(d_bad);
+    if (rc) return nullptr;
+    int P;
+    double scale;
+    rs_form(bad, 1, &P, &scale);
+    g_rs_last_pieces = P;
+    return rs_set_make(X, rows, wmax, ceil_div(X->width, RS_BK), P, scale);
+}
 
 extern "C" double irwls_tc_set_kbound(void *h) { return ((TcSet *)h)->kbound; }
 
 extern "C" void irwls_tc_set_free(void *h) {
     TcSet *t = (TcSet *)h;
     if (!t) return;
-    for (int k = 0; k < KR_P; ++k) {
-        irwls_dev_free(t->X[k]);
-        irwls_dev_free(t->B[k]);
-    }
+    irwls_dev_free(t->A);
+    irwls_dev_free(t->B);
     irwls_dev_free(t->q);
     irwls_dev_free(t->qb);
+    irwls_dev_free(t->bad);
     free(t);
 }
+
+namespace {
+// Gathers the rows idx[j < *d_n] into B, then runs the engine over the first
+// M rows of the set in the given mode.
+template <int P, int MODE>
+int rs_launch(TcSet *t, int M, const int *d_idx, const int *d_n, const double *d_cb, const double *d_init,
+              const double *d_tail, double *d_out, const TcSet *src = nullptr, double bias = 0.0, int hard = 0) {
+    // B rows come from the set itself (error updates) or from another set of
+    // the same layout (a model's support vectors)
+    const TcSet *from = src ? src : t;
+    const int gb = std::max(1, std::min(ceil_div((long long)t->wmax * t->kbn * P * 4, 256), 4096));
+    rs_gather_kernel<P><<<gb, 256, 0, irwls_stream()>>>(from->A, t->kbn, from->q, d_idx, d_n, t->wmax, t->B, t->qb);
+    IRWLS_LAUNCH_CHECK("tc_gather_rows");
+    constexpr int NS = rs_stages<P>();
+    const size_t smem = NS * RsStage<P>::BYTES + 1024;
+    static_assert(NS * RsStage<P>::BYTES + 1024 <= 227 * 1024, "ring exceeds shared memory");
+    cudaFuncSetAttribute(tc_rowsum_ws_kernel<P, NS, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int ntiles = ceil_div(M, RS_BM);
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    const int slot = MODE == 0 ? IRWLS_PROF_ROWSUM : IRWLS_PROF_PREDICT;
+    if (irwls_prof_on()) irwls_prof_begin(slot);
+    tc_rowsum_ws_kernel<P, NS, MODE><<<std::max(1, std::min(ntiles, sms)), RS_THREADS, smem, irwls_stream()>>>(
+        t->A, M, t->kbn, t->q, t->B, d_n, t->wmax, t->qb, d_cb, t->rbf, t->ng, t->dscale, d_init, d_tail, d_out, bias,
+        hard, irwls_dev_flags(), g_rs_wait_limit, g_rs_stall);
+    if (irwls_prof_on()) irwls_prof_end(slot);
+    IRWLS_LAUNCH_CHECK(MODE == 0 ? "tc_kernel_rowsum" : "tc_predict");
+    return 0;
+}
+}  // namespace
 
 // out_i = (init_i - sum_{j < *d_n} cb_j k(x_i, x_{idx_j})) - tail[0] for every
 // row of the set (init may alias out; tail may be NULL).
 extern "C" int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n, const double *d_cb,
                                       const double *d_init, const double *d_tail, double *d_out) {
     TcSet *t = (TcSet *)h;
-    const int per = t->ld / 8;
-    Pieces xp, bp;
-    for (int k = 0; k < KR_P; ++k) {
-        xp.p[k] = t->X[k];
-        bp.p[k] = t->B[k];
+    if (t->rows <= 0) return 0;
+    return t->pieces == 1 ? rs_launch<1, 0>(t, t->rows, d_idx, d_n, d_cb, d_init, d_tail, d_out)
+                          : rs_launch<3, 0>(t, t->rows, d_idx, d_n, d_cb, d_init, d_tail, d_out);
+}
+
+namespace {
+__global__ void iota_kernel(int *p, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+}  // namespace
+
+// Precision-form prediction (src/LIBIRWLS-predict.c:56-131 computes
+// f(x) = b + sum_j w_j k(x, sv_j) in FP64): the test rows T and the support
+// vectors S in one blocked operand form (1 exact piece when both sets allow
+// the same scale, else 3), f from the tensor-core dot products with an FP32
+// exp and Kahan-compensated FP32 sums, bias added in FP64; the sign (>= 0 ->
+// +1) when `hard`. T and S share the feature width.
+extern "C" int irwls_tc_predict(const irwls_dev_set *T, int n, const irwls_dev_set *S, int nSV, const double *d_w,
+                                double bias, int hard, double *d_out) {
+    if (n <= 0) return 0;
+    int *d_bad = nullptr, *d_idx = nullptr, bad[4] = {1, 1, 1, 1};
+    int rc = irwls_dev_malloc((void **)&d_bad, 4 * sizeof(int));
+    rc |= irwls_dev_malloc((void **)&d_idx, (size_t)std::max(nSV, 1) * sizeof(int));
+    if (!rc) rc |= rs_check(T, n, d_bad, bad);
+    if (!rc) rc |= rs_check(S, nSV, d_bad + 2, bad + 2);
+    TcSet *ts = nullptr, *ss = nullptr;
+    if (!rc) {
+        int P;
+        double scale;
+        rs_form(bad, 2, &P, &scale);
+        const int kbn = ceil_div(std::max(T->width, S->width), RS_BK);
+        ts = rs_set_make(T, n, nSV, kbn, P, scale);
+        ss = ts ? rs_set_make(S, nSV, 0, kbn, P, scale) : nullptr;
+        if (!ts || !ss) rc = -3;
     }
-    const int gb = std::max(1, std::min(ceil_div((long long)t->wmax * per, 256), 4096));
-    tc_gather_rows_kernel<<<gb, 256, 0, irwls_stream()>>>(xp, t->ld, t->q, d_idx, d_n, t->wmax, t->B[0], t->B[1],
-                                                          t->B[2], t->qb);
-    IRWLS_LAUNCH_CHECK("tc_gather_rows");
-    const size_t smem = KR_NS * TcRing<KR_BN, KR_P, KR_BK>::BYTES + 1024;
-    cudaFuncSetAttribute(tc_kernel_rowsum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
-    tc_kernel_rowsum_kernel<<<ceil_div(t->rows, TC_BM), TC_THREADS, smem, irwls_stream()>>>(
-        xp, t->ld, t->rows, t->q, bp, t->ld, d_n, t->wmax, t->qb, d_cb, t->ld / KR_BK, t->rbf, t->ng, d_init, d_tail,
-        d_out, irwls_dev_flags());
-    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
-    IRWLS_LAUNCH_CHECK("tc_kernel_rowsum");
-    return 0;
+    if (!rc && nSV > 0) {
+        iota_kernel<<<ceil_div(nSV, 256), 256, 0, irwls_stream()>>>(d_idx, nSV);
+        irwls_count_launch(1);
+        rc |= irwls_dev_h2d(ts->nbuf, &nSV, sizeof(int));
+    }
+    if (!rc) {
+        if (nSV <= 0)
+            rc = irwls_dev_memset(ts->nbuf, 0, sizeof(int));
+        if (!rc)
+            rc = ts->pieces == 1
+                     ? rs_launch<1, 1>(ts, n, d_idx, ts->nbuf, d_w, nullptr, nullptr, d_out, ss, bias, hard)
+                     : rs_launch<3, 1>(ts, n, d_idx, ts->nbuf, d_w, nullptr, nullptr, d_out, ss, bias, hard);
+    }
+    irwls_tc_set_free(ts);
+    irwls_tc_set_free(ss);
+    irwls_dev_free(d_bad);
+    irwls_dev_free(d_idx);
+    return rc;
 }

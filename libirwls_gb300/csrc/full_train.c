@@ -217,7 +217,15 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
         }
         if (irwls_full_norms(beta, bnew, l + 1, norms)) goto fail;
         if (irwls_dev_d2h(h_norms, norms, 2 * sizeof(double)) || irwls_dev_sync()) goto fail;
-        if (tcs) acc += eps * h_l1[0];
+        if (tcs) {
+            /* a tensor-core wait that ran out left these errors stale: stop now */
+            const int tc = irwls_tc_status();
+            if (tc) {
+                irwls_set_error(-13, "a tensor-core pipeline wait of the error update ran out (code %d)", tc);
+                goto fail;
+            }
+            acc += eps * h_l1[0];
+        }
         const double ratio = h_norms[0] / h_norms[1];
         if (ratio < props.Eta) stop = 1;
         if (irwls_dev_d2d(beta, bnew, L1 * sizeof(double))) goto fail;

@@ -232,6 +232,10 @@ double irwls_tc_set_kbound(void *h);
 void irwls_tc_set_free(void *h);
 int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n, const double *d_cb, const double *d_init,
                            const double *d_tail, double *d_out);
+/* Precision-form prediction: d_out = b + sum_j w_j k(t_i, s_j) (or its sign)
+ * from the tensor-core products; T and S share the feature width. */
+int irwls_tc_predict(const irwls_dev_set *T, int n, const irwls_dev_set *S, int nSV, const double *d_w, double bias,
+                     int hard, double *d_out);
 
 /* Resident-dataset drivers (full_train.c, budgeted_train.c). */
 int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double *beta_out);

@@ -2,7 +2,8 @@
  * predict.c -- batched prediction on the GPU (reference
  * src/LIBIRWLS-predict.c:56-131). The test rows and the model's support
  * vectors are uploaded into one feature-index space; the decision values are
- * ordered kernel row sums (bias first, then support vectors in model order).
+ * ordered kernel row sums (bias first, then support vectors in model order);
+ * in the precision form they come from the tensor-core engine of dev_tc.cu.
  * The accuracy line is computed on the host from the returned values, as the
  * reference does.
  */
@@ -58,8 +59,12 @@ static double *predict(svm_dataset ds, model m, predictProperties props, int har
         if (fast) rc |= irwls_dev_malloc((void **)&d_W, irwls_predict_linear_scratch(S.width, m.nSVs) * sizeof(double));
         if (!rc) {
             rc |= irwls_dev_h2d(d_w, m.weights, (size_t)m.nSVs * sizeof(double));
-            rc |= fast ? irwls_predict_linear(&T, n, &S, m.nSVs, d_w, m.bias, hard, d_W, d_out)
-                       : irwls_predict_soft(&T, n, &S, m.nSVs, d_w, m.bias, hard, d_out);
+            if (fast)
+                rc |= irwls_predict_linear(&T, n, &S, m.nSVs, d_w, m.bias, hard, d_W, d_out);
+            else if (irwls_get_precision() == IRWLS_PRECISION_MIXED)
+                rc |= irwls_tc_predict(&T, n, &S, m.nSVs, d_w, m.bias, hard, d_out);
+            else
+                rc |= irwls_predict_soft(&T, n, &S, m.nSVs, d_w, m.bias, hard, d_out);
             rc |= irwls_dev_d2h(out, d_out, (size_t)n * sizeof(double));
             rc |= irwls_dev_sync();
         }
