@@ -13,9 +13,12 @@
 // ignores that failure and solves with the stored negative Schur complement,
 // and so does this code.
 //
-// Per panel of 32 columns: one launch factors the diagonal block (redundantly
-// in every CTA, in shared memory) and solves the rows below it against it;
-// one launch applies the rank-32 update to the lower trailing matrix.
+// Two factorizations with the same arithmetic per element (so the same
+// bits): one cooperative launch scheduled by data flow (the default, below
+// chol_df_kernel), and a multi-launch sequence per panel of 32 columns (a
+// launch that solves the rows below the diagonal block against it, and a
+// launch that applies the rank-32 update to the lower trailing matrix and
+// factors the next diagonal block).
 #include <math.h>
 
 #include <atomic>
@@ -29,16 +32,13 @@ namespace {
 constexpr int NB = 32;
 
 // Factors the nb x nb diagonal block at (k0, k0) held in D (shared, NB x NB,
-// lower part valid), with LAPACK dpotrf's failed-pivot behaviour, and forms
-// the inverse of the lower factor in Di. Uses the whole CTA; ends synced.
+// lower part valid), with LAPACK dpotrf's failed-pivot behaviour, leaving
+// the reciprocal of each stored pivot in rp. Uses the whole CTA; ends synced.
 // FP64 runs at a fraction of the FP32 rate on this part, so every dependent
 // FP64 operation on this serial path costs tens of cycles: the pivot's
 // reciprocal square root is formed once and the column is scaled by it (as
-// dpotf2 scales by 1 / ajj), and each entry of the inverse is a dot product
-// split over 8 lanes of a warp.
-__device__ void factor_invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], int nb, int k0, int *flags,
-                                    int *failed_at) {
-    __shared__ double rp[NB];  // reciprocal of each stored pivot
+// dpotf2 scales by 1 / ajj).
+__device__ void factor_block(double (*D)[NB + 1], double *rp, int nb, int k0, int *flags, int *failed_at) {
     const int tid = threadIdx.x;
     if (tid == 0) *failed_at = -1;
     __syncthreads();
@@ -65,12 +65,19 @@ __device__ void factor_invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], i
         }
         __syncthreads();
     }
-    // inverse of the lower factor: column j by 8 lanes (threads 8 j .. 8 j + 7),
-    // Di[c][j] = -(sum_{j <= t < c} D[c][t] Di[t][j]) / D[c][c]
+    if (tid == 0 && *failed_at >= 0) atomicCAS(flags, 0, k0 + *failed_at + 1);
+}
+
+// Inverse of the factored block (its reciprocal pivots in rp): each entry a
+// dot product split over 8 lanes of a warp (column j by threads 8 j ..
+// 8 j + 7), Di[c][j] = -(sum_{j <= t < c} D[c][t] Di[t][j]) rp[c].
+// blockDim.x == 256; ends synced.
+__device__ void invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], const double *rp, int nb) {
+    const int tid = threadIdx.x;
     for (int t = tid; t < NB * NB; t += blockDim.x) Di[t / NB][t % NB] = 0.0;
     __syncthreads();
-    // (blockDim.x == 256 = 8 lanes x 32 columns; every lane of a warp runs the
-    // same iterations so that the shuffles always see the whole warp)
+    // (every lane of a warp runs the same iterations so that the shuffles
+    // always see the whole warp)
     {
         const int j = tid >> 3, q = tid & 7;
         if (q == 0 && j < nb) Di[j][j] = rp[j];
@@ -88,7 +95,31 @@ __device__ void factor_invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], i
         }
     }
     __syncthreads();
-    if (tid == 0 && *failed_at >= 0) atomicCAS(flags, 0, k0 + *failed_at + 1);
+}
+
+__device__ void factor_invert_block(double (*D)[NB + 1], double (*Di)[NB + 1], double *rp, int nb, int k0,
+                                    int *flags, int *failed_at) {
+    factor_block(D, rp, nb, k0, flags, failed_at);
+    invert_block(D, Di, rp, nb);
+}
+
+// Panel solve of the rows r < nr of T (columns c < nb) against the factored
+// diagonal block D with reciprocal pivots rp, in place, by forward
+// substitution: x_c = (a_c - sum_{t < c} x_t D[c][t]) rp[c], the sum taken
+// by FMAs in increasing t. Used by both factorizations, so they agree bit
+// for bit. blockDim.x == 256; ends synced.
+__device__ void subst_block(double (*T)[NB + 1], int nr, double (*D)[NB + 1], const double *rp, int nb) {
+    const int tid = threadIdx.x;
+    for (int t = 0; t < nb; ++t) {
+        for (int r = tid; r < nr; r += blockDim.x) T[r][t] = T[r][t] * rp[t];
+        __syncthreads();
+        const int m = nb - t - 1;
+        for (int e = tid; e < nr * m; e += blockDim.x) {
+            const int r = e / m, c = t + 1 + e % m;
+            T[r][c] = fma(-T[r][t], D[c][t], T[r][c]);
+        }
+        __syncthreads();
+    }
 }
 
 __device__ void store_block(double *M, int ld, int k0, int nb, double (*D)[NB + 1], double (*Di)[NB + 1],
@@ -105,6 +136,7 @@ __device__ void store_block(double *M, int ld, int k0, int nb, double (*D)[NB + 
 __global__ void __launch_bounds__(256) chol_factor0_kernel(double *__restrict__ M, int n, int ld,
                                                            int *__restrict__ flags, double *__restrict__ Dinv) {
     __shared__ double D[NB][NB + 1], Di[NB][NB + 1];
+    __shared__ double rp[NB];
     __shared__ int failed_at;
     const int nb = min(NB, n);
     for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
@@ -112,33 +144,37 @@ __global__ void __launch_bounds__(256) chol_factor0_kernel(double *__restrict__ 
         D[r][c] = (r < nb && c <= r) ? M[(size_t)c * ld + r] : 0.0;
     }
     __syncthreads();
-    factor_invert_block(D, Di, nb, 0, flags, &failed_at);
+    factor_invert_block(D, Di, rp, nb, 0, flags, &failed_at);
     store_block(M, ld, 0, nb, D, Di, Dinv);
 }
 
 // Panel solve: rows i >= k0 + nb (and the right-hand-side row n when present)
-// get L[i, k0:k0+nb] = A[i, k0:k0+nb] D^-T, an independent 32-term dot per
-// output. 8 rows per CTA, one output per thread.
+// get L[i, k0:k0+nb] = A[i, k0:k0+nb] D^-T by forward substitution against
+// the factored diagonal block (from M, its reciprocal pivots from the
+// diagonal of the stored inverse). 8 rows per CTA.
 __global__ void __launch_bounds__(256) chol_trsm_kernel(double *__restrict__ M, int ld, int k0, int nb, int nrows,
                                                         const double *__restrict__ Dinv) {
-    __shared__ double Di[NB][NB + 1];
+    __shared__ double D[NB][NB + 1];
     __shared__ double A[8][NB + 1];
+    __shared__ double rp[NB];
     const int tid = threadIdx.x;
     const int i0 = k0 + nb + blockIdx.x * 8;
-    for (int t = tid; t < NB * NB; t += 256) Di[t / NB][t % NB] = Dinv[t];
+    for (int t = tid; t < NB * NB; t += 256) {
+        const int r = t / NB, c = t % NB;
+        D[r][c] = (r < nb && c <= r) ? M[(size_t)(k0 + c) * ld + k0 + r] : 0.0;
+    }
+    if (tid < NB) rp[tid] = Dinv[tid * (NB + 1)];
     {
         const int c = tid / 8, r = tid % 8;  // 256 = 32 columns x 8 rows
         const int i = i0 + r;
         A[r][c] = (c < nb && i < nrows) ? M[(size_t)(k0 + c) * ld + i] : 0.0;
     }
     __syncthreads();
+    const int nr = min(8, nrows - i0);
+    subst_block(A, nr, D, rp, nb);
     const int c = tid / 8, r = tid % 8;
     const int i = i0 + r;
-    if (c < nb && i < nrows) {
-        double x = 0.0;
-        for (int t = 0; t <= c; ++t) x = fma(Di[c][t], A[r][t], x);
-        M[(size_t)(k0 + c) * ld + i] = x;
-    }
+    if (c < nb && i < nrows) M[(size_t)(k0 + c) * ld + i] = A[r][c];
 }
 
 // Trailing update of the lower part: M[i][j] -= sum_t L[i][t] L[j][t] over the
@@ -182,7 +218,8 @@ __global__ void __launch_bounds__(256) chol_update_kernel(double *__restrict__ M
         Li[rr][c] = (rr < nb2 && c <= rr) ? M[(size_t)(k1 + c) * ld + k1 + rr] : 0.0;
     }
     __syncthreads();
-    factor_invert_block(Li, Lj, nb2, k1, flags, &failed_at);
+    __shared__ double rp[NB];
+    factor_invert_block(Li, Lj, rp, nb2, k1, flags, &failed_at);
     store_block(M, ld, k1, nb2, Li, Lj, Dinv_next);
 }
 
@@ -249,8 +286,11 @@ __global__ void zero_upper_kernel(double *__restrict__ M, int n, int ld) {
 //
 // Every element gets the multi-launch path's operations in the same order:
 // per panel, acc = sum over the panel's 32 columns by FMA from zero, then
-// M - acc; the diagonal blocks through factor_invert_block; the panel solves
-// as products with the inverted block. The results are the same bits.
+// M - acc; the diagonal blocks through factor_block; the panel solves by
+// forward substitution against the factored block (subst_block). The
+// results are the same bits. A diagonal block's factor is published before
+// its inverse is formed: only the backward sweep, after this launch, reads
+// the inverse.
 //
 // The waits are bounded: one that runs out (which needs a fault in this
 // schedule) sets the pivot status to -1 and the tensor-core status word to
@@ -301,6 +341,7 @@ __global__ void __launch_bounds__(256) chol_df_kernel(double *__restrict__ M, in
                                                       int *__restrict__ flags, double *__restrict__ Dinv,
                                                       unsigned *__restrict__ ready, int *__restrict__ abort) {
     __shared__ double T[NB][NB + 1], Li[NB][NB + 1], Lj[NB][NB + 1];
+    __shared__ double rp[NB];
     __shared__ int failed_at, ok_sh;
     const int tid = threadIdx.x;
     const int nbc = (n + NB - 1) / NB, nbr = (nrows + NB - 1) / NB;
@@ -343,32 +384,41 @@ __global__ void __launch_bounds__(256) chol_df_kernel(double *__restrict__ M, in
                     if (r >= nc || c > r) T[r][c] = 0.0;
                 }
                 __syncthreads();
-                factor_invert_block(T, Li, nc, c0, flags, &failed_at);
+                factor_block(T, rp, nc, c0, flags, &failed_at);
+                // the factor and its reciprocal pivots (the inverse's
+                // diagonal) are all the panel solves read: publish them now
                 for (int e = tid; e < NB * NB; e += 256) {
                     const int r = e / NB, c = e % NB;
                     if (r < nc && c <= r) M[(size_t)(c0 + c) * ld + c0 + r] = T[r][c];
-                    Dinv[(size_t)j * NB * NB + e] = Li[r][c];
                 }
-                // the right-hand-side row: x_c = sum_{t <= c} Di[c][t] a_t
-                for (int e = tid; e < NB * NB; e += 256) {
-                    const int c = e / NB, r = e % NB;
-                    if (r < nc || r >= nr || c >= nc) continue;
-                    double x = 0.0;
-                    for (int q = 0; q <= c; ++q) x = fma(Li[c][q], Lj[r][q], x);
-                    M[(size_t)(c0 + c) * ld + r0 + r] = x;
-                }
+                if (tid < NB) Dinv[(size_t)j * NB * NB + tid * (NB + 1)] = tid < nc ? rp[tid] : 0.0;
                 df_publish(ready + j);
-                if (nr > nc) df_publish(ready + nbc + (size_t)j * nbr + i);
+                // the right-hand-side row, by the same substitution
+                if (nr > nc) {
+                    for (int e = tid; e < NB * NB; e += 256) {
+                        const int r = e / NB, c = e % NB;
+                        if (r < nr - nc) Li[r][c] = Lj[nc + r][c];
+                    }
+                    __syncthreads();
+                    subst_block(Li, nr - nc, T, rp, nc);
+                    for (int c = tid; c < nc; c += 256) M[(size_t)(c0 + c) * ld + r0 + nc] = Li[0][c];
+                    df_publish(ready + nbc + (size_t)j * nbr + i);
+                }
+                // the inverse (for the backward sweep after this launch)
+                invert_block(T, Lj, rp, nc);
+                for (int e = tid; e < NB * NB; e += 256) Dinv[(size_t)j * NB * NB + e] = Lj[e / NB][e % NB];
             } else {
                 if (!df_wait(ready + j, abort, &ok_sh)) goto fail;
-                for (int e = tid; e < NB * NB; e += 256) Li[e / NB][e % NB] = __ldcg(Dinv + (size_t)j * NB * NB + e);
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int r = e / NB, c = e % NB;
+                    Li[r][c] = (r < nc && c <= r) ? __ldcg(M + (size_t)(c0 + c) * ld + c0 + r) : 0.0;
+                }
+                if (tid < NB) rp[tid] = __ldcg(Dinv + (size_t)j * NB * NB + tid * (NB + 1));
                 __syncthreads();
-                const int c = tid / 8;
-                for (int r = tid % 8; r < NB; r += 8) {
-                    if (c >= nc || r >= nr) continue;
-                    double x = 0.0;
-                    for (int q = 0; q <= c; ++q) x = fma(Li[c][q], T[r][q], x);
-                    M[(size_t)(c0 + c) * ld + r0 + r] = x;
+                subst_block(T, nr, Li, rp, nc);
+                for (int e = tid; e < NB * NB; e += 256) {
+                    const int c = e / NB, r = e % NB;
+                    if (c < nc && r < nr) M[(size_t)(c0 + c) * ld + r0 + r] = T[r][c];
                 }
                 df_publish(ready + nbc + (size_t)j * nbr + i);
             }

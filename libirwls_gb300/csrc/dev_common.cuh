@@ -24,9 +24,10 @@ int *irwls_dev_flags();
 
 // ---------------------------------------------------------------------------
 // Kernel entries. All arithmetic is FP64 with explicit round-to-nearest
-// operations, so no multiply-add is contracted and the values match the
-// reference's x86 build (src/kernels.c:63-183) operation for operation;
-// exp() is CUDA's double-precision exponential.
+// operations, so the values match the reference's x86 build
+// (src/kernels.c:63-183) operation for operation: no multiply-add is
+// contracted except the one in norm_sqdist, whose result is provably the
+// reference's; exp() is CUDA's double-precision exponential.
 // ---------------------------------------------------------------------------
 struct KView {
     int mode;
@@ -70,10 +71,13 @@ __device__ __forceinline__ double raw_sqdist(const double *a, const double *b, i
 // index order (src/kernels.c:101-114). Entries whose partner value is zero
 // add a signed zero, which leaves the sum unchanged, so iterating one row's
 // entries against the other row's dense copy reproduces the merge-join.
+// (-2 b) a rounds to -2 round(b a) (scaling by two is exact), so each entry
+// is one multiply and one fused -2 t + s: the reference's value with two
+// FP64 operations instead of three (the FP64 pipe bounds these kernels).
 __device__ __forceinline__ double norm_sqdist(const double *a_dense, double qa, const KView &B, int jb) {
     double s = __dadd_rn(qa, B.q[jb]);
     const int p0 = B.rp[jb], p1 = B.rp[jb + 1];
-    for (int p = p0; p < p1; ++p) s = __dadd_rn(s, __dmul_rn(-2.0 * B.cv[p], a_dense[B.ci[p]]));
+    for (int p = p0; p < p1; ++p) s = __fma_rn(-2.0, __dmul_rn(B.cv[p], a_dense[B.ci[p]]), s);
     return s;
 }
 

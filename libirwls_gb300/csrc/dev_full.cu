@@ -385,32 +385,6 @@ __global__ void fill_ws_kernel(int *SW, int nSW, int *SIN, int nSIN, const int *
     }
 }
 
-// Precision form: the rows whose errors are kept exact (FP64 increments):
-// support vectors, rows with |e_i y_i| < band, and the working set SW.
-// flag[i] says whether row i was exact before; rows entering the set are
-// listed in Snew (their errors must be recomputed) unless `all_exact`.
-// mark: scratch of l ints, zero on entry and on exit.
-__global__ void __launch_bounds__(CT) exact_set_kernel(const double *__restrict__ e, const double *__restrict__ y,
-                                                       const double *__restrict__ beta, int l,
-                                                       const int *__restrict__ SW, int nSW, double band,
-                                                       int all_exact, int *flag, int *mark, int *S, int *Snew,
-                                                       int *counts) {
-    __shared__ int s_scan[CT];
-    for (int k = threadIdx.x; k < nSW; k += CT) mark[SW[k]] = 1;
-    __syncthreads();
-    auto in_set = [&](int i) { return beta[i] != 0.0 || fabs(e[i] * y[i]) < band || mark[i] != 0; };
-    const int nnew = all_exact ? 0
-                               : block_compact(l, [&](int i) { return in_set(i) && flag[i] == 0; },
-                                               [&](int p, int i) { Snew[p] = i; }, s_scan);
-    const int ns = block_compact(l, in_set, [&](int p, int i) { S[p] = i; }, s_scan);
-    for (int i = threadIdx.x; i < l; i += CT) flag[i] = in_set(i) ? 1 : 0;
-    __syncthreads();
-    for (int k = threadIdx.x; k < nSW; k += CT) mark[SW[k]] = 0;
-    if (threadIdx.x == 0) {
-        counts[0] = ns;
-        counts[1] = nnew;
-    }
-}
 
 __global__ void gather_kernel(const double *__restrict__ src, const int *__restrict__ idx, int n,
                               double *__restrict__ dst) {
@@ -436,6 +410,188 @@ __global__ void __launch_bounds__(CT) sv_list_kernel(const double *__restrict__ 
     if (threadIdx.x == 0) cnt[0] = n;
 }
 
+// ---- multi-block ordered compactions over all l rows ------------------------
+//
+// The outer classification and the precision form's exact set each split l
+// rows into ordered lists. One CTA walking 100000 rows evaluated every row's
+// FP64 tests several times on one SM (about 1 ms per call); here every row's
+// list is decided once, by all SMs, and the lists are written in ascending
+// row order by blocks of CB rows: a count pass per block, then a write pass
+// in which each block adds the counts of the blocks before it and places its
+// rows round by round with warp-ballot prefixes. The lists are the
+// single-CTA kernels' lists, element for element.
+constexpr int CB = 2048;
+
+__device__ __forceinline__ int bsum256(int v, int *ws) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int t = 0;
+    for (int k = 0; k < 8; ++k) t += ws[k];
+    __syncthreads();
+    return t;
+}
+
+// Writes the rows of one round (256 consecutive rows) that belong to list k
+// (member[k]) at base[k] + their rank among the round's members, in row
+// order; advances base[k] by the round's members. 256 threads.
+template <int NL>
+__device__ __forceinline__ void ordered_round(const bool (&member)[NL], int i, int *base, int *const (&out)[NL],
+                                              int (*ws)[8]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned bal[NL];
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+        bal[k] = __ballot_sync(0xffffffffu, member[k]);
+        if (lane == 0) ws[k][warp] = __popc(bal[k]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+        int off = 0, tot = 0;
+        for (int w = 0; w < 8; ++w) {
+            off += w < warp ? ws[k][w] : 0;
+            tot += ws[k][w];
+        }
+        if (member[k] && out[k]) out[k][base[k] + off + __popc(bal[k] & ((1u << lane) - 1u))] = i;
+        base[k] += tot;
+    }
+    __syncthreads();
+}
+
+// Classification codes: 0 inactive, 1 candidate, 2 + slot a violator of
+// type slot (its list is decided by first[slot]), 255 none.
+__global__ void classify_code_kernel(const double *__restrict__ bnew, const double *__restrict__ e,
+                                     const double *__restrict__ y, int l, double C, unsigned char *__restrict__ code,
+                                     int *__restrict__ first) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l; i += gridDim.x * blockDim.x) {
+        int slot = -1;
+        const int c = classify_one(bnew[i], e[i], y[i], C, &slot);
+        unsigned char v = 255;
+        if (c == 2 && slot >= 0) {
+            v = (unsigned char)(2 + slot);
+            atomicMin(first + slot, i);
+        } else if (c == 2 || c == 1) {
+            v = 1;
+        } else if (c == 0) {
+            v = 0;
+        }
+        code[i] = v;
+    }
+}
+
+// list of row i: 0 SW, 1 SC, 2 SIN, -1 none
+__device__ __forceinline__ int classify_list(unsigned char v, int i, const int *first) {
+    if (v >= 2 && v < 8) return first[v - 2] == i ? 0 : 1;
+    return v == 1 ? 1 : (v == 0 ? 2 : -1);
+}
+
+__global__ void __launch_bounds__(256) classify_count_kernel(const unsigned char *__restrict__ code, int l,
+                                                             const int *__restrict__ first, int *__restrict__ cnt) {
+    __shared__ int ws[8];
+    const int r0 = blockIdx.x * CB, r1 = min(l, r0 + CB);
+    int c[3] = {0, 0, 0};
+    for (int i = r0 + threadIdx.x; i < r1; i += 256) {
+        const int k = classify_list(code[i], i, first);
+        if (k >= 0) c[k] += 1;
+    }
+    for (int k = 0; k < 3; ++k) {
+        const int t = bsum256(c[k], ws);
+        if (threadIdx.x == 0) cnt[3 * blockIdx.x + k] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) classify_write_kernel(const unsigned char *__restrict__ code, int l,
+                                                             const int *__restrict__ first,
+                                                             const int *__restrict__ cnt, int nb, int *SW, int *SC,
+                                                             int *SIN, irwls_outer_counts *counts) {
+    __shared__ int ws[3][8];
+    int base[3];
+    for (int k = 0; k < 3; ++k) {
+        int part = 0;
+        for (int b = threadIdx.x; b < (int)blockIdx.x; b += 256) part += cnt[3 * b + k];
+        base[k] = bsum256(part, ws[0]);
+    }
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
+        counts->nSW = base[0] + cnt[3 * (nb - 1)];
+        counts->nSC = base[1] + cnt[3 * (nb - 1) + 1];
+        counts->nSIN = base[2] + cnt[3 * (nb - 1) + 2];
+    }
+    int *const out[3] = {SW, SC, SIN};
+    const int r0 = blockIdx.x * CB, r1 = min(l, r0 + CB);
+    for (int i0 = r0; i0 < r1; i0 += 256) {
+        const int i = i0 + threadIdx.x;
+        const int k = i < r1 ? classify_list(code[i], i, first) : -1;
+        const bool m[3] = {k == 0, k == 1, k == 2};
+        ordered_round<3>(m, i, base, out, ws);
+    }
+}
+
+__global__ void fill_int_kernel(int *p, int n, int v) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
+}
+
+__global__ void mark_kernel(const int *__restrict__ SW, int nSW, int *__restrict__ mark, int v) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nSW; k += gridDim.x * blockDim.x) mark[SW[k]] = v;
+}
+
+// Precision form: the rows whose errors are kept exact (FP64 increments):
+// support vectors, rows with |e_i y_i| < band, and the working set SW (marked
+// in `mark`, l ints that are zero on entry and on exit). flag[i] says whether
+// row i was exact before; rows entering the set are listed in Snew (their
+// errors must be recomputed) unless `all_exact`.
+__device__ __forceinline__ bool exact_in_set(const double *e, const double *y, const double *beta,
+                                             const int *mark, double band, int i) {
+    return beta[i] != 0.0 || fabs(e[i] * y[i]) < band || mark[i] != 0;
+}
+
+__global__ void __launch_bounds__(256) exact_count_kernel(const double *__restrict__ e, const double *__restrict__ y,
+                                                          const double *__restrict__ beta, int l,
+                                                          const int *__restrict__ mark, double band, int all_exact,
+                                                          const int *__restrict__ flag, int *__restrict__ cnt) {
+    __shared__ int ws[8];
+    const int r0 = blockIdx.x * CB, r1 = min(l, r0 + CB);
+    int cs = 0, cn = 0;
+    for (int i = r0 + threadIdx.x; i < r1; i += 256)
+        if (exact_in_set(e, y, beta, mark, band, i)) {
+            cs += 1;
+            cn += (!all_exact && flag[i] == 0) ? 1 : 0;
+        }
+    cs = bsum256(cs, ws);
+    cn = bsum256(cn, ws);
+    if (threadIdx.x == 0) {
+        cnt[2 * blockIdx.x] = cs;
+        cnt[2 * blockIdx.x + 1] = cn;
+    }
+}
+
+__global__ void __launch_bounds__(256) exact_write_kernel(const double *__restrict__ e, const double *__restrict__ y,
+                                                          const double *__restrict__ beta, int l,
+                                                          const int *__restrict__ mark, double band, int all_exact,
+                                                          int *__restrict__ flag, const int *__restrict__ cnt, int nb,
+                                                          int *S, int *Snew, int *counts) {
+    __shared__ int ws[2][8];
+    int base[2];
+    for (int k = 0; k < 2; ++k) {
+        int part = 0;
+        for (int b = threadIdx.x; b < (int)blockIdx.x; b += 256) part += cnt[2 * b + k];
+        base[k] = bsum256(part, ws[0]);
+    }
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
+        counts[0] = base[0] + cnt[2 * (nb - 1)];
+        counts[1] = base[1] + cnt[2 * (nb - 1) + 1];
+    }
+    int *const out[2] = {S, Snew};
+    const int r0 = blockIdx.x * CB, r1 = min(l, r0 + CB);
+    for (int i0 = r0; i0 < r1; i0 += 256) {
+        const int i = i0 + threadIdx.x;
+        const bool in = i < r1 && exact_in_set(e, y, beta, mark, band, i);
+        const bool m[2] = {in, in && !all_exact && flag[i] == 0};
+        if (i < r1) flag[i] = in ? 1 : 0;  // each row's flag is read and written by its own thread only
+        ordered_round<2>(m, i, base, out, ws);
+    }
+}
+
 }  // namespace
 
 // e = y - K(:, SV) beta_SV - b in FP64 over all l rows (the exact error
@@ -457,9 +613,22 @@ extern "C" int irwls_full_sv_list(const double *d_beta, int l, int *d_lst, doubl
 extern "C" int irwls_full_exact_set(const double *d_e, const double *d_y, const double *d_beta, int l,
                                     const int *d_SW, int nSW, double band, int all_exact, int *d_flag, int *d_mark,
                                     int *d_S, int *d_Snew, int *d_counts) {
-    exact_set_kernel<<<1, CT, 0, irwls_stream()>>>(d_e, d_y, d_beta, l, d_SW, nSW, band, all_exact, d_flag, d_mark,
-                                                   d_S, d_Snew, d_counts);
-    IRWLS_LAUNCH_CHECK("exact_set");
+    const int nb = std::max(1, ceil_div(l, CB));
+    int *cnt = (int *)irwls_ctx_scratch(2, (size_t)2 * nb * sizeof(int));
+    if (!cnt) return -3;
+    if (nSW > 0) {
+        mark_kernel<<<ceil_div(nSW, 256), 256, 0, irwls_stream()>>>(d_SW, nSW, d_mark, 1);
+        IRWLS_LAUNCH_CHECK("exact_mark");
+    }
+    exact_count_kernel<<<nb, 256, 0, irwls_stream()>>>(d_e, d_y, d_beta, l, d_mark, band, all_exact, d_flag, cnt);
+    IRWLS_LAUNCH_CHECK("exact_count");
+    exact_write_kernel<<<nb, 256, 0, irwls_stream()>>>(d_e, d_y, d_beta, l, d_mark, band, all_exact, d_flag, cnt,
+                                                       nb, d_S, d_Snew, d_counts);
+    IRWLS_LAUNCH_CHECK("exact_write");
+    if (nSW > 0) {
+        mark_kernel<<<ceil_div(nSW, 256), 256, 0, irwls_stream()>>>(d_SW, nSW, d_mark, 0);
+        IRWLS_LAUNCH_CHECK("exact_unmark");
+    }
     return 0;
 }
 
@@ -575,8 +744,30 @@ extern "C" int irwls_full_norms(const double *d_beta, const double *d_bnew, int 
 
 extern "C" int irwls_full_classify(const double *d_bnew, const double *d_e, const double *d_y, int l, double C,
                                    int *d_SW, int *d_SC, int *d_SIN, irwls_outer_counts *d_counts) {
-    classify_kernel<<<1, CT, 0, irwls_stream()>>>(d_bnew, d_e, d_y, l, C, d_SW, d_SC, d_SIN, d_counts);
-    IRWLS_LAUNCH_CHECK("classify");
+    if (l < 4 * CB) {
+        // small sets: one CTA is faster than four launches
+        classify_kernel<<<1, CT, 0, irwls_stream()>>>(d_bnew, d_e, d_y, l, C, d_SW, d_SC, d_SIN, d_counts);
+        IRWLS_LAUNCH_CHECK("classify");
+        return 0;
+    }
+    const int nb = ceil_div(l, CB);
+    // scratch slot 2: the per-block counts, then the six first-violator
+    // slots, then one code byte per row
+    const size_t cbytes = (size_t)3 * nb * sizeof(int), fbytes = 8 * sizeof(int);
+    unsigned char *sc = (unsigned char *)irwls_ctx_scratch(2, cbytes + fbytes + (size_t)l);
+    if (!sc) return -3;
+    int *cnt = (int *)sc, *first = (int *)(sc + cbytes);
+    unsigned char *code = sc + cbytes + fbytes;
+    fill_int_kernel<<<1, 32, 0, irwls_stream()>>>(first, 6, 0x7fffffff);
+    IRWLS_LAUNCH_CHECK("classify_first");
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    classify_code_kernel<<<std::min(ceil_div(l, 256), 8 * sms), 256, 0, irwls_stream()>>>(d_bnew, d_e, d_y, l, C,
+                                                                                         code, first);
+    IRWLS_LAUNCH_CHECK("classify_code");
+    classify_count_kernel<<<nb, 256, 0, irwls_stream()>>>(code, l, first, cnt);
+    IRWLS_LAUNCH_CHECK("classify_count");
+    classify_write_kernel<<<nb, 256, 0, irwls_stream()>>>(code, l, first, cnt, nb, d_SW, d_SC, d_SIN, d_counts);
+    IRWLS_LAUNCH_CHECK("classify_write");
     return 0;
 }
 

@@ -1184,18 +1184,37 @@ __device__ __forceinline__ bool mbar_wait_lim(uint32_t mbar, uint32_t parity, lo
     return done != 0;
 }
 
-// bad[0] |= some value is not exactly a bf16; bad[1] |= some value is not
-// k / 255 for an integer |k| <= 256 (so that 255 x is exactly a bf16).
-__global__ void rs_quant_check_kernel(const double *__restrict__ X, int rows, int cols, int ldx, int *bad) {
+// Operand-form check of a set's stored values (its CSR entries: zeros are
+// exact in both forms). bad[0] |= some value is not exactly a bf16 (bit
+// test: the low 45 mantissa bits zero, the exponent in bf16's normal range);
+// bad[1] |= some value is not RN(k / 255) for an integer |k| <= 256. For the
+// second, with k = rint(255 v), r = fma(v, 255, -k) = 255 v - k exactly (an
+// integer multiple of ulp(v)), and v = RN(k / 255) exactly when
+// |r| <= 127 ulp(v) (63 ulp when v is a power of two and k / 255 lies below
+// it, where the binade below is finer); k / 255 is never halfway between two
+// doubles unless it is an integer. A thread stops once both flags are set.
+__global__ void rs_quant_check_kernel(const double *__restrict__ v, long long n, int *bad) {
     int b0 = 0, b1 = 0;
-    const long long total = (long long)rows * cols;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const double v = X[(t / cols) * ldx + t % cols];
-        const float f = __double2float_rn(v);
-        if ((double)f != v || __bfloat162float(__float2bfloat16_rn(f)) != f) b0 = 1;
-        const double k = rint(v * 255.0);
-        if (!(fabs(k) <= 256.0) || k / 255.0 != v) b1 = 1;
+    const volatile int *vb = bad;
+    long long it = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x, ++it) {
+        if ((it & 63) == 0 && vb[0] && vb[1]) break;
+        const double x = v[t];
+        if (x == 0.0) continue;
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+        const int ex = (int)((bits >> 52) & 0x7ff);
+        const unsigned long long man = bits & ((1ULL << 52) - 1);
+        if ((man & ((1ULL << 45) - 1)) != 0 || ex < 1023 - 126 || ex > 1023 + 127) b0 = 1;
+        const double k = rint(x * 255.0);
+        if (!(fabs(k) <= 256.0) || ex < 64 || ex == 0x7ff) {
+            b1 = 1;
+            continue;
+        }
+        const double r = fma(x, 255.0, -k);
+        const double ulp = __longlong_as_double((long long)((unsigned long long)(ex - 52) << 52));
+        const double lim = (man == 0 && (r > 0.0) == (x > 0.0)) ? 63.0 : 127.0;
+        if (fabs(r) > lim * ulp) b1 = 1;
     }
     b0 = __any_sync(0xffffffffu, b0);
     b1 = __any_sync(0xffffffffu, b1);
@@ -1234,11 +1253,14 @@ __global__ void rs_split_kernel(const double *__restrict__ X, int rows, int cols
 }
 
 // Working-set row j < *d_n becomes row j of the blocked B (256-row chunks):
-// its 16-byte groups copied from the blocked A row idx[j]; qb[j] = q[idx[j]].
+// its 16-byte groups copied from the blocked A row idx[j]; qb[j] = q[idx[j]]
+// and cbf[j] = (float)cb[j] (converted once here: FP64 conversions run on
+// this part's narrow FP64 pipe, so the epilogue must not repeat them).
 template <int P>
 __global__ void rs_gather_kernel(const __nv_bfloat16 *__restrict__ A, int kbn, const float *__restrict__ q,
                                  const int *__restrict__ idx, const int *__restrict__ d_n, int nmax,
-                                 __nv_bfloat16 *__restrict__ B, float *__restrict__ qb) {
+                                 __nv_bfloat16 *__restrict__ B, float *__restrict__ qb,
+                                 const double *__restrict__ cb, float *__restrict__ cbf) {
     const int n = min(*d_n, nmax);
     const long long total = (long long)n * kbn * P * 4;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -1253,7 +1275,10 @@ __global__ void rs_gather_kernel(const __nv_bfloat16 *__restrict__ A, int kbn, c
         const size_t src = ((size_t)(i >> 7) * kbn + k) * P * RS_APIECE + (size_t)p * RS_APIECE + rs_core(i & 127, 8 * g);
         const size_t dst = ((size_t)(j >> 8) * kbn + k) * P * RS_BPIECE + (size_t)p * RS_BPIECE + rs_core(j & 255, 8 * g);
         *(uint4 *)(B + dst) = *(const uint4 *)(A + src);
-        if (k == 0 && p == 0 && g == 0) qb[j] = q[i];
+        if (k == 0 && p == 0 && g == 0) {
+            qb[j] = q[i];
+            cbf[j] = __double2float_rn(cb[j]);
+        }
     }
 }
 
@@ -1264,7 +1289,7 @@ template <int P, int NS, int MODE>
 __global__ void __launch_bounds__(RS_THREADS, 1) tc_rowsum_ws_kernel(
     const __nv_bfloat16 *__restrict__ A, int M, int kbn, const float *__restrict__ qa,
     const __nv_bfloat16 *__restrict__ B, const int *__restrict__ d_n, int nmax, const float *__restrict__ qb,
-    const double *__restrict__ cb, int rbf, float ng, float dscale, const double *init,
+    const float *__restrict__ cb, int rbf, float ng, float dscale, const double *init,
     const double *__restrict__ tail, double *out, double bias, int hard, int *flags, long long wait_limit,
     int stall) {
     using S = RsStage<P>;
@@ -1416,7 +1441,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) tc_rowsum_ws_kernel(
                             const float dot = v[jj] * dscale;
                             const float k =
                                 rbf ? expf(ng * fmaxf(qi + __ldg(qb + c_base + c) - 2.f * dot, 0.f)) : dot;
-                            const float y = __fsub_rn(__fmul_rn((float)__ldg(cb + c_base + c), k), comp);
+                            const float y = __fsub_rn(__fmul_rn(__ldg(cb + c_base + c), k), comp);
                             const float t = __fadd_rn(sum, y);
                             comp = __fsub_rn(__fsub_rn(t, sum), y);
                             sum = t;
@@ -1454,7 +1479,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) tc_rowsum_ws_kernel(
 
 struct TcSet {
     __nv_bfloat16 *A, *B;
-    float *q, *qb;
+    float *q, *qb, *cbf;
     int *bad;   // two words: the operand-form check, then the gathered-row count of a prediction
     int *nbuf;
     int rows, kbn, wmax, rbf, pieces;
@@ -1501,9 +1526,15 @@ int rs_check(const irwls_dev_set *X, int rows, int *d_bad, int bad[2]) {
     bad[0] = bad[1] = 0;
     if (rows <= 0) return 0;
     int rc = irwls_dev_memset(d_bad, 0, 2 * sizeof(int));
-    const long long total = (long long)rows * X->width;
-    const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 8 * 1024));
-    rs_quant_check_kernel<<<blocks, 256, 0, irwls_stream()>>>(X->X, rows, X->width, X->ld, d_bad);
+    // the stored values of rows 0..rows-1: the first rp[rows] CSR entries
+    int nnz = 0;
+    rc |= irwls_dev_d2h(&nnz, X->rp + rows, sizeof(int));
+    rc |= irwls_dev_sync();
+    if (rc) return rc;
+    const long long total = nnz;
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 8LL * sms));
+    rs_quant_check_kernel<<<blocks, 256, 0, irwls_stream()>>>(X->cv, total, d_bad);
     irwls_count_launch(1);
     rc |= irwls_dev_d2h(bad, d_bad, 2 * sizeof(int));
     rc |= irwls_dev_sync();
@@ -1542,6 +1573,7 @@ TcSet *rs_set_make(const irwls_dev_set *X, int rows, int wmax, int kbn, int P, d
     rc |= irwls_dev_malloc((void **)&t->B, bb);
     rc |= irwls_dev_malloc((void **)&t->q, (size_t)(rows > 0 ? rows : 1) * sizeof(float));
     rc |= irwls_dev_malloc((void **)&t->qb, (size_t)(wmax > 0 ? wmax : 1) * sizeof(float));
+    rc |= irwls_dev_malloc((void **)&t->cbf, (size_t)(wmax > 0 ? wmax : 1) * sizeof(float));
     if (!rc && rows > 0) {
         const long long total = (long long)ceil_div(rows, RS_BM) * RS_BM * t->kbn * RS_BK;
         const int blocks = (int)std::min<long long>((total + 255) / 256, 65535);
@@ -1596,6 +1628,7 @@ extern "C" void irwls_tc_set_free(void *h) {
     irwls_dev_free(t->B);
     irwls_dev_free(t->q);
     irwls_dev_free(t->qb);
+    irwls_dev_free(t->cbf);
     irwls_dev_free(t->bad);
     free(t);
 }
@@ -1610,7 +1643,8 @@ int rs_launch(TcSet *t, int M, const int *d_idx, const int *d_n, const double *d
     // the same layout (a model's support vectors)
     const TcSet *from = src ? src : t;
     const int gb = std::max(1, std::min(ceil_div((long long)t->wmax * t->kbn * P * 4, 256), 4096));
-    rs_gather_kernel<P><<<gb, 256, 0, irwls_stream()>>>(from->A, t->kbn, from->q, d_idx, d_n, t->wmax, t->B, t->qb);
+    rs_gather_kernel<P><<<gb, 256, 0, irwls_stream()>>>(from->A, t->kbn, from->q, d_idx, d_n, t->wmax, t->B, t->qb,
+                                                        d_cb, t->cbf);
     IRWLS_LAUNCH_CHECK("tc_gather_rows");
     constexpr int NS = rs_stages<P>();
     const size_t smem = NS * RsStage<P>::BYTES + 1024;
@@ -1621,7 +1655,7 @@ int rs_launch(TcSet *t, int M, const int *d_idx, const int *d_n, const double *d
     const int slot = MODE == 0 ? IRWLS_PROF_ROWSUM : IRWLS_PROF_PREDICT;
     if (irwls_prof_on()) irwls_prof_begin(slot);
     tc_rowsum_ws_kernel<P, NS, MODE><<<std::max(1, std::min(ntiles, sms)), RS_THREADS, smem, irwls_stream()>>>(
-        t->A, M, t->kbn, t->q, t->B, d_n, t->wmax, t->qb, d_cb, t->rbf, t->ng, t->dscale, d_init, d_tail, d_out, bias,
+        t->A, M, t->kbn, t->q, t->B, d_n, t->wmax, t->qb, t->cbf, t->rbf, t->ng, t->dscale, d_init, d_tail, d_out, bias,
         hard, irwls_dev_flags(), g_rs_wait_limit, g_rs_stall);
     if (irwls_prof_on()) irwls_prof_end(slot);
     IRWLS_LAUNCH_CHECK(MODE == 0 ? "tc_kernel_rowsum" : "tc_predict");

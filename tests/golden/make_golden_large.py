@@ -72,6 +72,17 @@ def arr(ptr, n, dtype=np.float64):
     return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype).copy()
 
 
+def packer(lib):
+    """The library whose calculate*Model packs the model: the reference's own,
+    or, for the restatement (which has none), this repository's host C
+    packing, which writes the same model bytes."""
+    try:
+        lib.calculateFULLModel
+        return lib
+    except AttributeError:
+        return _abi.load_library(os.path.join(ROOT, "libirwls_gb300", "libirwls_gb300.so"))
+
+
 def run_case(lib, libc, cfg, sgma_threads=1):
     hd, ht = datasets(cfg)
     out = dict(train_digest=np.array(synth.dataset_digest(hd)), test_digest=np.array(synth.dataset_digest(ht)))
@@ -87,7 +98,7 @@ def run_case(lib, libc, cfg, sgma_threads=1):
         out["sv"] = sv
         out["beta_sv"] = beta[sv]
         out["bias"] = np.array(beta[hd.l])
-        mdl = lib.calculateFULLModel(p, hd.struct, b)
+        mdl = packer(lib).calculateFULLModel(p, hd.struct, b)
     else:
         p = _abi.make_properties(gamma=cfg["gamma"], C_=cfg["C"], kernel=cfg["kernel"], size=cfg["size"],
                                  algorithm=cfg["algorithm"], threads=sgma_threads)
@@ -100,7 +111,7 @@ def run_case(lib, libc, cfg, sgma_threads=1):
         out["train_seconds"] = np.array(time.perf_counter() - t0)
         out["centroids"] = arr(c, cfg["size"], np.int32)
         out["weights"] = arr(w, cfg["size"])
-        mdl = lib.calculateBudgetedModel(p, hd.struct, c, w)
+        mdl = packer(lib).calculateBudgetedModel(p, hd.struct, c, w)
     pp = _abi.make_predict_properties(labels=0, soft=1)
     out["soft"] = arr(lib.softTest(ht.struct, mdl, pp), ht.l)
     pp.Soft = 0
