@@ -223,6 +223,38 @@ __global__ void __launch_bounds__(256) chol_update_kernel(double *__restrict__ M
     store_block(M, ld, k1, nb2, Li, Lj, Dinv_next);
 }
 
+// The two dot products of a backward-sweep block, shared by both sweeps so
+// that they give the same bits: each as four interleaved partial FMA chains
+// (the dependent chain of one FP64 FMA per term is four times shorter) added
+// as (s0 + s1) + (s2 + s3).
+// x_t = sum_{t <= c < nb} Di[c][t] yb[c]
+__device__ __forceinline__ double sweep_dot(const double (*Di)[NB + 1], const double *yb, int t, int nb) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int c = t;
+    for (; c + 3 < nb; c += 4) {
+        a0 = fma(Di[c][t], yb[c], a0);
+        a1 = fma(Di[c + 1][t], yb[c + 1], a1);
+        a2 = fma(Di[c + 2][t], yb[c + 2], a2);
+        a3 = fma(Di[c + 3][t], yb[c + 3], a3);
+    }
+    for (; c < nb; ++c) a0 = fma(Di[c][t], yb[c], a0);
+    return (a0 + a1) + (a2 + a3);
+}
+
+// sum_{c < nb} col[c] xb[c]
+__device__ __forceinline__ double sweep_row(const double *col, const double *xb, int nb) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int c = 0;
+    for (; c + 3 < nb; c += 4) {
+        a0 = fma(col[c], xb[c], a0);
+        a1 = fma(col[c + 1], xb[c + 1], a1);
+        a2 = fma(col[c + 2], xb[c + 2], a2);
+        a3 = fma(col[c + 3], xb[c + 3], a3);
+    }
+    for (; c < nb; ++c) a0 = fma(col[c], xb[c], a0);
+    return (a0 + a1) + (a2 + a3);
+}
+
 // Backward sweep L^T x = z, z in row n of M; one CTA, z in shared memory,
 // 32-row blocks from the bottom: x_b = D_b^-T y_b (parallel dots with the
 // stored inverse), then the rows above are updated.
@@ -241,19 +273,9 @@ __global__ void __launch_bounds__(256) chol_backsolve_kernel(const double *__res
         __syncthreads();
         if (tid < NB) yb[tid] = (r0 + tid < r1) ? z[r0 + tid] : 0.0;
         __syncthreads();
-        if (tid < r1 - r0) {
-            double v = 0.0;
-            for (int c = tid; c < r1 - r0; ++c) v = fma(Di[c][tid], yb[c], v);
-            z[r0 + tid] = v;
-        }
+        if (tid < r1 - r0) z[r0 + tid] = sweep_dot(Di, yb, tid, r1 - r0);
         __syncthreads();
-        for (int r = tid; r < r0; r += blockDim.x) {
-            double v = z[r];
-            const double *col = M + (size_t)r * ld;
-#pragma unroll 8
-            for (int c = r0; c < r1; ++c) v = fma(-col[c], z[c], v);
-            z[r] = v;
-        }
+        for (int r = tid; r < r0; r += blockDim.x) z[r] = z[r] - sweep_row(M + (size_t)r * ld + r0, z + r0, r1 - r0);
         __syncthreads();
     }
     for (int c = tid; c < n; c += blockDim.x) x[c] = z[c];
@@ -366,13 +388,31 @@ __global__ void __launch_bounds__(256) chol_df_kernel(double *__restrict__ M, in
                     Lj[r][kk] = r < nc ? __ldcg(M + (size_t)(kc + kk) * ld + c0 + r) : 0.0;
                 }
                 __syncthreads();
-                const int r = tid % NB;
-                for (int cc = tid / NB; cc < NB; cc += 8) {
-                    if (r >= nr || cc >= nc || (i == j && cc > r)) continue;
-                    double acc = 0.0;
+                if (i != j) {
+                    const int r = tid % NB;
+                    for (int cc = tid / NB; cc < NB; cc += 8) {
+                        if (r >= nr || cc >= nc) continue;
+                        double acc = 0.0;
 #pragma unroll 8
-                    for (int kk = 0; kk < NB; ++kk) acc = fma(Li[r][kk], Lj[cc][kk], acc);
-                    T[r][cc] = T[r][cc] - acc;
+                        for (int kk = 0; kk < NB; ++kk) acc = fma(Li[r][kk], Lj[cc][kk], acc);
+                        T[r][cc] = T[r][cc] - acc;
+                    }
+                } else {
+                    // a diagonal tile needs only its lower triangle: threads
+                    // take its NB (NB + 1) / 2 elements (the same FMAs per
+                    // element), not the full tile's divergent columns, which
+                    // halves this step on the factorization's critical path
+                    for (int e = tid; e < NB * (NB + 1) / 2; e += 256) {
+                        int r = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+                        while (r * (r + 1) / 2 > e) --r;
+                        while ((r + 1) * (r + 2) / 2 <= e) ++r;
+                        const int cc = e - r * (r + 1) / 2;
+                        if (r >= nr || cc >= nc) continue;
+                        double acc = 0.0;
+#pragma unroll 8
+                        for (int kk = 0; kk < NB; ++kk) acc = fma(Li[r][kk], Lj[cc][kk], acc);
+                        T[r][cc] = T[r][cc] - acc;
+                    }
                 }
                 __syncthreads();
             }
@@ -480,37 +520,35 @@ size_t df_ready_words(int n, int has_b) {
 // shared memory from the block's rows of z (final since the previous block),
 // CTA 0 stores it, and the owners of the rows above subtract L_b^T x_b; every
 // value takes the single-CTA sweep's FMAs in the same order, so the results
-// are the same bits. A grid barrier closes each block.
+// are the same bits. A grid barrier closes each block; the next block's
+// inverse is loaded into the other shared buffer before it.
 __global__ void __launch_bounds__(256) chol_backsolve_coop_kernel(double *__restrict__ M, int n, int ld,
                                                                   const double *__restrict__ Dinv,
                                                                   double *__restrict__ x) {
     cooperative_groups::grid_group grid = cooperative_groups::this_grid();
-    __shared__ double Di[NB][NB + 1];
+    __shared__ double Di[2][NB][NB + 1];  // this block's inverse and the next one's, loaded ahead
     __shared__ double yb[NB];
     __shared__ double xb[NB];
     const int tid = threadIdx.x;
     const int r = blockIdx.x * blockDim.x + tid;
     double *z = M + n;  // z[c] at z[c * ld]
     const int nblk = (n + NB - 1) / NB;
+    for (int t = tid; t < NB * NB; t += blockDim.x)
+        Di[(nblk - 1) & 1][t / NB][t % NB] = Dinv[(size_t)(nblk - 1) * NB * NB + t];
     for (int b = nblk - 1; b >= 0; --b) {
-        const int r0 = b * NB, r1 = min(n, r0 + NB);
-        for (int t = tid; t < NB * NB; t += blockDim.x) Di[t / NB][t % NB] = Dinv[(size_t)b * NB * NB + t];
+        const int r0 = b * NB, r1 = min(n, r0 + NB), u = b & 1;
         if (tid < NB) yb[tid] = (r0 + tid < r1) ? z[(size_t)(r0 + tid) * ld] : 0.0;
         __syncthreads();
         if (tid < r1 - r0) {
-            double v = 0.0;
-            for (int c = tid; c < r1 - r0; ++c) v = fma(Di[c][tid], yb[c], v);
+            const double v = sweep_dot(Di[u], yb, tid, r1 - r0);
             xb[tid] = v;
             if (blockIdx.x == 0) x[r0 + tid] = v;
         }
         __syncthreads();
-        if (r < r0) {
-            double v = z[(size_t)r * ld];
-            const double *col = M + (size_t)r * ld;
-#pragma unroll 8
-            for (int c = r0; c < r1; ++c) v = fma(-col[c], xb[c - r0], v);
-            z[(size_t)r * ld] = v;
-        }
+        if (r < r0) z[(size_t)r * ld] = z[(size_t)r * ld] - sweep_row(M + (size_t)r * ld + r0, xb, r1 - r0);
+        if (b > 0)
+            for (int t = tid; t < NB * NB; t += blockDim.x)
+                Di[u ^ 1][t / NB][t % NB] = Dinv[(size_t)(b - 1) * NB * NB + t];
         grid.sync();
     }
 }

@@ -1431,11 +1431,11 @@ __global__ void __launch_bounds__(RS_THREADS, 1) tc_rowsum_ws_kernel(
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
                 const int c_base = h * RS_BN + 128 * g;
                 const int ncol = min(128, N - c_base);
-                for (int c0 = 0; c0 < ncol; c0 += 8) {
-                    float v[8];
-                    tc_ld8_lanes(tmem + b * RS_BN + 128 * g, 32 * ew, c0, v);
+                for (int c0 = 0; c0 < ncol; c0 += 32) {
+                    float v[32];
+                    tc_ld32_lanes(tmem + b * RS_BN + 128 * g, 32 * ew, c0, v);
 #pragma unroll
-                    for (int jj = 0; jj < 8; ++jj) {
+                    for (int jj = 0; jj < 32; ++jj) {
                         const int c = c0 + jj;
                         if (c < ncol) {
                             const float dot = v[jj] * dscale;
