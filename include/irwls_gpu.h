@@ -45,6 +45,29 @@ void irwls_debug_tc_wait(long long limit, int stall);
  * (binary and 8-bit data; the products are then exact), else 3 (hi + mid +
  * lo of the FP32 value). */
 int irwls_last_tc_pieces(void);
+/* Working-set solves of precision-form full IRWLS since the last reset:
+ * those done by the FP32-factor + FP64-refinement cluster solve, and those
+ * whose order fitted it but which went to the FP64 factorization (an FP32
+ * pivot that was not positive, or a refinement that did not converge). */
+void irwls_ws_mixed_counts(long long *solves, long long *fallbacks, int reset);
+/* The precision form's solve of a full-IRWLS working-set system, device
+ * pointers: the bordered matrix [H y; y^T 0] of src/full-train.c:165-186
+ * with H's lower triangle in d_H (n1 x n1, column-major, leading dimension
+ * ld >= n1 + 1) and y in row n1 of the same array, right-hand side d_rhs
+ * (n1 + 1 values); d_x (n1 + 1 values) receives the solution that the
+ * reference's dpotrf/dpotrs call (src/ParallelAlgorithms.c:361-388) gives,
+ * whose last pivot fails by construction: with u = H^-1 y, v = H^-1 r and
+ * s = y^T u, x_n = (r_n - y^T v) / s^2 and x = v - u x_n. H is factored in
+ * FP32 inside one 16-CTA thread-block cluster and the two solves are refined
+ * with FP64 residuals until they reach FP64 accuracy. Runs on the library's
+ * stream and synchronizes it; d_H is not modified. Returns 0 when solved, 1
+ * when the system must be solved in FP64 instead (n1 < 1, n1 above
+ * irwls_ws_mixed_max(), an FP32 pivot that was not positive, or a
+ * refinement that did not converge; d_x is then not a solution), or a
+ * negative error code. irwls_ws_mixed_max() is 512, or 0 when the device
+ * cannot run a 16-CTA cluster. */
+int irwls_ws_solve_mixed(const double *d_H, int n1, int ld, const double *d_rhs, double *d_x);
+int irwls_ws_mixed_max(void);
 /* 1 when a CUDA device is usable. The library has no CPU path: without a
  * device every training or prediction call fails with an error. */
 int irwls_gpu_available(void);

@@ -9,8 +9,23 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "dev_common.cuh"
+#include "irwls_gpu.h"
+
+// Working-set solves of the precision form: by the cluster solve, and
+// handed to the FP64 factorization although their order fitted the cluster.
+static std::atomic<long long> g_ws_mixed_solves{0}, g_ws_mixed_fallbacks{0};
+
+extern "C" void irwls_ws_mixed_counts(long long *solves, long long *fallbacks, int reset) {
+    if (solves) *solves = g_ws_mixed_solves.load();
+    if (fallbacks) *fallbacks = g_ws_mixed_fallbacks.load();
+    if (reset) {
+        g_ws_mixed_solves = 0;
+        g_ws_mixed_fallbacks = 0;
+    }
+}
 
 namespace {
 
@@ -701,7 +716,16 @@ extern "C" int irwls_sub_iterate(irwls_sub_ws *ws, const irwls_dev_set *X, doubl
     }
     build_border_kernel<<<ceil_div(n1 + 1, 256), 256, 0, irwls_stream()>>>(*ws, n1);
     IRWLS_LAUNCH_CHECK("build_border");
-    if (irwls_dev_chol_solve(ws->H, n, ws->ldH, ws->rhs, ws->bsol)) return -2;
+    // precision form: FP32 factor + FP64 refinement in one cluster launch,
+    // the FP64 factorization where that cannot run or does not converge
+    int solve = 1;
+    if (irwls_get_precision() == IRWLS_PRECISION_MIXED) {
+        solve = irwls_ws_solve_mixed(ws->H, n1, ws->ldH, ws->rhs, ws->bsol);
+        if (solve < 0) return -2;
+        g_ws_mixed_solves += solve == 0;
+        g_ws_mixed_fallbacks += solve == 1 && n1 >= 1 && n1 <= irwls_ws_mixed_max();
+    }
+    if (solve == 1 && irwls_dev_chol_solve(ws->H, n, ws->ldH, ws->rhs, ws->bsol)) return -2;
     sub_update_kernel<<<1, CT, 0, irwls_stream()>>>(*ws, C, n1, n3);
     IRWLS_LAUNCH_CHECK("sub_update");
     // e_i -= k(i, j) (bnew_j - beta_j) over changed j, then the bias change

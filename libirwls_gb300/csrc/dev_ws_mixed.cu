@@ -1,0 +1,593 @@
+// dev_ws_mixed.cu -- the precision form's working-set solve of full IRWLS:
+// FP32 Cholesky in one thread-block cluster, FP64 iterative refinement.
+//
+// The reference solves the bordered system
+//
+//   [ H    y ] [ x  ]   [ r   ]
+//   [ y^T  0 ] [ xn ] = [ r_n ]        (src/full-train.c:165-196)
+//
+// by dpotrf + dpotrs (src/ParallelAlgorithms.c:361-388). Its last pivot is
+// -s with s = y^T H^-1 y > 0, which dpotrf stores without a root and
+// reports; dpotrs then solves with that factor, i.e. with the matrix
+// [H y; y^T s + s^2]. Written out by block elimination that solution is
+//
+//   u = H^-1 y,  v = H^-1 r,  s = y^T u,
+//   xn = (r_n - y^T v) / s^2,   x = v - u xn,
+//
+// which this kernel computes with H itself SPD (H = K o y y^T + diag(1/a)).
+// H's working-set systems are well conditioned (condition numbers below
+// 10^3 on the full-IRWLS workloads), so an FP32 factor with FP64 residuals
+// reaches FP64 accuracy in two refinement steps.
+//
+// One cluster of 16 CTAs (a 4 x 4 grid (p, q)) holds H in distributed shared
+// memory as 32 x 32 FP32 blocks, block (i, j) (i >= j) on CTA
+// (i mod 4, j mod 4). Per block column k:
+//   F  the owner of (k, k) factors it (one warp, shuffles; LAPACK's
+//      unblocked right-looking order);
+//   P  the owners of (i, k), i > k, solve L_ik L_kk^T = A_ik by substitution;
+//      the owners of row k of W = L^-1 scale it by L_kk^-1 (substitution);
+//   U  every CTA copies the panel blocks it needs from their owners' shared
+//      memory and applies A_ij -= L_ik L_jk^T (k < j <= i) and
+//      W_ij -= L_ik W_kj (i > k, j <= k) to its own blocks; the owner of
+//      (k + 1, k + 1) then factors it.
+// A cluster barrier separates F/P and P/U. W = L^-1 is formed alongside the
+// factor, so each solve with the factor is two block GEMVs (z = W b,
+// x = W^T z) instead of two triangular sweeps. The refinement residuals
+// b - H x are FP64 over H's FP64 entries in global memory.
+//
+// Every reduction has a fixed order, so the result does not depend on
+// timing. All CTAs run the same sequence of cluster barriers (the control
+// flow depends only on n1 and on values every CTA computes identically).
+// The outcome is reported in device flag word 2: 0 solved, 1 an FP32 pivot
+// was not positive, 2 the refinement did not converge; the caller then
+// solves the system in FP64 instead.
+#include <cooperative_groups.h>
+
+#include <atomic>
+
+#include "dev_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+constexpr int WB = 32;                     // block size
+constexpr int WNB = 16;                    // blocks per dimension: order <= 512
+constexpr int WP = 4, WQ = 4;              // CTA grid of the cluster
+constexpr int WC = WP * WQ;                // cluster size
+constexpr int WT = 512;                    // threads per CTA
+constexpr int WWARPS = WT / 32;
+constexpr int LDB = WB + 1;                // padded row of a stored block
+constexpr int BLK = WB * LDB;              // floats per stored block
+constexpr int SR = WNB / WP, SCOL = WNB / WQ;  // owned row / column blocks per CTA
+constexpr int SLOTS = SR * SCOL;
+constexpr int MAXIT = 5;                   // refinement steps before giving up
+
+// shared-memory layout (floats)
+constexpr int OFF_A = 0;                       // A slots: the factor L
+constexpr int OFF_W = OFF_A + SLOTS * BLK;     // W slots: L^-1
+constexpr int OFF_PL = OFF_W + SLOTS * BLK;    // panel L_ik of my rows, transposed [t][r]
+constexpr int OFF_PC = OFF_PL + SR * WB * WB;  // panel L_jk of my columns [c][t]
+constexpr int OFF_PW = OFF_PC + SCOL * BLK;    // row k of W for my columns [t][c]
+constexpr int OFF_DK = OFF_PW + SCOL * BLK;    // L_kk
+constexpr int OFF_DI = OFF_DK + BLK;           // 1 / L_kk[t][t]
+constexpr int SMEM_FLOATS = OFF_DI + WB;
+constexpr size_t SMEM_BYTES = (size_t)SMEM_FLOATS * sizeof(float);
+
+// after the factorization the A slots and the panel buffers hold the solve's
+// vectors (same offsets in every CTA: partial sums are read remotely)
+constexpr int NV = WNB * WB;                   // padded order
+constexpr int OFF_VEC = OFF_A;                 // doubles: y, r, u, v, rho_u, rho_v
+constexpr int OFF_BF = OFF_VEC + 2 * 6 * NV;   // floats: solve input [2][NV]
+constexpr int OFF_CF = OFF_BF + 2 * NV;        // floats: solve output [2][NV]
+constexpr int OFF_DP = OFF_CF + 2 * NV;        // doubles: per-slot row partials [SLOTS][2][WB]
+constexpr int OFF_DPC = OFF_DP + 2 * SLOTS * 2 * WB;  // doubles: per-slot column partials
+constexpr int OFF_VEND = OFF_DPC + 2 * SLOTS * 2 * WB;
+constexpr int OFF_ZP = OFF_PL;                 // floats: z partials [SR][2][WB]
+constexpr int OFF_ZF = OFF_ZP + SR * 2 * WB;   // floats: reduced z of my rows
+constexpr int OFF_XP = OFF_ZF + SR * 2 * WB;   // floats: x partials [SCOL][2][WB]
+constexpr int OFF_BP = OFF_XP + SCOL * 2 * WB; // floats: per-slot partials [SLOTS][2][WB]
+constexpr int OFF_RR = OFF_BP + SLOTS * 2 * WB;        // doubles: row residual partials [SR][2][WB]
+constexpr int OFF_RC = OFF_RR + 2 * SR * 2 * WB;       // doubles: column residual partials [SCOL][2][WB]
+constexpr int OFF_PEND = OFF_RC + 2 * SCOL * 2 * WB;
+static_assert(OFF_VEND <= OFF_W, "solve vectors overflow the A slots");
+static_assert(OFF_PEND <= SMEM_FLOATS, "partials overflow the panel buffers");
+static_assert((OFF_PL % 4) == 0 && (OFF_RR % 2) == 0 && (OFF_DP % 2) == 0, "alignment");
+
+__device__ __forceinline__ int slot_of(int i, int j) { return (i / WP) * SCOL + (j / WQ); }
+__device__ __forceinline__ int owner_of(int i, int j) { return (i % WP) * WQ + (j % WQ); }
+
+// Factors the stored block in place (lane = row), LAPACK's unblocked
+// right-looking order; the upper part is cleared. Returns true if every pivot
+// was positive.
+__device__ bool factor_warp(float *D, int lane) {
+    float a[WB];
+#pragma unroll
+    for (int t = 0; t < WB; ++t) a[t] = D[lane * LDB + t];
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < WB; ++k) {
+        const float piv = __shfl_sync(0xffffffffu, a[k], k);
+        ok = ok && (piv > 0.f);
+        const float rs = rsqrtf(piv);
+        const float l = a[k] * rs;
+        a[k] = l;
+#pragma unroll
+        for (int j = k + 1; j < WB; ++j) {
+            const float lj = __shfl_sync(0xffffffffu, l, j);
+            a[j] = fmaf(-l, lj, a[j]);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < WB; ++t) D[lane * LDB + t] = t <= lane ? a[t] : 0.f;
+    return ok;
+}
+
+// X L^T = B in place, lane = row of B (B stored [r][t]).
+__device__ void subst_rows(float *B, const float *Dk, const float *dinv, int lane) {
+    float a[WB];
+#pragma unroll
+    for (int t = 0; t < WB; ++t) a[t] = B[lane * LDB + t];
+#pragma unroll
+    for (int s = 0; s < WB; ++s) {
+        a[s] *= dinv[s];
+#pragma unroll
+        for (int t = s + 1; t < WB; ++t) a[t] = fmaf(-a[s], Dk[t * LDB + s], a[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < WB; ++t) B[lane * LDB + t] = a[t];
+}
+
+// L X = B in place, lane = column of B (B stored [t][c]); B = I when `ident`.
+__device__ void subst_cols(float *B, const float *Dk, const float *dinv, int lane, bool ident) {
+    float b[WB];
+#pragma unroll
+    for (int t = 0; t < WB; ++t) b[t] = ident ? (t == lane ? 1.f : 0.f) : B[t * LDB + lane];
+#pragma unroll
+    for (int s = 0; s < WB; ++s) {
+        b[s] *= dinv[s];
+#pragma unroll
+        for (int t = s + 1; t < WB; ++t) b[t] = fmaf(-Dk[t * LDB + s], b[s], b[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < WB; ++t) B[t * LDB + lane] = b[t];
+}
+
+// out[r][c] -= sum_t LT[t][r] R(t, c), lane = c; R(t, c) = R[c][t] (a block of
+// L, `by_t` false) or R[t][c] (a block of W). Sum over t in increasing order.
+__device__ void block_update(float *out, const float *LT, const float *R, bool by_t, int lane) {
+    float acc[WB];
+#pragma unroll
+    for (int r = 0; r < WB; ++r) acc[r] = 0.f;
+#pragma unroll 4
+    for (int t = 0; t < WB; ++t) {
+        const float rv = by_t ? R[t * LDB + lane] : R[lane * LDB + t];
+        const float4 *l4 = (const float4 *)(LT + t * WB);
+#pragma unroll
+        for (int q = 0; q < WB / 4; ++q) {
+            const float4 l = l4[q];
+            acc[4 * q] = fmaf(l.x, rv, acc[4 * q]);
+            acc[4 * q + 1] = fmaf(l.y, rv, acc[4 * q + 1]);
+            acc[4 * q + 2] = fmaf(l.z, rv, acc[4 * q + 2]);
+            acc[4 * q + 3] = fmaf(l.w, rv, acc[4 * q + 3]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < WB; ++r) out[r * LDB + lane] -= acc[r];
+}
+
+// Copies a stored block (BLK floats) from CTA `rank` into dst.
+__device__ void fetch_block(cg::cluster_group &cl, float *dst, float *src_local, int rank, int tid, int nthr) {
+    const float4 *src = (const float4 *)cl.map_shared_rank(src_local, rank);
+    float4 *d = (float4 *)dst;
+    for (int v = tid; v < BLK / 4; v += nthr) d[v] = src[v];
+}
+
+// The same block transposed into dst[t][r] (unpadded).
+__device__ void fetch_block_t(cg::cluster_group &cl, float *dst, float *src_local, int rank, int tid, int nthr) {
+    const float4 *src = (const float4 *)cl.map_shared_rank(src_local, rank);
+    for (int v = tid; v < BLK / 4; v += nthr) {
+        const float4 x = src[v];
+        const float xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int g = 4 * v + u, r = g / LDB, t = g % LDB;
+            if (t < WB) dst[t * WB + r] = xs[u];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restrict__ H, int n1, int ld,
+                                                       const double *__restrict__ rhs, double *__restrict__ x,
+                                                       int *__restrict__ flags) {
+    cg::cluster_group cl = cg::this_cluster();
+    extern __shared__ __align__(16) float sm[];
+    __shared__ int bad_sh;
+    __shared__ double red[WWARPS];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int me = (int)cl.block_rank();
+    const int p = me / WQ, q = me % WQ;
+    const int NB = (n1 + WB - 1) / WB;
+    float *A = sm + OFF_A, *W = sm + OFF_W, *PL = sm + OFF_PL, *PC = sm + OFF_PC, *PW = sm + OFF_PW;
+    float *Dk = sm + OFF_DK, *dinv = sm + OFF_DI;
+    if (tid == 0) bad_sh = 0;
+
+    // ---- load my blocks of H (FP32, identity beyond n1) and W = I ----
+    for (int ib = p; ib < NB; ib += WP)
+        for (int jb = q; jb <= ib; jb += WQ) {
+            float *a = A + slot_of(ib, jb) * BLK, *w = W + slot_of(ib, jb) * BLK;
+            for (int e = tid; e < WB * WB; e += WT) {
+                const int r = e & 31, c = e >> 5, gi = ib * WB + r, gj = jb * WB + c;
+                float v;
+                if (gi < n1 && gj < n1) v = gi >= gj ? __double2float_rn(H[(size_t)gj * ld + gi]) : 0.f;
+                else v = gi == gj ? 1.f : 0.f;
+                a[r * LDB + c] = v;
+                w[r * LDB + c] = gi == gj ? 1.f : 0.f;
+            }
+        }
+    __syncthreads();
+    if (NB > 0 && owner_of(0, 0) == me && warp == 0) {
+        if (!factor_warp(A + slot_of(0, 0) * BLK, lane) && lane == 0) bad_sh = 1;
+    }
+
+    // ---- factorization with W = L^-1 alongside ----
+    for (int k = 0; k < NB; ++k) {
+        cl.sync();  // diagonal block k is factored
+        const int kp = k % WP, kq = k % WQ, dk_owner = owner_of(k, k);
+        const bool col_k = kq == q, row_k = kp == p;
+        if (col_k || row_k) {
+            fetch_block(cl, Dk, A + slot_of(k, k) * BLK, dk_owner, tid, WT);
+            __syncthreads();
+            if (tid < WB) dinv[tid] = __frcp_rn(Dk[tid * LDB + tid]);
+            __syncthreads();
+            // one warp per task: panel rows below k in column k, then row k of W
+            int task = 0;
+            if (col_k)
+                for (int ib = p; ib < NB; ib += WP)
+                    if (ib > k) {
+                        if (task++ % WWARPS == warp) subst_rows(A + slot_of(ib, k) * BLK, Dk, dinv, lane);
+                    }
+            if (row_k)
+                for (int jb = q; jb <= k; jb += WQ)
+                    if (task++ % WWARPS == warp) subst_cols(W + slot_of(k, jb) * BLK, Dk, dinv, lane, jb == k);
+        }
+        __syncthreads();
+        cl.sync();  // column k of L and row k of W are final
+        // panel blocks this CTA's updates read
+        for (int ib = p; ib < NB; ib += WP)
+            if (ib > k) fetch_block_t(cl, PL + (ib / WP) * WB * WB, A + slot_of(ib, k) * BLK, owner_of(ib, k), tid, WT);
+        for (int jb = q; jb < NB; jb += WQ) {
+            if (jb > k) fetch_block(cl, PC + (jb / WQ) * BLK, A + slot_of(jb, k) * BLK, owner_of(jb, k), tid, WT);
+            else fetch_block(cl, PW + (jb / WQ) * BLK, W + slot_of(k, jb) * BLK, owner_of(k, jb), tid, WT);
+        }
+        __syncthreads();
+        int task = 0;
+        for (int ib = p; ib < NB; ib += WP) {
+            if (ib <= k) continue;
+            for (int jb = q; jb <= ib; jb += WQ) {
+                if (task++ % WWARPS != warp) continue;
+                if (jb > k) block_update(A + slot_of(ib, jb) * BLK, PL + (ib / WP) * WB * WB, PC + (jb / WQ) * BLK, false, lane);
+                else block_update(W + slot_of(ib, jb) * BLK, PL + (ib / WP) * WB * WB, PW + (jb / WQ) * BLK, true, lane);
+            }
+        }
+        __syncthreads();
+        if (k + 1 < NB && owner_of(k + 1, k + 1) == me && warp == 0) {
+            if (!factor_warp(A + slot_of(k + 1, k + 1) * BLK, lane) && lane == 0) bad_sh = 1;
+        }
+    }
+    cl.sync();  // nobody reads the A slots remotely any more
+
+    // ---- solves with W and FP64 refinement ----
+    double *vy = (double *)(sm + OFF_VEC), *vr = vy + NV, *vu = vr + NV, *vv = vu + NV, *ru = vv + NV,
+           *rv = ru + NV;
+    float *bf = sm + OFF_BF, *cf = sm + OFF_CF, *zp = sm + OFF_ZP, *zf = sm + OFF_ZF, *xp = sm + OFF_XP,
+          *bp = sm + OFF_BP;
+    double *dp = (double *)(sm + OFF_DP), *dpc = (double *)(sm + OFF_DPC), *rr = (double *)(sm + OFF_RR),
+           *rc = (double *)(sm + OFF_RC);
+    for (int g = tid; g < NV; g += WT) {
+        vy[g] = g < n1 ? H[(size_t)g * ld + n1] : 0.0;
+        vr[g] = g < n1 ? rhs[g] : 0.0;
+    }
+    __syncthreads();
+
+    // (cf[0], cf[1]) = W^T W (bf[0], bf[1]) in FP32
+    auto solve = [&]() {
+        for (int ib = p; ib < NB; ib += WP)
+            for (int jb = q; jb <= ib; jb += WQ) {
+                const int s = slot_of(ib, jb);
+                if (s % WWARPS != warp) continue;
+                const float *w = W + s * BLK;
+                float a0 = 0.f, a1 = 0.f;
+                for (int c = 0; c < WB; ++c) {
+                    const float wv = w[lane * LDB + c];
+                    a0 = fmaf(wv, bf[jb * WB + c], a0);
+                    a1 = fmaf(wv, bf[NV + jb * WB + c], a1);
+                }
+                bp[(s * 2) * WB + lane] = a0;
+                bp[(s * 2 + 1) * WB + lane] = a1;
+            }
+        __syncthreads();
+        if (tid < SR * 2 * WB) {
+            const int a = tid / (2 * WB), h = (tid / WB) & 1, r = tid % WB, ib = p + a * WP;
+            float z = 0.f;
+            if (ib < NB)
+                for (int jb = q; jb <= ib; jb += WQ) z += bp[(slot_of(ib, jb) * 2 + h) * WB + r];
+            zp[(a * 2 + h) * WB + r] = z;
+        }
+        __syncthreads();
+        cl.sync();
+        if (tid < SR * 2 * WB) {
+            float z = 0.f;
+            for (int qq = 0; qq < WQ; ++qq) z += cl.map_shared_rank(zp, p * WQ + qq)[tid];
+            zf[tid] = z;
+        }
+        __syncthreads();
+        for (int ib = p; ib < NB; ib += WP)
+            for (int jb = q; jb <= ib; jb += WQ) {
+                const int s = slot_of(ib, jb);
+                if (s % WWARPS != warp) continue;
+                const float *w = W + s * BLK, *z0 = zf + ((ib / WP) * 2) * WB, *z1 = z0 + WB;
+                float a0 = 0.f, a1 = 0.f;
+                for (int r = 0; r < WB; ++r) {
+                    const float wv = w[r * LDB + lane];
+                    a0 = fmaf(wv, z0[r], a0);
+                    a1 = fmaf(wv, z1[r], a1);
+                }
+                bp[(s * 2) * WB + lane] = a0;
+                bp[(s * 2 + 1) * WB + lane] = a1;
+            }
+        __syncthreads();
+        if (tid < SCOL * 2 * WB) {
+            const int b = tid / (2 * WB), h = (tid / WB) & 1, c = tid % WB, jb = q + b * WQ;
+            float xs = 0.f;
+            if (jb < NB)
+                for (int ib = p; ib < NB; ib += WP)
+                    if (ib >= jb) xs += bp[(slot_of(ib, jb) * 2 + h) * WB + c];
+            xp[(b * 2 + h) * WB + c] = xs;
+        }
+        __syncthreads();
+        cl.sync();
+        for (int e = tid; e < 2 * NB * WB; e += WT) {
+            const int h = e / (NB * WB), g = e % (NB * WB), jb = g / WB, c = g % WB;
+            float xs = 0.f;
+            for (int pp = 0; pp < WP; ++pp)
+                xs += cl.map_shared_rank(xp, pp * WQ + jb % WQ)[((jb / WQ) * 2 + h) * WB + c];
+            cf[h * NV + g] = xs;
+        }
+        __syncthreads();
+    };
+
+    // (ru, rv) = (y, r) - H (u, v) in FP64
+    auto residual = [&]() {
+        for (int ib = p; ib < NB; ib += WP)
+            for (int jb = q; jb <= ib; jb += WQ) {
+                const int s = slot_of(ib, jb);
+                if (s % WWARPS != warp) continue;
+                const int gi = ib * WB + lane;
+                double a0 = 0.0, a1 = 0.0;
+                for (int c = 0; c < WB; ++c) {
+                    const int gj = jb * WB + c;
+                    double h = 0.0;
+                    if (gi < n1 && gj < n1) h = gi >= gj ? H[(size_t)gj * ld + gi] : H[(size_t)gi * ld + gj];
+                    a0 = fma(h, vu[gj], a0);
+                    a1 = fma(h, vv[gj], a1);
+                }
+                dp[(s * 2) * WB + lane] = a0;
+                dp[(s * 2 + 1) * WB + lane] = a1;
+                if (ib > jb) {
+                    const int gj = jb * WB + lane;
+                    double c0 = 0.0, c1 = 0.0;
+                    for (int r = 0; r < WB; ++r) {
+                        const int gr = ib * WB + r;
+                        const double h = (gr < n1 && gj < n1) ? H[(size_t)gj * ld + gr] : 0.0;
+                        c0 = fma(h, vu[gr], c0);
+                        c1 = fma(h, vv[gr], c1);
+                    }
+                    dpc[(s * 2) * WB + lane] = c0;
+                    dpc[(s * 2 + 1) * WB + lane] = c1;
+                }
+            }
+        __syncthreads();
+        if (tid < SR * 2 * WB) {
+            const int a = tid / (2 * WB), h = (tid / WB) & 1, r = tid % WB, ib = p + a * WP;
+            double t = 0.0;
+            if (ib < NB)
+                for (int jb = q; jb <= ib; jb += WQ) t += dp[(slot_of(ib, jb) * 2 + h) * WB + r];
+            rr[(a * 2 + h) * WB + r] = t;
+        } else if (tid < SR * 2 * WB + SCOL * 2 * WB) {
+            const int u = tid - SR * 2 * WB;
+            const int b = u / (2 * WB), h = (u / WB) & 1, c = u % WB, jb = q + b * WQ;
+            double t = 0.0;
+            if (jb < NB)
+                for (int ib = p; ib < NB; ib += WP)
+                    if (ib > jb) t += dpc[(slot_of(ib, jb) * 2 + h) * WB + c];
+            rc[(b * 2 + h) * WB + c] = t;
+        }
+        __syncthreads();
+        cl.sync();
+        for (int e = tid; e < 2 * NB * WB; e += WT) {
+            const int h = e / (NB * WB), g = e % (NB * WB), ib = g / WB, r = g % WB;
+            double t = 0.0;
+            for (int qq = 0; qq < WQ; ++qq)
+                t += cl.map_shared_rank(rr, (ib % WP) * WQ + qq)[((ib / WP) * 2 + h) * WB + r];
+            for (int pp = 0; pp < WP; ++pp)
+                t += cl.map_shared_rank(rc, pp * WQ + ib % WQ)[((ib / WQ) * 2 + h) * WB + r];
+            (h ? rv : ru)[g] = (h ? vr : vy)[g] - t;
+        }
+        __syncthreads();
+    };
+
+    // max |v| over the first n1 entries of a full vector (every CTA alike)
+    auto maxabs = [&](const double *v) {
+        double m = 0.0;
+        for (int g = tid; g < n1; g += WT) m = fmax(m, fabs(v[g]));
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        __syncthreads();
+        if (lane == 0) red[warp] = m;
+        __syncthreads();
+        double t = 0.0;
+        for (int w = 0; w < WWARPS; ++w) t = fmax(t, red[w]);
+        __syncthreads();
+        return t;
+    };
+
+    for (int g = tid; g < NV; g += WT) {
+        bf[g] = __double2float_rn(vy[g]);
+        bf[NV + g] = __double2float_rn(vr[g]);
+    }
+    __syncthreads();
+    solve();
+    for (int g = tid; g < NV; g += WT) {
+        vu[g] = (double)cf[g];
+        vv[g] = (double)cf[NV + g];
+    }
+    __syncthreads();
+    double last_u = maxabs(vu), last_v = maxabs(vv);
+    bool converged = false;
+    for (int it = 0; it < MAXIT && !converged; ++it) {
+        residual();
+        for (int g = tid; g < NV; g += WT) {
+            bf[g] = __double2float_rn(ru[g]);
+            bf[NV + g] = __double2float_rn(rv[g]);
+        }
+        __syncthreads();
+        solve();
+        for (int g = tid; g < NV; g += WT) {
+            vu[g] += (double)cf[g];
+            vv[g] += (double)cf[NV + g];
+        }
+        __syncthreads();
+        // the correction just applied, and the next one it predicts
+        // (|c_k|^2 / |c_{k-1}| for a linearly converging iteration)
+        for (int g = tid; g < NV; g += WT) {
+            ru[g] = (double)cf[g];
+            rv[g] = (double)cf[NV + g];
+        }
+        __syncthreads();
+        const double cu = maxabs(ru), cv = maxabs(rv), nu = maxabs(vu), nv = maxabs(vv);
+        const double tol = 0x1p-44;
+        const bool ok_u = cu == 0.0 || (cu <= 0.5 * last_u && cu * cu <= tol * nu * last_u);
+        const bool ok_v = cv == 0.0 || (cv <= 0.5 * last_v && cv * cv <= tol * nv * last_v);
+        converged = ok_u && ok_v;
+        last_u = cu;
+        last_v = cv;
+    }
+
+    // ---- the bordered system's solution, and the status ----
+    if (me == 0) {
+        double s = 0.0, yv = 0.0;
+        // fixed-order sums: per thread over a stride, then the warps in order
+        for (int g = tid; g < n1; g += WT) {
+            s = fma(vy[g], vu[g], s);
+            yv = fma(vy[g], vv[g], yv);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+            yv += __shfl_xor_sync(0xffffffffu, yv, o);
+        }
+        __shared__ double red2[2][WWARPS];
+        if (lane == 0) {
+            red2[0][warp] = s;
+            red2[1][warp] = yv;
+        }
+        __syncthreads();
+        double ss = 0.0, yvs = 0.0;
+        for (int w = 0; w < WWARPS; ++w) {
+            ss += red2[0][w];
+            yvs += red2[1][w];
+        }
+        const double xn = (rhs[n1] - yvs) / (ss * ss);
+        for (int g = tid; g < n1; g += WT) x[g] = fma(-vu[g], xn, vv[g]);
+        if (tid == 0) x[n1] = xn;
+    }
+    cl.sync();  // every remote read of this CTA's shared memory is done
+    if (me == 0 && tid == 0) {
+        int bad = 0;
+        for (int r = 0; r < WC; ++r) bad |= *cl.map_shared_rank(&bad_sh, r);
+        flags[2] = bad ? 1 : (converged ? 0 : 2);
+    }
+    cl.sync();
+}
+
+// Whether a 16-CTA cluster of this kernel can be resident on the current
+// device (checked once per device).
+bool cluster_ok() {
+    constexpr int kDevices = 64;
+    static std::atomic<int> state[kDevices];  // 0 unknown, 1 no, 2 yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) {
+        cudaGetLastError();
+        return false;
+    }
+    int s = state[dev].load(std::memory_order_acquire);
+    if (s == 0) {
+        bool ok = cudaFuncSetAttribute(ws_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) ==
+                      cudaSuccess &&
+                  cudaFuncSetAttribute(ws_mixed_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+        if (ok) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = WC;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(WC);
+            cfg.blockDim = dim3(WT);
+            cfg.dynamicSmemBytes = SMEM_BYTES;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nc = 0;
+            ok = cudaOccupancyMaxActiveClusters(&nc, ws_mixed_kernel, &cfg) == cudaSuccess && nc >= 1;
+        }
+        cudaGetLastError();
+        s = ok ? 2 : 1;
+        state[dev].store(s, std::memory_order_release);
+    }
+    return s == 2;
+}
+
+}  // namespace
+
+// Largest working set the cluster solve takes (0 when the device cannot run
+// the cluster).
+extern "C" int irwls_ws_mixed_max(void) { return cluster_ok() ? WNB * WB : 0; }
+
+// The bordered working-set system of full IRWLS in the precision form: H's
+// lower triangle (n1 x n1, column-major, leading dimension ld), the border
+// y in row n1 of the same array, right-hand side rhs (n1 + 1 values); the
+// solution goes to x (n1 + 1 values). Returns 0 when solved, 1 when the FP32
+// factor or the refinement failed (x is then not written with a valid
+// solution and the caller solves in FP64), a negative code on a launch error.
+// Synchronizes the stream to read the outcome.
+extern "C" int irwls_ws_solve_mixed(const double *d_H, int n1, int ld, const double *d_rhs, double *d_x) {
+    if (n1 < 1 || n1 > WNB * WB || ld < n1 + 1 || !cluster_ok()) return 1;
+    int *flags = irwls_dev_flags();
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = WC;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(WC);
+    cfg.blockDim = dim3(WT);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.stream = irwls_stream();
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_CHOL);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, ws_mixed_kernel, d_H, n1, ld, d_rhs, d_x, flags);
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_CHOL);
+    if (e != cudaSuccess) {
+        irwls_set_error(-2, "working-set cluster solve launch: %s", cudaGetErrorString(e));
+        return -2;
+    }
+    IRWLS_LAUNCH_CHECK("ws_mixed");
+    int st = -1;
+    e = cudaMemcpyAsync(&st, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, irwls_stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(irwls_stream());
+    if (e != cudaSuccess) {
+        irwls_set_error(-2, "working-set cluster solve: %s", cudaGetErrorString(e));
+        return -2;
+    }
+    return st == 0 ? 0 : 1;
+}

@@ -124,10 +124,12 @@ int irwls_dev_kernel_block_t(const irwls_dev_set *A, const int *d_ia, int nA, co
  * non-NULL the right-hand side is row n of M (copied there from d_b when d_b
  * is non-NULL) and the solution of L L^T x = b is written to d_x. */
 int irwls_dev_chol_solve(double *d_M, int n, int ld, const double *d_b, double *d_x);
+/* The first failed pivot (1-based, 0 if none) of the last factorization in
+ * *info; synchronous. */
 int irwls_dev_chol_info(int *info);
 int irwls_dev_zero_upper(double *d_M, int n, int ld);
 /* out = A v (trans 0) or A^T v (trans 1), A column-major size x size. */
-int irwls_dev_gemv(const double *d_A, const double *d_v, double *d_out, int size, int trans);   /* synchronous; 0 or the first failed pivot (1-based) */
+int irwls_dev_gemv(const double *d_A, const double *d_v, double *d_out, int size, int trans);
 
 /* ---- full IRWLS steps (dev_full.cu) -------------------------------------- */
 typedef struct irwls_sub_stats {
