@@ -77,8 +77,8 @@ constexpr size_t SMEM_BYTES = (size_t)SMEM_FLOATS * sizeof(float);
 // after the factorization the A slots and the panel buffers hold the solve's
 // vectors (same offsets in every CTA: partial sums are read remotely)
 constexpr int NV = WNB * WB;                   // padded order
-constexpr int OFF_VEC = OFF_A;                 // doubles: y, r, u, v, rho_u, rho_v
-constexpr int OFF_BF = OFF_VEC + 2 * 6 * NV;   // floats: solve input [2][NV]
+constexpr int OFF_VEC = OFF_A;                 // doubles: y, r, u, v
+constexpr int OFF_BF = OFF_VEC + 2 * 4 * NV;   // floats: solve input [2][NV]
 constexpr int OFF_CF = OFF_BF + 2 * NV;        // floats: solve output [2][NV]
 constexpr int OFF_DP = OFF_CF + 2 * NV;        // doubles: per-slot row partials [SLOTS][2][WB]
 constexpr int OFF_DPC = OFF_DP + 2 * SLOTS * 2 * WB;  // doubles: per-slot column partials
@@ -183,16 +183,63 @@ __device__ void fetch_block(cg::cluster_group &cl, float *dst, float *src_local,
     for (int v = tid; v < BLK / 4; v += nthr) d[v] = src[v];
 }
 
-// The same block transposed into dst[t][r] (unpadded).
-__device__ void fetch_block_t(cg::cluster_group &cl, float *dst, float *src_local, int rank, int tid, int nthr) {
-    const float4 *src = (const float4 *)cl.map_shared_rank(src_local, rank);
-    for (int v = tid; v < BLK / 4; v += nthr) {
-        const float4 x = src[v];
-        const float xs[4] = {x.x, x.y, x.z, x.w};
+constexpr int Q4 = BLK / 4;  // 16-byte pieces of a stored block
+
+// The panel blocks of step k that this CTA's updates read, copied from their
+// owners' shared memory with all copies in flight together: L_ik of its row
+// blocks i > k (transposed, PL), L_jk of its column blocks j > k (PC) and
+// W_kj of its column blocks j <= k (PW).
+__device__ void fetch_panels(cg::cluster_group &cl, float *A, float *W, float *PL, float *PC, float *PW, int k,
+                             int NB, int p, int q, int tid) {
+    const int i0 = k + 1 + ((p - (k + 1)) % WP + WP) % WP;  // first row block > k of this CTA
+    const int j0 = k + 1 + ((q - (k + 1)) % WQ + WQ) % WQ;  // first column block > k
+    const int nPL = i0 < NB ? (NB - 1 - i0) / WP + 1 : 0;
+    const int nPC = j0 < NB ? (NB - 1 - j0) / WQ + 1 : 0;
+    const int nPW = q <= k ? (k - q) / WQ + 1 : 0;
+    const int total = (nPL + nPC + nPW) * Q4;
+    constexpr int PF = 8;  // pieces per thread per round, loaded before any is stored
+    for (int base = 0; base < total; base += PF * WT) {
+        float4 buf[PF];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int g = 4 * v + u, r = g / LDB, t = g % LDB;
-            if (t < WB) dst[t * WB + r] = xs[u];
+        for (int u = 0; u < PF; ++u) {
+            const int v = base + u * WT + tid;
+            if (v >= total) continue;
+            const int f = v / Q4, o = v % Q4;
+            const float *src;
+            int rank;
+            if (f < nPL) {
+                const int ib = i0 + f * WP;
+                src = A + slot_of(ib, k) * BLK;
+                rank = owner_of(ib, k);
+            } else if (f < nPL + nPC) {
+                const int jb = j0 + (f - nPL) * WQ;
+                src = A + slot_of(jb, k) * BLK;
+                rank = owner_of(jb, k);
+            } else {
+                const int jb = q + (f - nPL - nPC) * WQ;
+                src = W + slot_of(k, jb) * BLK;
+                rank = owner_of(k, jb);
+            }
+            buf[u] = ((const float4 *)cl.map_shared_rank(src, rank))[o];
+        }
+#pragma unroll
+        for (int u = 0; u < PF; ++u) {
+            const int v = base + u * WT + tid;
+            if (v >= total) continue;
+            const int f = v / Q4, o = v % Q4;
+            if (f < nPL) {
+                float *dst = PL + ((i0 + f * WP) / WP) * WB * WB;
+                const float xs[4] = {buf[u].x, buf[u].y, buf[u].z, buf[u].w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int g = 4 * o + e, r = g / LDB, t = g % LDB;
+                    if (t < WB) dst[t * WB + r] = xs[e];
+                }
+            } else if (f < nPL + nPC) {
+                ((float4 *)(PC + ((j0 + (f - nPL) * WQ) / WQ) * BLK))[o] = buf[u];
+            } else {
+                ((float4 *)(PW + ((q + (f - nPL - nPC) * WQ) / WQ) * BLK))[o] = buf[u];
+            }
         }
     }
 }
@@ -202,8 +249,9 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
                                                        int *__restrict__ flags) {
     cg::cluster_group cl = cg::this_cluster();
     extern __shared__ __align__(16) float sm[];
-    __shared__ int bad_sh;
-    __shared__ double red[WWARPS];
+    __shared__ int bad_sh, flag_sh;
+    __shared__ float redf[WWARPS];
+    __shared__ double xn_sh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int me = (int)cl.block_rank();
     const int p = me / WQ, q = me % WQ;
@@ -253,33 +301,33 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
         }
         __syncthreads();
         cl.sync();  // column k of L and row k of W are final
-        // panel blocks this CTA's updates read
-        for (int ib = p; ib < NB; ib += WP)
-            if (ib > k) fetch_block_t(cl, PL + (ib / WP) * WB * WB, A + slot_of(ib, k) * BLK, owner_of(ib, k), tid, WT);
-        for (int jb = q; jb < NB; jb += WQ) {
-            if (jb > k) fetch_block(cl, PC + (jb / WQ) * BLK, A + slot_of(jb, k) * BLK, owner_of(jb, k), tid, WT);
-            else fetch_block(cl, PW + (jb / WQ) * BLK, W + slot_of(k, jb) * BLK, owner_of(k, jb), tid, WT);
-        }
+        fetch_panels(cl, A, W, PL, PC, PW, k, NB, p, q, tid);
         __syncthreads();
+        // the next diagonal block first, by warp 0, which then factors it
+        // while the other warps apply the remaining updates
+        const bool own_next = k + 1 < NB && owner_of(k + 1, k + 1) == me;
         int task = 0;
         for (int ib = p; ib < NB; ib += WP) {
             if (ib <= k) continue;
             for (int jb = q; jb <= ib; jb += WQ) {
-                if (task++ % WWARPS != warp) continue;
+                int w;
+                if (own_next && ib == k + 1 && jb == k + 1) w = 0;
+                else w = own_next ? 1 + task++ % (WWARPS - 1) : task++ % WWARPS;
+                if (w != warp) continue;
                 if (jb > k) block_update(A + slot_of(ib, jb) * BLK, PL + (ib / WP) * WB * WB, PC + (jb / WQ) * BLK, false, lane);
                 else block_update(W + slot_of(ib, jb) * BLK, PL + (ib / WP) * WB * WB, PW + (jb / WQ) * BLK, true, lane);
             }
         }
-        __syncthreads();
-        if (k + 1 < NB && owner_of(k + 1, k + 1) == me && warp == 0) {
+        if (own_next && warp == 0) {
+            __syncwarp();
             if (!factor_warp(A + slot_of(k + 1, k + 1) * BLK, lane) && lane == 0) bad_sh = 1;
         }
+        __syncthreads();
     }
     cl.sync();  // nobody reads the A slots remotely any more
 
     // ---- solves with W and FP64 refinement ----
-    double *vy = (double *)(sm + OFF_VEC), *vr = vy + NV, *vu = vr + NV, *vv = vu + NV, *ru = vv + NV,
-           *rv = ru + NV;
+    double *vy = (double *)(sm + OFF_VEC), *vr = vy + NV, *vu = vr + NV, *vv = vu + NV;
     float *bf = sm + OFF_BF, *cf = sm + OFF_CF, *zp = sm + OFF_ZP, *zf = sm + OFF_ZF, *xp = sm + OFF_XP,
           *bp = sm + OFF_BP;
     double *dp = (double *)(sm + OFF_DP), *dpc = (double *)(sm + OFF_DPC), *rr = (double *)(sm + OFF_RR),
@@ -347,41 +395,60 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
         }
         __syncthreads();
         cl.sync();
-        for (int e = tid; e < 2 * NB * WB; e += WT) {
-            const int h = e / (NB * WB), g = e % (NB * WB), jb = g / WB, c = g % WB;
+        for (int e = tid; e < 2 * NV; e += WT) {
+            const int h = e / NV, g = e % NV, jb = g / WB, c = g % WB;
             float xs = 0.f;
-            for (int pp = 0; pp < WP; ++pp)
-                xs += cl.map_shared_rank(xp, pp * WQ + jb % WQ)[((jb / WQ) * 2 + h) * WB + c];
+            if (jb < NB)
+                for (int pp = 0; pp < WP; ++pp)
+                    xs += cl.map_shared_rank(xp, pp * WQ + jb % WQ)[((jb / WQ) * 2 + h) * WB + c];
             cf[h * NV + g] = xs;
         }
         __syncthreads();
     };
 
-    // (ru, rv) = (y, r) - H (u, v) in FP64
+    // (y, r) - H (u, v) in FP64, rounded to FP32 into bf for the next solve
     auto residual = [&]() {
         for (int ib = p; ib < NB; ib += WP)
             for (int jb = q; jb <= ib; jb += WQ) {
                 const int s = slot_of(ib, jb);
                 if (s % WWARPS != warp) continue;
+                // H is read in halves of 16 entries per lane, all loads of a
+                // half in flight before its FMAs (in increasing index order)
                 const int gi = ib * WB + lane;
                 double a0 = 0.0, a1 = 0.0;
-                for (int c = 0; c < WB; ++c) {
-                    const int gj = jb * WB + c;
-                    double h = 0.0;
-                    if (gi < n1 && gj < n1) h = gi >= gj ? H[(size_t)gj * ld + gi] : H[(size_t)gi * ld + gj];
-                    a0 = fma(h, vu[gj], a0);
-                    a1 = fma(h, vv[gj], a1);
+#pragma unroll
+                for (int h0 = 0; h0 < WB; h0 += 16) {
+                    double hv[16];
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        const int gj = jb * WB + h0 + c;
+                        hv[c] = (gi < n1 && gj < n1) ? (gi >= gj ? H[(size_t)gj * ld + gi] : H[(size_t)gi * ld + gj])
+                                                     : 0.0;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        a0 = fma(hv[c], vu[jb * WB + h0 + c], a0);
+                        a1 = fma(hv[c], vv[jb * WB + h0 + c], a1);
+                    }
                 }
                 dp[(s * 2) * WB + lane] = a0;
                 dp[(s * 2 + 1) * WB + lane] = a1;
                 if (ib > jb) {
                     const int gj = jb * WB + lane;
                     double c0 = 0.0, c1 = 0.0;
-                    for (int r = 0; r < WB; ++r) {
-                        const int gr = ib * WB + r;
-                        const double h = (gr < n1 && gj < n1) ? H[(size_t)gj * ld + gr] : 0.0;
-                        c0 = fma(h, vu[gr], c0);
-                        c1 = fma(h, vv[gr], c1);
+#pragma unroll
+                    for (int h0 = 0; h0 < WB; h0 += 16) {
+                        double hv[16];
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) {
+                            const int gr = ib * WB + h0 + r;
+                            hv[r] = (gr < n1 && gj < n1) ? H[(size_t)gj * ld + gr] : 0.0;
+                        }
+#pragma unroll
+                        for (int r = 0; r < 16; ++r) {
+                            c0 = fma(hv[r], vu[ib * WB + h0 + r], c0);
+                            c1 = fma(hv[r], vv[ib * WB + h0 + r], c1);
+                        }
                     }
                     dpc[(s * 2) * WB + lane] = c0;
                     dpc[(s * 2 + 1) * WB + lane] = c1;
@@ -405,29 +472,33 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
         }
         __syncthreads();
         cl.sync();
-        for (int e = tid; e < 2 * NB * WB; e += WT) {
-            const int h = e / (NB * WB), g = e % (NB * WB), ib = g / WB, r = g % WB;
+        // the next solve reads the residual of this CTA's column blocks only
+        const int ncq = q < NB ? (NB - 1 - q) / WQ + 1 : 0;
+        for (int e = tid; e < 2 * ncq * WB; e += WT) {
+            const int h = e / (ncq * WB), u = e % (ncq * WB), ib = q + (u / WB) * WQ, r = u % WB;
+            const int g = ib * WB + r;
             double t = 0.0;
             for (int qq = 0; qq < WQ; ++qq)
                 t += cl.map_shared_rank(rr, (ib % WP) * WQ + qq)[((ib / WP) * 2 + h) * WB + r];
             for (int pp = 0; pp < WP; ++pp)
-                t += cl.map_shared_rank(rc, pp * WQ + ib % WQ)[((ib / WQ) * 2 + h) * WB + r];
-            (h ? rv : ru)[g] = (h ? vr : vy)[g] - t;
+                t += cl.map_shared_rank(rc, pp * WQ + q)[((ib / WQ) * 2 + h) * WB + r];
+            bf[h * NV + g] = __double2float_rn((h ? vr : vy)[g] - t);
         }
         __syncthreads();
     };
 
-    // max |v| over the first n1 entries of a full vector (every CTA alike)
-    auto maxabs = [&](const double *v) {
-        double m = 0.0;
-        for (int g = tid; g < n1; g += WT) m = fmax(m, fabs(v[g]));
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    // max |v| over the first n1 entries of an FP32 vector (every CTA alike;
+    // FP32 because every FP64 operation repeated by 512 threads costs about
+    // 0.2 us on this part's FP64 pipe)
+    auto maxabs_f = [&](const float *v) {
+        float m = 0.f;
+        for (int g = tid; g < n1; g += WT) m = fmaxf(m, fabsf(v[g]));
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
         __syncthreads();
-        if (lane == 0) red[warp] = m;
+        if (lane == 0) redf[warp] = m;
         __syncthreads();
-        double t = 0.0;
-        for (int w = 0; w < WWARPS; ++w) t = fmax(t, red[w]);
-        __syncthreads();
+        float t = 0.f;
+        for (int w = 0; w < WWARPS; ++w) t = fmaxf(t, redf[w]);
         return t;
     };
 
@@ -441,62 +512,51 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
         vu[g] = (double)cf[g];
         vv[g] = (double)cf[NV + g];
     }
-    __syncthreads();
-    double last_u = maxabs(vu), last_v = maxabs(vv);
+    // the first solve's sizes stand for |u| and |v| in the stop test
+    const float nu = maxabs_f(cf), nv = maxabs_f(cf + NV);
+    float last_u = nu, last_v = nv;
     bool converged = false;
     for (int it = 0; it < MAXIT && !converged; ++it) {
         residual();
-        for (int g = tid; g < NV; g += WT) {
-            bf[g] = __double2float_rn(ru[g]);
-            bf[NV + g] = __double2float_rn(rv[g]);
-        }
-        __syncthreads();
         solve();
         for (int g = tid; g < NV; g += WT) {
             vu[g] += (double)cf[g];
             vv[g] += (double)cf[NV + g];
         }
-        __syncthreads();
         // the correction just applied, and the next one it predicts
         // (|c_k|^2 / |c_{k-1}| for a linearly converging iteration)
-        for (int g = tid; g < NV; g += WT) {
-            ru[g] = (double)cf[g];
-            rv[g] = (double)cf[NV + g];
+        const float cu = maxabs_f(cf), cv = maxabs_f(cf + NV);
+        if (tid == 0) {
+            const double tol = 0x1p-40;
+            const bool ok_u = cu == 0.f || (cu <= 0.5f * last_u && (double)cu * cu <= tol * nu * last_u);
+            const bool ok_v = cv == 0.f || (cv <= 0.5f * last_v && (double)cv * cv <= tol * nv * last_v);
+            flag_sh = ok_u && ok_v;
         }
         __syncthreads();
-        const double cu = maxabs(ru), cv = maxabs(rv), nu = maxabs(vu), nv = maxabs(vv);
-        const double tol = 0x1p-44;
-        const bool ok_u = cu == 0.0 || (cu <= 0.5 * last_u && cu * cu <= tol * nu * last_u);
-        const bool ok_v = cv == 0.0 || (cv <= 0.5 * last_v && cv * cv <= tol * nv * last_v);
-        converged = ok_u && ok_v;
+        converged = flag_sh != 0;
         last_u = cu;
         last_v = cv;
+        __syncthreads();
     }
 
     // ---- the bordered system's solution, and the status ----
     if (me == 0) {
-        double s = 0.0, yv = 0.0;
-        // fixed-order sums: per thread over a stride, then the warps in order
-        for (int g = tid; g < n1; g += WT) {
-            s = fma(vy[g], vu[g], s);
-            yv = fma(vy[g], vv[g], yv);
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            s += __shfl_xor_sync(0xffffffffu, s, o);
-            yv += __shfl_xor_sync(0xffffffffu, yv, o);
-        }
-        __shared__ double red2[2][WWARPS];
-        if (lane == 0) {
-            red2[0][warp] = s;
-            red2[1][warp] = yv;
+        // s = y.u and y.v by warp 0: lane sums over a stride, then a fixed
+        // shuffle tree
+        if (warp == 0) {
+            double s = 0.0, yv = 0.0;
+            for (int g = lane; g < n1; g += 32) {
+                s = fma(vy[g], vu[g], s);
+                yv = fma(vy[g], vv[g], yv);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                s += __shfl_xor_sync(0xffffffffu, s, o);
+                yv += __shfl_xor_sync(0xffffffffu, yv, o);
+            }
+            if (lane == 0) xn_sh = (rhs[n1] - yv) / (s * s);
         }
         __syncthreads();
-        double ss = 0.0, yvs = 0.0;
-        for (int w = 0; w < WWARPS; ++w) {
-            ss += red2[0][w];
-            yvs += red2[1][w];
-        }
-        const double xn = (rhs[n1] - yvs) / (ss * ss);
+        const double xn = xn_sh;
         for (int g = tid; g < n1; g += WT) x[g] = fma(-vu[g], xn, vv[g]);
         if (tid == 0) x[n1] = xn;
     }
