@@ -46,6 +46,7 @@
 #include <atomic>
 
 #include "dev_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -69,8 +70,9 @@ constexpr int OFF_W = OFF_A + SLOTS * BLK;     // W slots: L^-1
 constexpr int OFF_PL = OFF_W + SLOTS * BLK;    // panel L_ik of my rows, transposed [t][r]
 constexpr int OFF_PC = OFF_PL + SR * WB * WB;  // panel L_jk of my columns [c][t]
 constexpr int OFF_PW = OFF_PC + SCOL * BLK;    // row k of W for my columns [t][c]
-constexpr int OFF_DK = OFF_PW + SCOL * BLK;    // L_kk
-constexpr int OFF_DI = OFF_DK + BLK;           // 1 / L_kk[t][t]
+constexpr int OFF_DK = OFF_PW + SCOL * BLK;    // L_kk, two buffers (step parity)
+constexpr int OFF_STG = OFF_DK + 2 * BLK;      // my panel blocks transposed, for sending
+constexpr int OFF_DI = OFF_STG + SR * WB * WB; // 1 / L_kk[t][t]
 constexpr int SMEM_FLOATS = OFF_DI + WB;
 constexpr size_t SMEM_BYTES = (size_t)SMEM_FLOATS * sizeof(float);
 
@@ -176,72 +178,55 @@ __device__ void block_update(float *out, const float *LT, const float *R, bool b
     for (int r = 0; r < WB; ++r) out[r * LDB + lane] -= acc[r];
 }
 
-// Copies a stored block (BLK floats) from CTA `rank` into dst.
-__device__ void fetch_block(cg::cluster_group &cl, float *dst, float *src_local, int rank, int tid, int nthr) {
-    const float4 *src = (const float4 *)cl.map_shared_rank(src_local, rank);
-    float4 *d = (float4 *)dst;
-    for (int v = tid; v < BLK / 4; v += nthr) d[v] = src[v];
+constexpr long long WS_WAIT_LIMIT = 1LL << 22;  // polls of a data wait before it gives up
+
+// The shared::cluster address, in CTA `rank`, of a local shared address (the
+// layout is the same in every CTA).
+__device__ __forceinline__ uint32_t cl_addr(uint32_t local, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
 }
 
-constexpr int Q4 = BLK / 4;  // 16-byte pieces of a stored block
+// Sends `bytes` of this CTA's shared memory at src to the same offset dst in
+// CTA `rank` with the bulk-copy engine; the copy completes on that CTA's
+// mbarrier at offset bar. The caller has made the source visible to the
+// async proxy (fence.proxy.async after the writes).
+__device__ __forceinline__ void send(uint32_t dst, uint32_t src, uint32_t bytes, uint32_t bar, int rank) {
+    asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     cl_addr(dst, rank)),
+                 "r"(src), "r"(bytes), "r"(cl_addr(bar, rank))
+                 : "memory");
+}
 
-// The panel blocks of step k that this CTA's updates read, copied from their
-// owners' shared memory with all copies in flight together: L_ik of its row
-// blocks i > k (transposed, PL), L_jk of its column blocks j > k (PC) and
-// W_kj of its column blocks j <= k (PW).
-__device__ void fetch_panels(cg::cluster_group &cl, float *A, float *W, float *PL, float *PC, float *PW, int k,
-                             int NB, int p, int q, int tid) {
-    const int i0 = k + 1 + ((p - (k + 1)) % WP + WP) % WP;  // first row block > k of this CTA
-    const int j0 = k + 1 + ((q - (k + 1)) % WQ + WQ) % WQ;  // first column block > k
+__device__ __forceinline__ void expect_bytes(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the phase of parity `parity` of the mbarrier at bar.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity) {
+    uint32_t done = 0;
+    for (long long it = 0; it < WS_WAIT_LIMIT && !done; ++it)
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// Panel blocks of step k that CTA (p, q) receives: L_ik of its row blocks
+// i > k (transposed, 4 KB each), L_jk of its column blocks j > k and W_kj of
+// its column blocks j <= k (4224 bytes each).
+__device__ __forceinline__ uint32_t panel_bytes(int k, int NB, int p, int q) {
+    const int i0 = k + 1 + ((p - (k + 1)) % WP + WP) % WP;
+    const int j0 = k + 1 + ((q - (k + 1)) % WQ + WQ) % WQ;
     const int nPL = i0 < NB ? (NB - 1 - i0) / WP + 1 : 0;
     const int nPC = j0 < NB ? (NB - 1 - j0) / WQ + 1 : 0;
     const int nPW = q <= k ? (k - q) / WQ + 1 : 0;
-    const int total = (nPL + nPC + nPW) * Q4;
-    constexpr int PF = 8;  // pieces per thread per round, loaded before any is stored
-    for (int base = 0; base < total; base += PF * WT) {
-        float4 buf[PF];
-#pragma unroll
-        for (int u = 0; u < PF; ++u) {
-            const int v = base + u * WT + tid;
-            if (v >= total) continue;
-            const int f = v / Q4, o = v % Q4;
-            const float *src;
-            int rank;
-            if (f < nPL) {
-                const int ib = i0 + f * WP;
-                src = A + slot_of(ib, k) * BLK;
-                rank = owner_of(ib, k);
-            } else if (f < nPL + nPC) {
-                const int jb = j0 + (f - nPL) * WQ;
-                src = A + slot_of(jb, k) * BLK;
-                rank = owner_of(jb, k);
-            } else {
-                const int jb = q + (f - nPL - nPC) * WQ;
-                src = W + slot_of(k, jb) * BLK;
-                rank = owner_of(k, jb);
-            }
-            buf[u] = ((const float4 *)cl.map_shared_rank(src, rank))[o];
-        }
-#pragma unroll
-        for (int u = 0; u < PF; ++u) {
-            const int v = base + u * WT + tid;
-            if (v >= total) continue;
-            const int f = v / Q4, o = v % Q4;
-            if (f < nPL) {
-                float *dst = PL + ((i0 + f * WP) / WP) * WB * WB;
-                const float xs[4] = {buf[u].x, buf[u].y, buf[u].z, buf[u].w};
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int g = 4 * o + e, r = g / LDB, t = g % LDB;
-                    if (t < WB) dst[t * WB + r] = xs[e];
-                }
-            } else if (f < nPL + nPC) {
-                ((float4 *)(PC + ((j0 + (f - nPL) * WQ) / WQ) * BLK))[o] = buf[u];
-            } else {
-                ((float4 *)(PW + ((q + (f - nPL - nPC) * WQ) / WQ) * BLK))[o] = buf[u];
-            }
-        }
-    }
+    return (uint32_t)(nPL * WB * WB * 4 + (nPC + nPW) * BLK * 4);
 }
 
 __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restrict__ H, int n1, int ld,
@@ -252,13 +237,22 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
     __shared__ int bad_sh, flag_sh;
     __shared__ float redf[WWARPS];
     __shared__ double xn_sh;
+    // panel blocks received; L_kk received, one mbarrier per Dk buffer
+    __shared__ __align__(8) uint64_t pan_bar, dk_bar[2];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int me = (int)cl.block_rank();
     const int p = me / WQ, q = me % WQ;
     const int NB = (n1 + WB - 1) / WB;
     float *A = sm + OFF_A, *W = sm + OFF_W, *PL = sm + OFF_PL, *PC = sm + OFF_PC, *PW = sm + OFF_PW;
-    float *Dk = sm + OFF_DK, *dinv = sm + OFF_DI;
-    if (tid == 0) bad_sh = 0;
+    float *Dk = sm + OFF_DK, *STG = sm + OFF_STG, *dinv = sm + OFF_DI;
+    const uint32_t pan_b = smem_u32(&pan_bar), dk_b0 = smem_u32(&dk_bar[0]), dk_b1 = smem_u32(&dk_bar[1]);
+    if (tid == 0) {
+        bad_sh = 0;
+        mbar_init(&pan_bar, 1);
+        mbar_init(&dk_bar[0], 1);
+        mbar_init(&dk_bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
 
     // ---- load my blocks of H (FP32, identity beyond n1) and W = I ----
     for (int ib = p; ib < NB; ib += WP)
@@ -274,37 +268,83 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
             }
         }
     __syncthreads();
+    cl.sync();  // every CTA's mbarriers are initialized before anything is sent
+
+    // L_kk (factored by its owner's warp 0) to the CTAs of block row and
+    // block column k, into the Dk buffer of step parity k & 1; lane 0 sends
+    auto send_dk = [&](int kk) {
+        __syncwarp();
+        if (lane == 0) {
+            proxy_fence();
+            const uint32_t src = smem_u32(A + slot_of(kk, kk) * BLK), dst = smem_u32(Dk + (kk & 1) * BLK);
+            const uint32_t bar = (kk & 1) ? dk_b1 : dk_b0;
+            for (int qq = 0; qq < WQ; ++qq) send(dst, src, BLK * 4, bar, (kk % WP) * WQ + qq);
+            for (int pp = 0; pp < WP; ++pp)
+                if (pp != kk % WP) send(dst, src, BLK * 4, bar, pp * WQ + kk % WQ);
+        }
+    };
     if (NB > 0 && owner_of(0, 0) == me && warp == 0) {
         if (!factor_warp(A + slot_of(0, 0) * BLK, lane) && lane == 0) bad_sh = 1;
+        send_dk(0);
     }
 
     // ---- factorization with W = L^-1 alongside ----
+    // Every block a step produces is sent by its owner to the CTAs whose
+    // updates read it; a receiver waits on its mbarrier for the bytes it
+    // expects. The cluster barrier at the top of a step keeps the receive
+    // buffers of step k from being written before every CTA finished step
+    // k - 1 (the L_kk buffers and their mbarriers alternate, since
+    // L_{k+1,k+1} is sent during step k).
+    int dk_n[2] = {0, 0};  // L_kk blocks received per buffer (the mbarrier phases)
     for (int k = 0; k < NB; ++k) {
-        cl.sync();  // diagonal block k is factored
-        const int kp = k % WP, kq = k % WQ, dk_owner = owner_of(k, k);
-        const bool col_k = kq == q, row_k = kp == p;
+        cl.sync();
+        const bool col_k = k % WQ == q, row_k = k % WP == p;
         if (col_k || row_k) {
-            fetch_block(cl, Dk, A + slot_of(k, k) * BLK, dk_owner, tid, WT);
+            const uint32_t bar = (k & 1) ? dk_b1 : dk_b0;
+            if (tid == 0) expect_bytes(bar, BLK * 4);
+            if (!wait_phase(bar, (uint32_t)dk_n[k & 1] & 1u)) bad_sh = 3;
+            ++dk_n[k & 1];
+            const float *D = Dk + (k & 1) * BLK;
+            if (tid < WB) dinv[tid] = __frcp_rn(D[tid * LDB + tid]);
             __syncthreads();
-            if (tid < WB) dinv[tid] = __frcp_rn(Dk[tid * LDB + tid]);
-            __syncthreads();
-            // one warp per task: panel rows below k in column k, then row k of W
+            // one warp per task: panel rows below k in column k, then row k
+            // of W; each block is sent as soon as it is solved
             int task = 0;
             if (col_k)
-                for (int ib = p; ib < NB; ib += WP)
-                    if (ib > k) {
-                        if (task++ % WWARPS == warp) subst_rows(A + slot_of(ib, k) * BLK, Dk, dinv, lane);
+                for (int ib = p; ib < NB; ib += WP) {
+                    if (ib <= k || task++ % WWARPS != warp) continue;
+                    float *blk = A + slot_of(ib, k) * BLK, *st = STG + (ib / WP) * WB * WB;
+                    subst_rows(blk, D, dinv, lane);
+                    __syncwarp();
+#pragma unroll 8
+                    for (int t = 0; t < WB; ++t) st[t * WB + lane] = blk[lane * LDB + t];
+                    __syncwarp();
+                    if (lane == 0) {
+                        proxy_fence();
+                        for (int qq = 0; qq < WQ; ++qq)
+                            send(smem_u32(PL + (ib / WP) * WB * WB), smem_u32(st), WB * WB * 4, pan_b, p * WQ + qq);
+                        for (int pp = 0; pp < WP; ++pp)
+                            send(smem_u32(PC + (ib / WQ) * BLK), smem_u32(blk), BLK * 4, pan_b, pp * WQ + ib % WQ);
                     }
+                }
             if (row_k)
-                for (int jb = q; jb <= k; jb += WQ)
-                    if (task++ % WWARPS == warp) subst_cols(W + slot_of(k, jb) * BLK, Dk, dinv, lane, jb == k);
+                for (int jb = q; jb <= k; jb += WQ) {
+                    if (task++ % WWARPS != warp) continue;
+                    float *blk = W + slot_of(k, jb) * BLK;
+                    subst_cols(blk, D, dinv, lane, jb == k);
+                    __syncwarp();
+                    if (lane == 0) {
+                        proxy_fence();
+                        for (int pp = 0; pp < WP; ++pp)
+                            send(smem_u32(PW + (jb / WQ) * BLK), smem_u32(blk), BLK * 4, pan_b, pp * WQ + q);
+                    }
+                }
         }
-        __syncthreads();
-        cl.sync();  // column k of L and row k of W are final
-        fetch_panels(cl, A, W, PL, PC, PW, k, NB, p, q, tid);
+        if (tid == 0) expect_bytes(pan_b, panel_bytes(k, NB, p, q));
+        if (!wait_phase(pan_b, (uint32_t)k & 1u)) bad_sh = 3;
         __syncthreads();
         // the next diagonal block first, by warp 0, which then factors it
-        // while the other warps apply the remaining updates
+        // and sends it while the other warps apply the remaining updates
         const bool own_next = k + 1 < NB && owner_of(k + 1, k + 1) == me;
         int task = 0;
         for (int ib = p; ib < NB; ib += WP) {
@@ -321,7 +361,9 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
         if (own_next && warp == 0) {
             __syncwarp();
             if (!factor_warp(A + slot_of(k + 1, k + 1) * BLK, lane) && lane == 0) bad_sh = 1;
+            send_dk(k + 1);
         }
+        proxy_fence();  // this CTA's reads of the receive buffers precede the next step's sends into them
         __syncthreads();
     }
     cl.sync();  // nobody reads the A slots remotely any more
