@@ -45,6 +45,13 @@ void irwls_debug_tc_wait(long long limit, int stall);
  * (binary and 8-bit data; the products are then exact), else 3 (hi + mid +
  * lo of the FP32 value). */
 int irwls_last_tc_pieces(void);
+/* Kernel row sums of precision-form full IRWLS done in the exact-integer
+ * mode since the last reset: on data whose values are integers after the
+ * operand scale (8-bit values / 255, binary) with squared row norms below
+ * 2^24 in those units, the exact rows' updates, the working-set updates and
+ * G13 take their dot products exactly from the tensor cores (bf16 integer
+ * products, FP32 sums below 2^24) and the exp and sums in FP64. */
+long long irwls_tc_exact_calls(int reset);
 /* Working-set solves of precision-form full IRWLS since the last reset:
  * those done by the FP32-factor + FP64-refinement cluster solve, and those
  * whose order fitted it but which went to the FP64 factorization (an FP32

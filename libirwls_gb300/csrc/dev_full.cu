@@ -700,6 +700,9 @@ extern "C" int irwls_sub_init(irwls_sub_ws *ws, const irwls_dev_set *X, double C
 // issued here at the start of the next iteration, when n1/n3 are known.
 extern "C" int irwls_sub_g13(irwls_sub_ws *ws, const irwls_dev_set *X, int n1, int n3) {
     if (n3 <= 0 || n1 <= 0) return 0;
+    const int ex = irwls_tc_exact_rowsum(ws->tcs, X, ws->gl1, n1, ws->gl3, n3, nullptr, n3, ws->rhs, X->y, X->y, +1,
+                                         nullptr, nullptr, ws->G13);
+    if (ex != 1) return ex;
     return irwls_dev_kernel_rowsum(X, ws->gl1, n1, X, ws->gl3, n3, ws->rhs, X->y, X->y, 0, +1, nullptr, nullptr,
                                    ws->G13);
 }
@@ -729,8 +732,13 @@ extern "C" int irwls_sub_iterate(irwls_sub_ws *ws, const irwls_dev_set *X, doubl
     sub_update_kernel<<<1, CT, 0, irwls_stream()>>>(*ws, C, n1, n3);
     IRWLS_LAUNCH_CHECK("sub_update");
     // e_i -= k(i, j) (bnew_j - beta_j) over changed j, then the bias change
-    if (irwls_dev_kernel_rowsum_n(X, ws->map, ws->w, X, ws->lst, ws->cnt, ws->dlt, nullptr, nullptr, -1, ws->e,
-                                  ws->scal, ws->e))
+    // (exact tensor-core dot products in the precision form where the data
+    // allow them: at most w changed entries)
+    const int ex = irwls_tc_exact_rowsum(ws->tcs, X, ws->map, ws->w, ws->lst, 0, ws->cnt, ws->w, ws->dlt, nullptr,
+                                         nullptr, -1, ws->e, ws->scal, ws->e);
+    if (ex < 0) return -2;
+    if (ex == 1 && irwls_dev_kernel_rowsum_n(X, ws->map, ws->w, X, ws->lst, ws->cnt, ws->dlt, nullptr, nullptr, -1,
+                                             ws->e, ws->scal, ws->e))
         return -2;
     sub_groups_kernel<<<1, CT, 0, irwls_stream()>>>(*ws, C);
     IRWLS_LAUNCH_CHECK("sub_groups");

@@ -27,6 +27,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "blocked_bf16.cuh"
 #include "dev_common.cuh"
@@ -1485,6 +1486,14 @@ struct TcSet {
     int rows, kbn, wmax, rbf, pieces;
     float ng, dscale;
     double kbound;
+    // exact-integer mode (irwls_tc_exact_rowsum): whether it applies, the
+    // operand scale, and its grow-only buffers (gathered rows, partial sums)
+    int exact;
+    double scale;
+    __nv_bfloat16 *Ag;
+    long long ag_cap;
+    double *part;
+    long long part_cap;
 };
 
 // max over rows of q (one CTA): |x_i . x_j| <= max q bounds linear kernel values.
@@ -1564,6 +1573,7 @@ TcSet *rs_set_make(const irwls_dev_set *X, int rows, int wmax, int kbn, int P, d
     t->rbf = X->mode != IRWLS_K_LINEAR;
     t->ng = (float)X->neg_gamma;
     t->pieces = P;
+    t->scale = scale;
     t->dscale = (float)(1.0 / (scale * scale));
     int rc = irwls_dev_malloc((void **)&t->bad, 4 * sizeof(int));
     t->nbuf = t->bad + 2;
@@ -1604,6 +1614,52 @@ TcSet *rs_set_make(const irwls_dev_set *X, int rows, int wmax, int kbn, int P, d
 }
 }  // namespace
 
+namespace {
+// bad[0] |= some stored value times `scale` is not an integer.
+__global__ void rs_int_check_kernel(const double *__restrict__ v, long long n, double scale, int *bad) {
+    int b = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double x = v[t] * scale;
+        if (x != rint(x)) b = 1;
+    }
+    b = __any_sync(0xffffffffu, b);
+    if ((threadIdx.x & 31) == 0 && b) atomicOr(bad, 1);
+}
+
+// Whether the exact-integer mode applies to a one-piece set (sets t->exact):
+// every stored value times the scale an integer (true by construction for
+// scale 255: the value is RN(k / 255) and the split rounds it to k), the
+// kernel RBF in norm form or linear, and max_i ||scale x_i||^2 < 2^24, so that
+// every partial sum of a dot product of two rows is an integer below 2^24.
+int rs_exact_check(const irwls_dev_set *X, TcSet *t) {
+    t->exact = 0;
+    if (t->pieces != 1 || X->mode == IRWLS_K_RAW_RBF) return 0;
+    int nnz = 0, bad = 0;
+    int rc = irwls_dev_d2h(&nnz, X->rp + t->rows, sizeof(int));
+    rc |= irwls_dev_sync();
+    if (rc) return rc;
+    if (t->scale == 1.0 && nnz > 0) {
+        rc |= irwls_dev_memset(t->bad, 0, sizeof(int));
+        const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+        const int blocks = (int)std::max<long long>(1, std::min<long long>((nnz + 255LL) / 256, 8LL * sms));
+        rs_int_check_kernel<<<blocks, 256, 0, irwls_stream()>>>(X->cv, nnz, 1.0, t->bad);
+        irwls_count_launch(1);
+        rc |= irwls_dev_d2h(&bad, t->bad, sizeof(int));
+        rc |= irwls_dev_sync();
+        if (rc) return rc;
+    }
+    max_q_kernel<<<1, 1024, 0, irwls_stream()>>>(t->q, t->rows, t->qb);
+    irwls_count_launch(1);
+    float mq = 0.f;
+    rc |= irwls_dev_d2h(&mq, t->qb, sizeof(float));
+    rc |= irwls_dev_sync();
+    if (rc) return rc;
+    const double bound = 1.001 * (double)mq * t->scale * t->scale;
+    t->exact = !bad && bound < 16777216.0;
+    return 0;
+}
+}  // namespace
+
 // Blocked copy of rows 0..rows-1 of a device set for the precision form, in
 // the operand form its values allow, with room for `wmax` gathered rows.
 extern "C" void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax) {
@@ -1616,7 +1672,12 @@ extern "C" void *irwls_tc_set_create(const irwls_dev_set *X, int rows, int wmax)
     double scale;
     rs_form(bad, 1, &P, &scale);
     g_rs_last_pieces = P;
-    return rs_set_make(X, rows, wmax, ceil_div(X->width, RS_BK), P, scale);
+    TcSet *t = rs_set_make(X, rows, wmax, ceil_div(X->width, RS_BK), P, scale);
+    if (t && rows > 0 && rs_exact_check(X, t)) {
+        irwls_tc_set_free(t);
+        return nullptr;
+    }
+    return t;
 }
 
 extern "C" double irwls_tc_set_kbound(void *h) { return ((TcSet *)h)->kbound; }
@@ -1630,6 +1691,8 @@ extern "C" void irwls_tc_set_free(void *h) {
     irwls_dev_free(t->qb);
     irwls_dev_free(t->cbf);
     irwls_dev_free(t->bad);
+    irwls_dev_free(t->Ag);
+    irwls_dev_free(t->part);
     free(t);
 }
 
@@ -1721,4 +1784,280 @@ extern "C" int irwls_tc_predict(const irwls_dev_set *T, int n, const irwls_dev_s
     irwls_dev_free(d_bad);
     irwls_dev_free(d_idx);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Exact-integer mode of the engine: FP64 kernel row sums over a row subset,
+// with the dot products on the tensor cores.
+//
+// When every stored value times the set's scale s (1 or 255) is an integer
+// and max_i ||s x_i||^2 < 2^24 (rs_exact_check), each one-piece bf16 product
+// (s x_ik)(s x_jk) is an integer and every partial sum of a dot product is an
+// integer of magnitude at most ||s x_i|| ||s x_j|| < 2^24: the FP32
+// accumulation is exact in any order. The kernel value then follows in FP64,
+// k_ij = exp(-gamma ((q_i + q_j) - 2 dot / s^2)) (RBF) or dot / s^2 (linear),
+// within a few ulps of the reference's value, at about 25 FP64 operations
+// per value instead of two per stored feature; so do the weighted sums
+// (in a different order than the reference's left-to-right one).
+//
+// One CTA per item (a 128-row tile of the gathered rows x CW columns of the
+// gathered list): warp 0 streams the operands through a 4-stage bulk-copy
+// ring, warp 1 issues the MMAs into a 128 x CW FP32 accumulator in tensor
+// memory, then all 8 warps form the item's partial row sums in FP64
+// (rows by lane, columns split between two warp groups), written to
+// part[h][row]; ex_combine_kernel adds the partials of each row in item
+// order. Every wait is bounded; a wait that runs out sets device flag 1.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int EX_THREADS = 256;
+constexpr int EX_NS = 4;
+std::atomic<long long> g_ex_calls{0};
+
+// Rows ia[i < nA] of the full blocked copy A into the tile layout of the row
+// subset Ag (16-byte groups of one core-matrix row at a time).
+__global__ void rs_gather_rows_kernel(const __nv_bfloat16 *__restrict__ A, int kbn, const int *__restrict__ ia,
+                                      int nA, __nv_bfloat16 *__restrict__ Ag) {
+    const long long total = (long long)nA * kbn * 4;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(t & 3);
+        const long long rest = t >> 2;
+        const int k = (int)(rest % kbn), i = (int)(rest / kbn), s = ia[i];
+        const size_t src = ((size_t)(s >> 7) * kbn + k) * RS_APIECE + rs_core(s & 127, 8 * g);
+        const size_t dst = ((size_t)(i >> 7) * kbn + k) * RS_APIECE + rs_core(i & 127, 8 * g);
+        *(uint4 *)(Ag + dst) = *(const uint4 *)(A + src);
+    }
+}
+
+template <int CW>
+__global__ void __launch_bounds__(EX_THREADS, 1) tc_exact_rowsum_kernel(
+    const __nv_bfloat16 *__restrict__ A, int M, int kbn, const __nv_bfloat16 *__restrict__ B,
+    const int *__restrict__ d_n, int nmax, int nchx, const double *__restrict__ q, const int *__restrict__ ia,
+    const int *__restrict__ ib, int rbf, double ng, double dscale, const double *__restrict__ cb,
+    const double *__restrict__ sa, const double *__restrict__ sb, double *__restrict__ part, int ldp, int *flags,
+    long long wait_limit) {
+    static_assert(CW == 64 || CW == 128 || CW == 256, "column width");
+    constexpr uint32_t A_BYTES = RS_APIECE * 2, B_MAX = CW * RS_BK * 2;
+    extern __shared__ __align__(1024) unsigned char ex_smem[];
+    __shared__ __align__(8) uint64_t full[EX_NS], empty[EX_NS], accf;
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int abort_flag;
+    __shared__ double half_sum[RS_BM];
+    const int N = max(0, min(*d_n, nmax));
+    const int tile = (int)blockIdx.x / nchx, h = (int)blockIdx.x % nchx, c0 = h * CW;
+    if (c0 >= N) return;  // the list is shorter than this item's columns
+    unsigned char *smem = ex_smem + ((1024 - (smem_u32(ex_smem) & 1023)) & 1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ncols = min(CW, N - c0), nr16 = (ncols + 15) / 16 * 16;
+    const uint32_t bbytes = (uint32_t)nr16 * RS_BK * 2;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < EX_NS; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], 1);
+        }
+        mbar_init(&accf, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+        abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(CW));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const uint32_t tmem = tmem_slot;
+    const uint32_t stage_bytes = A_BYTES + B_MAX;
+    if (warp == 0 && lane == 0) {
+        // producer: the A tile and this item's B rows of each 32-wide K block
+        const uint32_t base = smem_u32(smem);
+        const __nv_bfloat16 *Bc = B + (size_t)(c0 >> 8) * kbn * RS_BPIECE + (size_t)((c0 & 255) >> 3) * 256;
+        int issued = 0;
+        for (int k = 0; k < kbn; ++k) {
+            const int slot = k % EX_NS;
+            if (k >= EX_NS && !mbar_wait_lim(smem_u32(&empty[slot]), (uint32_t)(k / EX_NS - 1) & 1u, wait_limit))
+                abort_flag = 1;
+            if (abort_flag) break;
+            const uint32_t sb = base + slot * stage_bytes, fb = smem_u32(&full[slot]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(A_BYTES + bbytes));
+            bulk_g2s(sb, A + ((size_t)tile * kbn + k) * RS_APIECE, A_BYTES, fb);
+            bulk_g2s(sb + A_BYTES, Bc + (size_t)k * RS_BPIECE, bbytes, fb);
+            issued = k + 1;
+        }
+        // no copy is left in flight
+        for (int k = issued > EX_NS ? issued - EX_NS : 0; k < issued; ++k)
+            if (!mbar_wait_lim(smem_u32(&full[k % EX_NS]), (uint32_t)(k / EX_NS) & 1u, wait_limit)) abort_flag = 1;
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = tc_idesc(RS_BM, nr16);
+        bool any = false;
+        for (int k = 0; k < kbn && !abort_flag; ++k) {
+            const int slot = k % EX_NS;
+            if (!mbar_wait_lim(smem_u32(&full[slot]), (uint32_t)(k / EX_NS) & 1u, wait_limit)) {
+                abort_flag = 1;
+                break;
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::);
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            const uint32_t sa_ = smem_u32(smem + slot * stage_bytes), sbb = sa_ + A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < RS_BK / 16; ++kk)
+                mma_bf16(tmem, tc_desc_sbo(sa_ + kk * 256, 512), tc_desc_sbo(sbb + kk * 256, 512), idesc,
+                         (k > 0 || kk > 0) ? 1u : 0u);
+            tc_commit(&empty[slot]);
+            any = true;
+        }
+        // completes once every MMA issued has (or at once if none was)
+        if (any) tc_commit(&accf);
+        else mbar_arrive(&accf);
+    }
+    __syncwarp();
+    const bool got = mbar_wait_lim(smem_u32(&accf), 0u, wait_limit);
+    // one decision for the whole CTA (the epilogue has a named barrier)
+    const bool ok = __syncthreads_and(got ? 1 : 0) && !abort_flag;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (ok) {
+        const int ew = warp & 3, gh = warp >> 2, r = 32 * ew + lane, row = tile * RS_BM + r;
+        const bool valid = row < M;
+        const int gi = valid ? ia[row] : 0;
+        const double qi = valid ? q[gi] : 0.0, sai = (valid && sa) ? sa[gi] : 1.0;
+        double acc = 0.0;
+        for (int cc = 0; cc < CW / 2; cc += 32) {
+            const int cbase = gh * (CW / 2) + cc;
+            if (cbase >= ncols) break;
+            float v[32];
+            tc_ld32_lanes(tmem, 32 * ew, cbase, v);
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) {
+                const int c = cbase + jj;
+                if (c < ncols) {
+                    const int j = c0 + c, gj = ib[j];
+                    const double dot = (double)v[jj] * dscale;
+                    const double kv = rbf ? exp(ng * fma(-2.0, dot, qi + q[gj])) : dot;
+                    double t = cb ? cb[j] * kv : kv;
+                    if (sa) t *= sai;
+                    if (sb) t *= sb[gj];
+                    acc += t;
+                }
+            }
+        }
+        if (gh == 1) half_sum[r] = acc;
+        asm volatile("bar.sync 1, %0;\n" ::"r"(EX_THREADS));
+        if (gh == 0 && valid) part[(size_t)h * ldp + row] = acc + half_sum[r];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    if (threadIdx.x == 0 && !ok) atomicExch(flags + 1, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(CW));
+}
+
+// out_i = (init_i OP sum_h part[h][i]) - tail[0] over the items of the list
+// that *d_n leaves, in item order (init may alias out; init, tail optional).
+__global__ void ex_combine_kernel(const double *__restrict__ part, int ldp, int M, const int *__restrict__ d_n,
+                                  int nmax, int cw, int op, const double *init, const double *__restrict__ tail,
+                                  double *out) {
+    const int N = max(0, min(*d_n, nmax)), nch = (N + cw - 1) / cw;
+    const double tl = tail ? tail[0] : 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int h = 0; h < nch; ++h) s += part[(size_t)h * ldp + i];
+        double acc = init ? init[i] : 0.0;
+        acc = op > 0 ? acc + s : acc - s;
+        out[i] = tail ? acc - tl : acc;
+    }
+}
+
+__global__ void set_int_kernel(int *p, int v) { *p = v; }
+
+template <int CW>
+int ex_launch(TcSet *t, const irwls_dev_set *X, int nA, const int *d_ia, const int *d_ib, const int *d_n, int nmax,
+              const double *d_cb, const double *d_sa, const double *d_sb) {
+    const int ntiles = ceil_div(nA, RS_BM), nchx = ceil_div(nmax, CW);
+    const size_t smem = (size_t)EX_NS * (RS_APIECE * 2 + CW * RS_BK * 2) + 1024;
+    cudaFuncSetAttribute(tc_exact_rowsum_kernel<CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    tc_exact_rowsum_kernel<CW><<<ntiles * nchx, EX_THREADS, smem, irwls_stream()>>>(
+        t->Ag, nA, t->kbn, t->B, d_n, nmax, nchx, X->q, d_ia, d_ib, t->rbf, X->neg_gamma, 1.0 / (t->scale * t->scale),
+        d_cb, d_sa, d_sb, t->part, nA, irwls_dev_flags(), g_rs_wait_limit);
+    IRWLS_LAUNCH_CHECK("tc_exact_rowsum");
+    return 0;
+}
+
+}  // namespace
+
+// FP64 kernel row sums with exact tensor-core dot products (the precision
+// form's exact rows): for i < nA,
+//   out_i = (init_i OP sum_{j < n} t_ij) - tail[0],
+//   t_ij = ((cb_j k(x_ia[i], x_ib[j])) sa_ia[i]) sb_ib[j]   (cb, sa, sb optional),
+// n = nB, or *d_nB when d_nB is given (then at most nbmax). The same values as
+// irwls_dev_kernel_rowsum(_n) to within a few ulps of each kernel value and a
+// different summation order. Returns 1 without doing anything when the set
+// does not allow the exact mode or the list may exceed the set's gather room
+// (the caller then uses the FP64 kernels), else 0 or an error.
+extern "C" int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int *d_ia, int nA, const int *d_ib,
+                                     int nB, const int *d_nB, int nbmax, const double *d_cb, const double *d_sa,
+                                     const double *d_sb, int op, const double *d_init, const double *d_tail,
+                                     double *d_out) {
+    TcSet *t = (TcSet *)h;
+    if (!t || !t->exact) return 1;
+    if (!d_nB) nbmax = nB;
+    if (nbmax > t->wmax || nbmax < 0) return 1;
+    if (nA <= 0) return 0;
+    const int *d_n = d_nB;
+    if (!d_nB) {
+        set_int_kernel<<<1, 1, 0, irwls_stream()>>>(t->nbuf, nB);
+        IRWLS_LAUNCH_CHECK("tc_exact_count");
+        d_n = t->nbuf;
+    }
+    // grow-only buffers: the gathered rows and the partial sums
+    const long long rows_pad = (long long)ceil_div(nA, RS_BM) * RS_BM;
+    if (rows_pad > t->ag_cap) {
+        irwls_dev_free(t->Ag);
+        t->Ag = nullptr;
+        t->ag_cap = 0;
+        if (irwls_dev_malloc((void **)&t->Ag, (size_t)rows_pad * t->kbn * RS_BK * sizeof(__nv_bfloat16))) return -3;
+        t->ag_cap = rows_pad;
+    }
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    const int ntiles = ceil_div(nA, RS_BM);
+    // column width: enough items for every SM when the tiles are few
+    const int cw = (long long)ntiles * ceil_div(std::max(nbmax, 1), 128) >= 2LL * sms ? 128 : 64;
+    const long long need = (long long)ceil_div(std::max(nbmax, 1), cw) * nA;
+    if (need > t->part_cap) {
+        irwls_dev_free(t->part);
+        t->part = nullptr;
+        t->part_cap = 0;
+        if (irwls_dev_malloc((void **)&t->part, (size_t)need * sizeof(double))) return -3;
+        t->part_cap = need;
+    }
+    if (nbmax > 0) {
+        const int gr = std::max(1, std::min(ceil_div((long long)nA * t->kbn * 4, 256), 8 * sms));
+        rs_gather_rows_kernel<<<gr, 256, 0, irwls_stream()>>>(t->A, t->kbn, d_ia, nA, t->Ag);
+        IRWLS_LAUNCH_CHECK("tc_exact_gather_rows");
+        const int gb = std::max(1, std::min(ceil_div((long long)nbmax * t->kbn * 4, 256), 4096));
+        rs_gather_kernel<1><<<gb, 256, 0, irwls_stream()>>>(t->A, t->kbn, t->q, d_ib, d_n, t->wmax, t->B, t->qb,
+                                                            d_cb ? d_cb : X->q, t->cbf);
+        IRWLS_LAUNCH_CHECK("tc_exact_gather_cols");
+        if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
+        const int rc = cw == 128 ? ex_launch<128>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb)
+                                 : ex_launch<64>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb);
+        if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
+        if (rc) return rc;
+    }
+    ex_combine_kernel<<<std::max(1, std::min(ceil_div(nA, 256), 4 * sms)), 256, 0, irwls_stream()>>>(
+        t->part, nA, nA, d_n, nbmax, cw, op, d_init, d_tail, d_out);
+    IRWLS_LAUNCH_CHECK("tc_exact_combine");
+    ++g_ex_calls;
+    return 0;
+}
+
+// Whether a set made by irwls_tc_set_create allows the exact-integer mode.
+extern "C" int irwls_tc_set_exact(void *h) { return h && ((TcSet *)h)->exact; }
+
+// Row sums done in the exact-integer mode since the last reset.
+extern "C" long long irwls_tc_exact_calls(int reset) {
+    const long long n = g_ex_calls.load();
+    if (reset) g_ex_calls = 0;
+    return n;
 }

@@ -199,6 +199,7 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
         if (nSIN > 0 && irwls_full_gin(X, SW, nSW, SIN, nSIN, bnew, lst, cb, cnt, ws.GIN)) goto fail;
         ws.w = nSW;
         ws.map = SW;
+        ws.tcs = tcs;
         if (irwls_full_gather_ws(SW, nSW, e, beta, l, ws.e, ws.beta)) goto fail;
         if (irwls_dev_memset(ws.bbest, 0, (size_t)(nSW + 1) * sizeof(double))) goto fail;
         if (run_sub(&ws, X, &props)) goto fail;
@@ -207,9 +208,15 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
         if (tcs) {
             /* FP64 increments of the exact rows, tensor-core update of all
                rows, then the exact values written back */
-            if (nS > 0 && (irwls_dev_gather(e, xS, nS, eS) ||
-                           irwls_dev_kernel_rowsum_n(X, xS, nS, X, lst, cnt, cb, NULL, NULL, -1, eS, dbias, eS)))
-                goto fail;
+            if (nS > 0) {
+                /* at most nSW changed weights: exact tensor-core dot products
+                   where the data allow them, else the FP64 kernels */
+                if (irwls_dev_gather(e, xS, nS, eS)) goto fail;
+                const int ex = irwls_tc_exact_rowsum(tcs, X, xS, nS, lst, 0, cnt, nSW, cb, NULL, NULL, -1, eS, dbias, eS);
+                if (ex < 0 ||
+                    (ex == 1 && irwls_dev_kernel_rowsum_n(X, xS, nS, X, lst, cnt, cb, NULL, NULL, -1, eS, dbias, eS)))
+                    goto fail;
+            }
             if (irwls_tc_kernel_rowsum(tcs, lst, cnt, cb, e, dbias, e)) goto fail;
             if (irwls_dev_scatter(eS, xS, nS, e) || irwls_dev_d2h(h_l1, dbias + 1, sizeof(double))) goto fail;
         } else if (irwls_dev_kernel_rowsum_n(X, NULL, l, X, lst, cnt, cb, NULL, NULL, -1, e, dbias, e)) {
@@ -273,12 +280,19 @@ int irwls_full_train_dev(const irwls_dev_set *X, int l, properties props, double
                 goto fail;
             nS = h_xcnt[0];
             const int nnew = h_xcnt[1];
-            if (nnew > 0 && (irwls_full_sv_list(bnew, l, svlst, svcb, svcnt) ||
-                             irwls_dev_gather(X->y, xSnew, nnew, eS) ||
-                             irwls_dev_kernel_rowsum_n(X, xSnew, nnew, X, svlst, svcnt, svcb, NULL, NULL, -1, eS,
-                                                       bnew + l, eS) ||
-                             irwls_dev_scatter(eS, xSnew, nnew, e)))
-                goto fail;
+            if (nnew > 0) {
+                /* rows entering S: e = y - sum over the support vectors - b */
+                if (irwls_full_sv_list(bnew, l, svlst, svcb, svcnt) || irwls_dev_gather(X->y, xSnew, nnew, eS) ||
+                    irwls_dev_d2h(h_xcnt, svcnt, sizeof(int)) || irwls_dev_sync())
+                    goto fail;
+                const int nsv = h_xcnt[0];
+                const int ex = irwls_tc_exact_rowsum(tcs, X, xSnew, nnew, svlst, nsv, NULL, nsv, svcb, NULL, NULL, -1,
+                                                     eS, bnew + l, eS);
+                if (ex < 0 || (ex == 1 && irwls_dev_kernel_rowsum_n(X, xSnew, nnew, X, svlst, svcnt, svcb, NULL, NULL,
+                                                                    -1, eS, bnew + l, eS)))
+                    goto fail;
+                if (irwls_dev_scatter(eS, xSnew, nnew, e)) goto fail;
+            }
         }
     }
     if (irwls_dev_d2h(beta_out, bnew, L1 * sizeof(double)) || irwls_dev_sync()) goto fail;

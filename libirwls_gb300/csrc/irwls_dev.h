@@ -148,6 +148,7 @@ typedef struct irwls_sub_ws {
     irwls_sub_stats *stats;   /* device */
     irwls_sub_stats *h_stats; /* pinned host mirror */
     int ldH;
+    void *tcs;                /* precision form: the training's tensor-core set (NULL: FP64 throughout) */
 } irwls_sub_ws;
 
 int irwls_sub_alloc(irwls_sub_ws *ws, int cap);
@@ -232,6 +233,19 @@ int irwls_dev_scatter(const double *d_src, const int *d_idx, int n, double *d_ds
 /* Bound on |k(x_i, x_j)| over the set (1 for RBF, max q for linear). */
 double irwls_tc_set_kbound(void *h);
 void irwls_tc_set_free(void *h);
+/* Exact-integer mode (dev_tc.cu): FP64 kernel row sums over the rows d_ia
+ * (nA) against the list d_ib (nB entries, or *d_nB <= nbmax when d_nB is
+ * given) with the dot products exact on the tensor cores:
+ *   out_i = (init_i OP sum_j ((cb_j k(ia_i, ib_j)) sa_{ia_i}) sb_{ib_j}) - tail[0]
+ * (the irwls_dev_kernel_rowsum arguments; cb, sa, sb, init, tail optional).
+ * Returns 1 when the set does not allow it (values not integers after the
+ * set's scale, norms too large for exact FP32 sums, raw RBF mode) or the
+ * list may be longer than the set's gather room; the caller then uses the
+ * FP64 kernels. */
+int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int *d_ia, int nA, const int *d_ib, int nB,
+                          const int *d_nB, int nbmax, const double *d_cb, const double *d_sa, const double *d_sb,
+                          int op, const double *d_init, const double *d_tail, double *d_out);
+int irwls_tc_set_exact(void *h);
 int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n, const double *d_cb, const double *d_init,
                            const double *d_tail, double *d_out);
 /* Precision-form prediction: d_out = b + sum_j w_j k(t_i, s_j) (or its sign)

@@ -6,6 +6,10 @@ against the CPU oracle (the restatement of the reference, FP64):
   (the products are exact; only the FP32 accumulation rounds);
 - three pieces (hi + mid + lo of the FP32 value) otherwise.
 
+On the integer-valued sets the rows that decide the support vectors (the
+exact set, the working set, G13) take the exact-integer mode: dot products
+exact on the tensor cores, exp and sums in FP64.
+
 Bars (the precision form's contract): the support-vector set of the oracle,
 the dual objective within 1e-5 relative, >= 99.9 % of the held-out labels.
 Prediction in the precision form (the same engine, f = b + sum w k) is
@@ -59,11 +63,18 @@ def _mixed_full(lib, hd, p):
 @pytest.mark.parametrize("kind,pieces,gamma", [("digits", 1, 0.05), ("binary", 1, 0.1), ("gauss", 3, 0.1)])
 def test_precision_full_operand_forms_match_oracle(kind, pieces, gamma):
     lib = load()
+    lib.irwls_tc_exact_calls.argtypes = [C.c_int]
+    lib.irwls_tc_exact_calls.restype = C.c_longlong
     hd, ht = _sets(kind, 3000, 600, 91)
     p = {"gamma": gamma, "C": 10.0, "w": 300, "kernel": 1}
+    lib.irwls_tc_exact_calls(1)
     beta, ptr, prop = _mixed_full(lib, hd, p)
+    exact_calls = lib.irwls_tc_exact_calls(1)
     assert lib.irwls_tc_status() == 0
     assert lib.irwls_last_tc_pieces() == pieces
+    # integer-valued data (8-bit / 255, binary) take the exact-integer mode for
+    # the exact rows, the working-set updates and G13; FP32-split data do not
+    assert (exact_calls > 0) == (pieces == 1), exact_calls
     ref, rptr, _ = H.run_full(H.port(), hd, p)
     same_sv = np.array_equal(np.nonzero(beta[:-1])[0], np.nonzero(ref[:-1])[0])
     d_ref = H.dual_objective(hd, ref, p["gamma"], 1)
