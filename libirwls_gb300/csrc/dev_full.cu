@@ -162,6 +162,16 @@ __global__ void __launch_bounds__(64) build_H_kernel(irwls_sub_ws ws, KView X, i
     ws.H[(size_t)j * ws.ldH + i] = h;
 }
 
+// The diagonal's 1 / a_i after an exact-mode kernel block (the same
+// operations as build_H_kernel's diagonal).
+__global__ void build_H_diag_kernel(irwls_sub_ws ws, int n1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n1) {
+        double *h = ws.H + (size_t)i * ws.ldH + i;
+        *h = __dadd_rn(*h, __ddiv_rn(1.0, ws.a[ws.S1[i]]));
+    }
+}
+
 __global__ void build_border_kernel(irwls_sub_ws ws, int n1) {
     const int w = ws.w;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= n1; i += gridDim.x * blockDim.x) {
@@ -264,24 +274,6 @@ __global__ void __launch_bounds__(CT) sub_groups_kernel(irwls_sub_ws ws, double 
 
 // Inactive samples with a non-zero weight, their weights, and GIN[nSW] =
 // sum of the weights of every inactive sample (src/full-train.c:436-456).
-__global__ void __launch_bounds__(CT) gin_prepare_kernel(const int *__restrict__ SIN, int nSIN,
-                                                         const double *__restrict__ bnew, int *lst, double *cb,
-                                                         int *cnt, double *GIN, int nSW) {
-    __shared__ int s_scan[CT];
-    const int n = block_compact(nSIN, [&](int o) { return bnew[SIN[o]] != 0.0; },
-                                [&](int p, int o) {
-                                    lst[p] = SIN[o];
-                                    cb[p] = bnew[SIN[o]];
-                                },
-                                s_scan);
-    __shared__ double red[33];
-    const double g = block_sum_ordered(nSIN, [&](int o) { return bnew[SIN[o]]; }, red);
-    if (threadIdx.x == 0) {
-        cnt[0] = n;
-        GIN[nSW] = g;
-    }
-}
-
 __global__ void gather_ws_kernel(const int *__restrict__ SW, int nSW, const double *__restrict__ e,
                                  const double *__restrict__ beta, int l, double *esub, double *bsub) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nSW; i += gridDim.x * blockDim.x) {
@@ -320,17 +312,99 @@ __global__ void __launch_bounds__(CT) apply_ws_kernel(const int *__restrict__ SW
     if (threadIdx.x == 0) dbias[1] = l1;
 }
 
-__global__ void __launch_bounds__(CT) norms_kernel(const double *__restrict__ beta, const double *__restrict__ bnew,
-                                                   int n, double *out2) {
-    __shared__ double red[33];
-    const double dW = block_sum_ordered(n, [&](int i) {
+// ---- ordered reductions of the outer loop over many CTAs --------------------
+// block_sum_ordered splits [0, n) into CT chunks of ch = ceil(n / CT) (thread
+// t: [t ch, min(n, (t + 1) ch))), sums each left to right, then combines the
+// chunk sums by fixed shuffle trees. The chunk passes below compute the same
+// chunk sums on CT threads spread over CT / PC CTAs (on one SM the FP64 pipe
+// made these sums take 150 us); the final pass runs the same trees on one CTA
+// of CT threads. The results are the single-CTA kernels' bits.
+constexpr int PC = 128;  // threads per CTA of the chunk passes
+
+__device__ double chunk_tree_sum(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = red[lane];
+        for (int o = 16; o > 0; o >>= 1) t = __dadd_rn(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    const double r = red[32];
+    __syncthreads();
+    return r;
+}
+
+// dW = sum (beta - bnew)^2 and nW = sum beta^2 (src/full-train.c:512-520).
+__global__ void __launch_bounds__(PC) norms_chunk_kernel(const double *__restrict__ beta,
+                                                         const double *__restrict__ bnew, int n, double *part) {
+    const int t = blockIdx.x * PC + threadIdx.x, ch = (n + CT - 1) / CT, b = t * ch, e = min(n, b + ch);
+    double v1 = 0.0, v2 = 0.0;
+    for (int i = b; i < e; ++i) {
         const double d = __dsub_rn(beta[i], bnew[i]);
-        return __dmul_rn(d, d);
-    }, red);
-    const double nW = block_sum_ordered(n, [&](int i) { return __dmul_rn(beta[i], beta[i]); }, red);
+        v1 = __dadd_rn(v1, __dmul_rn(d, d));
+        v2 = __dadd_rn(v2, __dmul_rn(beta[i], beta[i]));
+    }
+    part[t] = v1;
+    part[CT + t] = v2;
+}
+
+__global__ void __launch_bounds__(CT) norms_final_kernel(const double *__restrict__ part, double *out2) {
+    __shared__ double red[33];
+    const double dW = chunk_tree_sum(part[threadIdx.x], red);
+    const double nW = chunk_tree_sum(part[CT + threadIdx.x], red);
     if (threadIdx.x == 0) {
         out2[0] = dW;
         out2[1] = nW;
+    }
+}
+
+// GIN's list (src/full-train.c:436-456): the entries of SIN with bnew != 0
+// in ascending order with their weights, and GIN[nSW] = sum over SIN of bnew.
+// Pass 1 counts and sums each chunk, pass 2 scans the counts and combines
+// the sums, pass 3 writes each chunk's entries at its offset.
+__global__ void __launch_bounds__(PC) gin_chunk_kernel(const int *__restrict__ SIN, int nSIN,
+                                                       const double *__restrict__ bnew, int *ccount, double *csum) {
+    const int t = blockIdx.x * PC + threadIdx.x, ch = (nSIN + CT - 1) / CT, b = t * ch, e = min(nSIN, b + ch);
+    int c = 0;
+    double v = 0.0;
+    for (int o = b; o < e; ++o) {
+        const double w = bnew[SIN[o]];
+        c += w != 0.0 ? 1 : 0;
+        v = __dadd_rn(v, w);
+    }
+    ccount[t] = c;
+    csum[t] = v;
+}
+
+__global__ void __launch_bounds__(CT) gin_scan_kernel(int *ccount, const double *__restrict__ csum, int *cnt,
+                                                      double *GIN, int nSW) {
+    __shared__ int s_scan[CT];
+    __shared__ double red[33];
+    const int total = block_exclusive_scan(s_scan, ccount[threadIdx.x]);
+    ccount[threadIdx.x] = s_scan[threadIdx.x];  // now the chunk's offset
+    const double g = chunk_tree_sum(csum[threadIdx.x], red);
+    if (threadIdx.x == 0) {
+        cnt[0] = total;
+        GIN[nSW] = g;
+    }
+}
+
+__global__ void __launch_bounds__(PC) gin_write_kernel(const int *__restrict__ SIN, int nSIN,
+                                                       const double *__restrict__ bnew,
+                                                       const int *__restrict__ coffset, int *lst, double *cb) {
+    const int t = blockIdx.x * PC + threadIdx.x, ch = (nSIN + CT - 1) / CT, b = t * ch, e = min(nSIN, b + ch);
+    int off = coffset[t];
+    for (int o = b; o < e; ++o) {
+        const double w = bnew[SIN[o]];
+        if (w != 0.0) {
+            lst[off] = SIN[o];
+            cb[off] = w;
+            ++off;
+        }
     }
 }
 
@@ -711,11 +785,21 @@ extern "C" int irwls_sub_iterate(irwls_sub_ws *ws, const irwls_dev_set *X, doubl
     const int n = n1 + 1;
     KView kv = kview(X);
     if (n1 > 0) {
-        dim3 grid(ceil_div(n1, 64), n1);
-        const size_t smem = (size_t)X->ld * sizeof(double);
-        if (smem > 48 * 1024) cudaFuncSetAttribute(build_H_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        build_H_kernel<<<grid, 64, smem, irwls_stream()>>>(*ws, kv, n1);
-        IRWLS_LAUNCH_CHECK("build_H");
+        // precision form on integer-valued data: the kernel block from exact
+        // tensor-core dot products (FP64 exp), then the diagonal's 1 / a
+        const int ex = irwls_tc_exact_block(ws->tcs, X, ws->gl1, n1, ws->gl1, n1, X->y, X->y, ws->H, ws->ldH, 1);
+        if (ex < 0) return -2;
+        if (ex == 0) {
+            build_H_diag_kernel<<<ceil_div(n1, 256), 256, 0, irwls_stream()>>>(*ws, n1);
+            IRWLS_LAUNCH_CHECK("build_H_diag");
+        } else {
+            dim3 grid(ceil_div(n1, 64), n1);
+            const size_t smem = (size_t)X->ld * sizeof(double);
+            if (smem > 48 * 1024)
+                cudaFuncSetAttribute(build_H_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            build_H_kernel<<<grid, 64, smem, irwls_stream()>>>(*ws, kv, n1);
+            IRWLS_LAUNCH_CHECK("build_H");
+        }
     }
     build_border_kernel<<<ceil_div(n1 + 1, 256), 256, 0, irwls_stream()>>>(*ws, n1);
     IRWLS_LAUNCH_CHECK("build_border");
@@ -747,8 +831,17 @@ extern "C" int irwls_sub_iterate(irwls_sub_ws *ws, const irwls_dev_set *X, doubl
 
 extern "C" int irwls_full_gin(const irwls_dev_set *X, const int *d_SW, int nSW, const int *d_SIN, int nSIN,
                               const double *d_bnew, int *d_lst, double *d_cb, int *d_cnt, double *d_GIN) {
-    gin_prepare_kernel<<<1, CT, 0, irwls_stream()>>>(d_SIN, nSIN, d_bnew, d_lst, d_cb, d_cnt, d_GIN, nSW);
-    IRWLS_LAUNCH_CHECK("gin_prepare");
+    // scratch slot 2: the chunk counts (then offsets) and chunk sums
+    unsigned char *sc = (unsigned char *)irwls_ctx_scratch(2, (size_t)CT * (sizeof(int) + sizeof(double)));
+    if (!sc) return -3;
+    double *csum = (double *)sc;
+    int *ccount = (int *)(sc + (size_t)CT * sizeof(double));
+    gin_chunk_kernel<<<CT / PC, PC, 0, irwls_stream()>>>(d_SIN, nSIN, d_bnew, ccount, csum);
+    IRWLS_LAUNCH_CHECK("gin_chunk");
+    gin_scan_kernel<<<1, CT, 0, irwls_stream()>>>(ccount, csum, d_cnt, d_GIN, nSW);
+    IRWLS_LAUNCH_CHECK("gin_scan");
+    gin_write_kernel<<<CT / PC, PC, 0, irwls_stream()>>>(d_SIN, nSIN, d_bnew, ccount, d_lst, d_cb);
+    IRWLS_LAUNCH_CHECK("gin_write");
     return irwls_dev_kernel_rowsum_n(X, d_SW, nSW, X, d_lst, d_cnt, d_cb, X->y, nullptr, +1, nullptr, nullptr,
                                      d_GIN);
 }
@@ -769,8 +862,12 @@ extern "C" int irwls_full_apply_ws(const int *d_SW, int nSW, const double *d_bt,
 }
 
 extern "C" int irwls_full_norms(const double *d_beta, const double *d_bnew, int n, double *d_out2) {
-    norms_kernel<<<1, CT, 0, irwls_stream()>>>(d_beta, d_bnew, n, d_out2);
-    IRWLS_LAUNCH_CHECK("norms");
+    double *part = (double *)irwls_ctx_scratch(2, (size_t)2 * CT * sizeof(double));
+    if (!part) return -3;
+    norms_chunk_kernel<<<CT / PC, PC, 0, irwls_stream()>>>(d_beta, d_bnew, n, part);
+    IRWLS_LAUNCH_CHECK("norms_chunk");
+    norms_final_kernel<<<1, CT, 0, irwls_stream()>>>(part, d_out2);
+    IRWLS_LAUNCH_CHECK("norms_final");
     return 0;
 }
 

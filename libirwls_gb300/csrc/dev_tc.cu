@@ -1830,13 +1830,16 @@ __global__ void rs_gather_rows_kernel(const __nv_bfloat16 *__restrict__ A, int k
     }
 }
 
-template <int CW>
+// STORE: the kernel values themselves, out[j * ldp + i] = (k_ij sa_i) sb_j
+// (a column-major block; with `lower`, items wholly above the diagonal are
+// skipped), instead of partial row sums.
+template <int CW, bool STORE>
 __global__ void __launch_bounds__(EX_THREADS, 1) tc_exact_rowsum_kernel(
     const __nv_bfloat16 *__restrict__ A, int M, int kbn, const __nv_bfloat16 *__restrict__ B,
     const int *__restrict__ d_n, int nmax, int nchx, const double *__restrict__ q, const int *__restrict__ ia,
     const int *__restrict__ ib, int rbf, double ng, double dscale, const double *__restrict__ cb,
-    const double *__restrict__ sa, const double *__restrict__ sb, double *__restrict__ part, int ldp, int *flags,
-    long long wait_limit) {
+    const double *__restrict__ sa, const double *__restrict__ sb, double *__restrict__ part, long long ldp,
+    int lower, int *flags, long long wait_limit) {
     static_assert(CW == 64 || CW == 128 || CW == 256, "column width");
     constexpr uint32_t A_BYTES = RS_APIECE * 2, B_MAX = CW * RS_BK * 2;
     extern __shared__ __align__(1024) unsigned char ex_smem[];
@@ -1847,6 +1850,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1) tc_exact_rowsum_kernel(
     const int N = max(0, min(*d_n, nmax));
     const int tile = (int)blockIdx.x / nchx, h = (int)blockIdx.x % nchx, c0 = h * CW;
     if (c0 >= N) return;  // the list is shorter than this item's columns
+    if (STORE && lower && c0 > tile * RS_BM + RS_BM - 1) return;  // above the diagonal
     unsigned char *smem = ex_smem + ((1024 - (smem_u32(ex_smem) & 1023)) & 1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ncols = min(CW, N - c0), nr16 = (ncols + 15) / 16 * 16;
@@ -1938,13 +1942,19 @@ __global__ void __launch_bounds__(EX_THREADS, 1) tc_exact_rowsum_kernel(
                     double t = cb ? cb[j] * kv : kv;
                     if (sa) t *= sai;
                     if (sb) t *= sb[gj];
-                    acc += t;
+                    if (STORE) {
+                        if (valid) part[(size_t)j * ldp + row] = t;
+                    } else {
+                        acc += t;
+                    }
                 }
             }
         }
-        if (gh == 1) half_sum[r] = acc;
-        asm volatile("bar.sync 1, %0;\n" ::"r"(EX_THREADS));
-        if (gh == 0 && valid) part[(size_t)h * ldp + row] = acc + half_sum[r];
+        if (!STORE) {
+            if (gh == 1) half_sum[r] = acc;
+            asm volatile("bar.sync 1, %0;\n" ::"r"(EX_THREADS));
+            if (gh == 0 && valid) part[(size_t)h * ldp + row] = acc + half_sum[r];
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
@@ -1971,16 +1981,38 @@ __global__ void ex_combine_kernel(const double *__restrict__ part, int ldp, int 
 
 __global__ void set_int_kernel(int *p, int v) { *p = v; }
 
-template <int CW>
+template <int CW, bool STORE>
 int ex_launch(TcSet *t, const irwls_dev_set *X, int nA, const int *d_ia, const int *d_ib, const int *d_n, int nmax,
-              const double *d_cb, const double *d_sa, const double *d_sb) {
+              const double *d_cb, const double *d_sa, const double *d_sb, double *out, long long ldo, int lower) {
     const int ntiles = ceil_div(nA, RS_BM), nchx = ceil_div(nmax, CW);
     const size_t smem = (size_t)EX_NS * (RS_APIECE * 2 + CW * RS_BK * 2) + 1024;
-    cudaFuncSetAttribute(tc_exact_rowsum_kernel<CW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    tc_exact_rowsum_kernel<CW><<<ntiles * nchx, EX_THREADS, smem, irwls_stream()>>>(
+    cudaFuncSetAttribute(tc_exact_rowsum_kernel<CW, STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    tc_exact_rowsum_kernel<CW, STORE><<<ntiles * nchx, EX_THREADS, smem, irwls_stream()>>>(
         t->Ag, nA, t->kbn, t->B, d_n, nmax, nchx, X->q, d_ia, d_ib, t->rbf, X->neg_gamma, 1.0 / (t->scale * t->scale),
-        d_cb, d_sa, d_sb, t->part, nA, irwls_dev_flags(), g_rs_wait_limit);
-    IRWLS_LAUNCH_CHECK("tc_exact_rowsum");
+        d_cb, d_sa, d_sb, out, ldo, lower, irwls_dev_flags(), g_rs_wait_limit);
+    IRWLS_LAUNCH_CHECK(STORE ? "tc_exact_block" : "tc_exact_rowsum");
+    return 0;
+}
+
+// Gathers the rows ia (nA) and the list entries ib (*d_n <= nmax) of the set.
+int ex_gather(TcSet *t, const irwls_dev_set *X, const int *d_ia, int nA, const int *d_ib, const int *d_n, int nmax,
+              const double *d_cb) {
+    const long long rows_pad = (long long)ceil_div(nA, RS_BM) * RS_BM;
+    if (rows_pad > t->ag_cap) {
+        irwls_dev_free(t->Ag);
+        t->Ag = nullptr;
+        t->ag_cap = 0;
+        if (irwls_dev_malloc((void **)&t->Ag, (size_t)rows_pad * t->kbn * RS_BK * sizeof(__nv_bfloat16))) return -3;
+        t->ag_cap = rows_pad;
+    }
+    const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
+    const int gr = std::max(1, std::min(ceil_div((long long)nA * t->kbn * 4, 256), 8 * sms));
+    rs_gather_rows_kernel<<<gr, 256, 0, irwls_stream()>>>(t->A, t->kbn, d_ia, nA, t->Ag);
+    IRWLS_LAUNCH_CHECK("tc_exact_gather_rows");
+    const int gb = std::max(1, std::min(ceil_div((long long)std::max(nmax, 1) * t->kbn * 4, 256), 4096));
+    rs_gather_kernel<1><<<gb, 256, 0, irwls_stream()>>>(t->A, t->kbn, t->q, d_ib, d_n, t->wmax, t->B, t->qb,
+                                                        d_cb ? d_cb : X->q, t->cbf);
+    IRWLS_LAUNCH_CHECK("tc_exact_gather_cols");
     return 0;
 }
 
@@ -2010,15 +2042,6 @@ extern "C" int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int 
         IRWLS_LAUNCH_CHECK("tc_exact_count");
         d_n = t->nbuf;
     }
-    // grow-only buffers: the gathered rows and the partial sums
-    const long long rows_pad = (long long)ceil_div(nA, RS_BM) * RS_BM;
-    if (rows_pad > t->ag_cap) {
-        irwls_dev_free(t->Ag);
-        t->Ag = nullptr;
-        t->ag_cap = 0;
-        if (irwls_dev_malloc((void **)&t->Ag, (size_t)rows_pad * t->kbn * RS_BK * sizeof(__nv_bfloat16))) return -3;
-        t->ag_cap = rows_pad;
-    }
     const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
     const int ntiles = ceil_div(nA, RS_BM);
     // column width: enough items for every SM when the tiles are few
@@ -2032,22 +2055,40 @@ extern "C" int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int 
         t->part_cap = need;
     }
     if (nbmax > 0) {
-        const int gr = std::max(1, std::min(ceil_div((long long)nA * t->kbn * 4, 256), 8 * sms));
-        rs_gather_rows_kernel<<<gr, 256, 0, irwls_stream()>>>(t->A, t->kbn, d_ia, nA, t->Ag);
-        IRWLS_LAUNCH_CHECK("tc_exact_gather_rows");
-        const int gb = std::max(1, std::min(ceil_div((long long)nbmax * t->kbn * 4, 256), 4096));
-        rs_gather_kernel<1><<<gb, 256, 0, irwls_stream()>>>(t->A, t->kbn, t->q, d_ib, d_n, t->wmax, t->B, t->qb,
-                                                            d_cb ? d_cb : X->q, t->cbf);
-        IRWLS_LAUNCH_CHECK("tc_exact_gather_cols");
+        int rc = ex_gather(t, X, d_ia, nA, d_ib, d_n, nbmax, d_cb);
+        if (rc) return rc;
         if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
-        const int rc = cw == 128 ? ex_launch<128>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb)
-                                 : ex_launch<64>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb);
+        rc = cw == 128 ? ex_launch<128, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0)
+                       : ex_launch<64, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0);
         if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
         if (rc) return rc;
     }
     ex_combine_kernel<<<std::max(1, std::min(ceil_div(nA, 256), 4 * sms)), 256, 0, irwls_stream()>>>(
         t->part, nA, nA, d_n, nbmax, cw, op, d_init, d_tail, d_out);
     IRWLS_LAUNCH_CHECK("tc_exact_combine");
+    ++g_ex_calls;
+    return 0;
+}
+
+// The kernel block itself in the exact-integer mode: out[j * ldo + i] =
+// (k(x_ia[i], x_ib[j]) sa_ia[i]) sb_ib[j] for i < nA, j < nB (sa, sb
+// optional); with `lower`, only the blocks on or below the diagonal (i >= j
+// up to the 128 x 64 item grid; the rest of the upper part may be left
+// unwritten). Returns 1 when the set does not allow it or nB exceeds its
+// gather room.
+extern "C" int irwls_tc_exact_block(void *h, const irwls_dev_set *X, const int *d_ia, int nA, const int *d_ib, int nB,
+                                    const double *d_sa, const double *d_sb, double *d_out, long long ldo, int lower) {
+    TcSet *t = (TcSet *)h;
+    if (!t || !t->exact || nB > t->wmax || nB < 0) return 1;
+    if (nA <= 0 || nB <= 0) return 0;
+    set_int_kernel<<<1, 1, 0, irwls_stream()>>>(t->nbuf, nB);
+    IRWLS_LAUNCH_CHECK("tc_exact_count");
+    int rc = ex_gather(t, X, d_ia, nA, d_ib, t->nbuf, nB, nullptr);
+    if (rc) return rc;
+    if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
+    rc = ex_launch<64, true>(t, X, nA, d_ia, d_ib, t->nbuf, nB, nullptr, d_sa, d_sb, d_out, ldo, lower);
+    if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
+    if (rc) return rc;
     ++g_ex_calls;
     return 0;
 }

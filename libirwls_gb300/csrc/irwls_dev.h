@@ -246,6 +246,11 @@ int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int *d_ia, int 
                           const int *d_nB, int nbmax, const double *d_cb, const double *d_sa, const double *d_sb,
                           int op, const double *d_init, const double *d_tail, double *d_out);
 int irwls_tc_set_exact(void *h);
+/* The same mode writing the kernel block: out[j * ldo + i] =
+ * (k(ia_i, ib_j) sa_{ia_i}) sb_{ib_j} for i < nA, j < nB (only the blocks
+ * touching the lower triangle when `lower`); 1 when not applicable. */
+int irwls_tc_exact_block(void *h, const irwls_dev_set *X, const int *d_ia, int nA, const int *d_ib, int nB,
+                         const double *d_sa, const double *d_sb, double *d_out, long long ldo, int lower);
 int irwls_tc_kernel_rowsum(void *h, const int *d_idx, const int *d_n, const double *d_cb, const double *d_init,
                            const double *d_tail, double *d_out);
 /* Precision-form prediction: d_out = b + sum_j w_j k(t_i, s_j) (or its sign)
