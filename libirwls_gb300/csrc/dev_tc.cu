@@ -1840,7 +1840,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1) tc_exact_rowsum_kernel(
     const int *__restrict__ ib, int rbf, double ng, double dscale, const double *__restrict__ cb,
     const double *__restrict__ sa, const double *__restrict__ sb, double *__restrict__ part, long long ldp,
     int lower, int *flags, long long wait_limit) {
-    static_assert(CW == 64 || CW == 128 || CW == 256, "column width");
+    static_assert(CW == 32 || CW == 64 || CW == 128, "column width");
+    // columns per warp group in the epilogue (one group when CW is 32)
+    constexpr int HALF = CW >= 64 ? CW / 2 : CW;
     constexpr uint32_t A_BYTES = RS_APIECE * 2, B_MAX = CW * RS_BK * 2;
     extern __shared__ __align__(1024) unsigned char ex_smem[];
     __shared__ __align__(8) uint64_t full[EX_NS], empty[EX_NS], accf;
@@ -1927,8 +1929,8 @@ __global__ void __launch_bounds__(EX_THREADS, 1) tc_exact_rowsum_kernel(
         const int gi = valid ? ia[row] : 0;
         const double qi = valid ? q[gi] : 0.0, sai = (valid && sa) ? sa[gi] : 1.0;
         double acc = 0.0;
-        for (int cc = 0; cc < CW / 2; cc += 32) {
-            const int cbase = gh * (CW / 2) + cc;
+        for (int cc = 0; cc < HALF; cc += 32) {
+            const int cbase = gh * HALF + cc;
             if (cbase >= ncols) break;
             float v[32];
             tc_ld32_lanes(tmem, 32 * ew, cbase, v);
@@ -2045,7 +2047,8 @@ extern "C" int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int 
     const int sms = irwls_num_sms() > 0 ? irwls_num_sms() : 148;
     const int ntiles = ceil_div(nA, RS_BM);
     // column width: enough items for every SM when the tiles are few
-    const int cw = (long long)ntiles * ceil_div(std::max(nbmax, 1), 128) >= 2LL * sms ? 128 : 64;
+    int cw = 128;
+    while (cw > 32 && (long long)ntiles * ceil_div(std::max(nbmax, 1), cw) < 2LL * sms) cw >>= 1;
     const long long need = (long long)ceil_div(std::max(nbmax, 1), cw) * nA;
     if (need > t->part_cap) {
         irwls_dev_free(t->part);
@@ -2058,8 +2061,9 @@ extern "C" int irwls_tc_exact_rowsum(void *h, const irwls_dev_set *X, const int 
         int rc = ex_gather(t, X, d_ia, nA, d_ib, d_n, nbmax, d_cb);
         if (rc) return rc;
         if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
-        rc = cw == 128 ? ex_launch<128, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0)
-                       : ex_launch<64, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0);
+        rc = cw == 128  ? ex_launch<128, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0)
+             : cw == 64 ? ex_launch<64, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0)
+                        : ex_launch<32, false>(t, X, nA, d_ia, d_ib, d_n, nbmax, d_cb, d_sa, d_sb, t->part, nA, 0);
         if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
         if (rc) return rc;
     }
@@ -2086,7 +2090,7 @@ extern "C" int irwls_tc_exact_block(void *h, const irwls_dev_set *X, const int *
     int rc = ex_gather(t, X, d_ia, nA, d_ib, t->nbuf, nB, nullptr);
     if (rc) return rc;
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_ROWSUM);
-    rc = ex_launch<64, true>(t, X, nA, d_ia, d_ib, t->nbuf, nB, nullptr, d_sa, d_sb, d_out, ldo, lower);
+    rc = ex_launch<32, true>(t, X, nA, d_ia, d_ib, t->nbuf, nB, nullptr, d_sa, d_sb, d_out, ldo, lower);
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_ROWSUM);
     if (rc) return rc;
     ++g_ex_calls;
