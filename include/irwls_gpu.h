@@ -181,7 +181,7 @@ void irwls_last_run_info(int *par_iterations, int *active_rows);
  * iterations of active_rows * (m + 1) * m (lower triangle and K2 row). */
 double irwls_last_gram_flops(void);
 /* bf16 tensor-core flops issued by the precision form's Gram kernel since
- * the last call with reset != 0 (36 digit-pair products per tile step). */
+ * the last call with reset != 0 (28 digit-pair products per tile step). */
 double irwls_gram_tc_flops(int reset);
 /* Host-to-device and device-to-host bytes copied since the library was loaded. */
 void irwls_transfer_bytes(long long *h2d, long long *d2h);

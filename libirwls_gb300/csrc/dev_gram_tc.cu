@@ -9,23 +9,24 @@
 //
 // 1. Each column c of A' gets a power of two sigma_c >= max_p |A'_pc| (a
 //    column-max pass), and each entry becomes the integer
-//    N_pc = round(A'_pc / sigma_c * 2^47), |N| <= 2^47, by integer operations
-//    on its bits. N is written in 8 balanced base-64 digits d_0 .. d_7
-//    (d_0 lowest), |d_s| <= 32 (|d_7| <= 33): small integers, exact in bf16.
-// 2. sum_p N_pi N_pj = sum_u 64^u L_u(i, j), L_u = sum_{s+t=u} sum_p
-//    d_s(p,i) d_t(p,j). The levels u = 7 ... 14 are kept (36 digit pairs);
-//    the dropped levels weigh at most 2^-44 of the top one, so each entry of
-//    G carries an error of about 2^-47 max|A'_.i| max|A'_.j| per row, the
-//    accuracy of the double-float Gram this replaces.
+//    N_pc = round(A'_pc / sigma_c * 2^48), |N| <= 2^48, by integer operations
+//    on its bits. N is written in 7 balanced base-128 digits d_0 .. d_6
+//    (d_0 lowest), |d_s| <= 64: small integers, exact in bf16.
+// 2. sum_p N_pi N_pj = sum_u 128^u L_u(i, j), L_u = sum_{s+t=u} sum_p
+//    d_s(p,i) d_t(p,j). The levels u = 6 ... 12 are kept (28 digit pairs);
+//    the dropped levels weigh at most about 2^-46 of the top one, so each
+//    entry of G carries an error of about 2^-46 max|A'_.i| max|A'_.j| per
+//    row, the accuracy of the double-float Gram this replaces.
 // 3. A CTA owns a 128 x 64 tile of G and one split-K chunk of the rows. Per
-//    16-row stage the 36 digit-pair products go to 8 level accumulators of
-//    128 x 64 FP32 in tensor memory (all 512 columns). Every product is an
-//    integer of magnitude <= 33^2 = 1089 and a level sums at most 8 pairs, so
-//    over 1024 rows every partial sum is an integer below 8 * 1024 * 1089 <
-//    2^24: exact in FP32, whatever the order of accumulation. Every 1024 rows
-//    the epilogue drains the levels into a 96-bit integer per entry
-//    (T += sum_u 64^(u-7) L_u), so the whole sum stays exact.
-// 4. G_ij = sigma_i sigma_j 2^-52 T_ij, written as the FP64 partials that
+//    16-row stage the 28 digit-pair products go to 7 level accumulators of
+//    128 x 64 FP32 in tensor memory (448 of its 512 columns). Every product
+//    is an integer of magnitude <= 64^2 = 4096 and a level sums at most 7
+//    pairs, so over 512 rows every partial sum is an integer below
+//    7 * 512 * 4096 < 2^24: exact in FP32, whatever the order of
+//    accumulation. Every 512 rows the epilogue drains the levels into a
+//    96-bit integer per entry (T += sum_u 128^(u-6) L_u), so the whole sum
+//    stays exact.
+// 4. G_ij = sigma_i sigma_j 2^-54 T_ij, written as the FP64 partials that
 //    gram_reduce_kernel adds to KC.
 //
 // Operands reach shared memory by bulk copies: the slices are stored in the
@@ -43,17 +44,22 @@
 
 namespace {
 
-constexpr int GS = 8;                  // digits per entry
-constexpr int GFRAC = 47;              // N = round(v * 2^47), |v| <= 1
+constexpr int GS = 7;                  // digits per entry
+constexpr int GBITS = 7;               // digit base 2^7
+constexpr int GFRAC = 48;              // N = round(v * 2^48), |v| <= 1
+constexpr int GPAIRS = GS * (GS + 1) / 2;            // digit pairs of the kept levels
+constexpr int GSCALE = 2 * GFRAC - GBITS * (GS - 1);  // G = sigma_i sigma_j 2^-GSCALE T
 constexpr int GM = 128, GN = 64;       // tile of G: rows (A' columns) x columns
 constexpr int GBK = 16;                // rows of A' per stage
 constexpr int GPIECE = GM * GBK;       // elements of one digit piece (4 KB)
-constexpr int GDRAIN = 64;             // stages between drains (1024 rows)
-constexpr int GNS = 4;                 // ring stages
+constexpr int GDRAIN = 32;             // stages between drains (512 rows)
+constexpr int GNS = 5;                 // ring stages
 constexpr int G_THREADS = 384;
-constexpr uint32_t A_STAGE = GS * GPIECE * 2;      // 32 KB: 8 pieces of 128 rows
+constexpr uint32_t A_STAGE = GS * GPIECE * 2;      // 28 KB: 7 pieces of 128 rows
 constexpr uint32_t B_PIECE = GN * GBK * 2;         // 2 KB: 64 rows of one piece
-constexpr uint32_t G_STAGE = A_STAGE + GS * B_PIECE;  // 48 KB
+constexpr uint32_t G_STAGE = A_STAGE + GS * B_PIECE;  // 42 KB
+static_assert(GS * 64 <= 512, "level accumulators exceed tensor memory");
+static_assert((long long)GS * GDRAIN * GBK * (1 << (2 * (GBITS - 1))) < (1LL << 24), "level sums must stay exact");
 
 // Element offset of (row r of the 128-row tile, k of the 16-row block) in a
 // digit piece: 8 x 8 core matrices, 128 bytes apart along k, 256 along r.
@@ -101,20 +107,21 @@ __device__ __forceinline__ int col_exp(unsigned long long mxbits) {
     return E - 1023 + (pow2 ? 0 : 1);
 }
 
-// round(v * 2^(47 - e)) for |v| <= 2^e, from the bits of v (no FP64 pipe).
-__device__ __forceinline__ long long fixed47(double v, int e) {
+// round(v * 2^(48 - e)) for |v| <= 2^e, ties away from zero, from the bits of
+// v (no FP64 pipe).
+__device__ __forceinline__ long long fixed48(double v, int e) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
     const int E = (int)((b >> 52) & 0x7ff);
     if (E == 0) return 0;  // zero (subnormals, below 2^-1022, are dropped)
     const unsigned long long M = (b & ((1ULL << 52) - 1)) | (1ULL << 52);
     // v = M 2^(E - 1075); N = M 2^(E - 1075 + 47 - e) = M >> sh
-    const int sh = 1075 + e - GFRAC - E;  // >= 5 since |v| <= 2^e
+    const int sh = 1075 + e - GFRAC - E;  // >= 4 since |v| <= 2^e
     long long N = 0;
     if (sh < 64) N = (long long)((M + (1ULL << (sh - 1))) >> sh);
     return (b >> 63) ? -N : N;
 }
 
-// The slices of A'. Thread = (column c, group of 8 rows): the 8 digits of the
+// The slices of A'. Thread = (column c, group of 8 rows): the 7 digits of the
 // group's entries, one 16-byte store per digit piece. Rows >= nact and
 // columns > m are written as zeros.
 __global__ void __launch_bounds__(256) gram_slice_kernel(const double *__restrict__ KSC, int m,
@@ -123,9 +130,9 @@ __global__ void __launch_bounds__(256) gram_slice_kernel(const double *__restric
                                                          const double *__restrict__ day,
                                                          const unsigned long long *__restrict__ cmax, int ncols,
                                                          int npb, __nv_bfloat16 *__restrict__ S) {
-    __shared__ uint16_t bf[67];  // bf16 bits of -33 ... 33
-    if (threadIdx.x < 67) {
-        const __nv_bfloat16 h = __float2bfloat16_rn((float)((int)threadIdx.x - 33));
+    __shared__ uint16_t bf[129];  // bf16 bits of -64 ... 64
+    if (threadIdx.x < 129) {
+        const __nv_bfloat16 h = __float2bfloat16_rn((float)((int)threadIdx.x - 64));
         bf[threadIdx.x] = *(const uint16_t *)&h;
     }
     __syncthreads();
@@ -143,19 +150,19 @@ __global__ void __launch_bounds__(256) gram_slice_kernel(const double *__restric
             long long N = 0;
             if (p < nact && c <= m && e > -1100) {
                 const double v = c < m ? __dmul_rn(sd[p], KSC[(size_t)act[p] * m + c]) : day[p];
-                N = fixed47(v, e);
+                N = fixed48(v, e);
             }
 #pragma unroll
             for (int s = 0; s < GS; ++s) {
                 int d;
                 if (s < GS - 1) {
-                    d = (int)(N & 63);
-                    if (d >= 32) d -= 64;
-                    N = (N - d) >> 6;
+                    d = (int)(N & 127);
+                    if (d >= 64) d -= 128;
+                    N = (N - d) >> 7;
                 } else {
-                    d = (int)N;  // |d| <= 33
+                    d = (int)N;  // |d| <= 64
                 }
-                const uint32_t hb = bf[d + 33];
+                const uint32_t hb = bf[d + 64];
                 if (k & 1) w[s][k >> 1] |= hb << 16;
                 else w[s][k >> 1] = hb;
             }
@@ -267,7 +274,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
         }
         __syncwarp();
     } else if (warp == 1) {
-        // MMA issue: level u - 7 += sum_{s+t=u} A_s B_t, u = 7 ... 14
+        // MMA issue: level u - 6 += sum_{s+t=u} A_s B_t, u = 6 ... 12
         if (lane == 0) {
             constexpr uint32_t idesc = tc_idesc(GM, GN);
             const uint32_t base = smem_u32(smem);
@@ -337,17 +344,16 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
                 for (int v = 0; v < GS; ++v) tc_ld4(lanes + v * GN + c4, L[v]);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    // levels 11-14 and 7-10 by Horner in 64-bit integers (each
-                    // below 2^44), then T += t_hi 2^24 + t_lo
-                    long long th = __float2int_rn(L[7][j]);
-                    th = th * 64 + __float2int_rn(L[6][j]);
-                    th = th * 64 + __float2int_rn(L[5][j]);
-                    th = th * 64 + __float2int_rn(L[4][j]);
-                    long long tl = __float2int_rn(L[3][j]);
-                    tl = tl * 64 + __float2int_rn(L[2][j]);
-                    tl = tl * 64 + __float2int_rn(L[1][j]);
-                    tl = tl * 64 + __float2int_rn(L[0][j]);
-                    acc_add(T[c4 + j], th >> 8, (uint32_t)th << 24);
+                    // levels 9-12 and 6-8 by Horner in 64-bit integers (below
+                    // 2^45 and 2^38), then T += t_hi 2^21 + t_lo
+                    long long th = __float2int_rn(L[6][j]);
+                    th = th * 128 + __float2int_rn(L[5][j]);
+                    th = th * 128 + __float2int_rn(L[4][j]);
+                    th = th * 128 + __float2int_rn(L[3][j]);
+                    long long tl = __float2int_rn(L[2][j]);
+                    tl = tl * 128 + __float2int_rn(L[1][j]);
+                    tl = tl * 128 + __float2int_rn(L[0][j]);
+                    acc_add(T[c4 + j], th >> 11, (uint32_t)th << 21);
                     acc_add(T[c4 + j], tl >> 32, (uint32_t)tl);
                 }
             }
@@ -367,7 +373,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
                         double g = 0.0;
                         if (er > -1100 && ec > -1100) {
                             const double t = fma((double)T[j].hi, 4294967296.0, (double)T[j].lo);
-                            g = ldexp(t, er + ec - 52);
+                            g = ldexp(t, er + ec - GSCALE);
                         }
                         out[c] = g;
                     }
@@ -389,7 +395,7 @@ size_t slices_bytes(int l, int m) {
 
 }  // namespace
 
-// bf16 tensor-core flops issued by gram_tc_kernel since the last read (36
+// bf16 tensor-core flops issued by gram_tc_kernel since the last read (28
 // digit-pair products per 128 x 64 x 16 step of every tile).
 static double g_tc_flops = 0.0;
 extern "C" double irwls_gram_tc_flops(int reset) {
@@ -441,7 +447,7 @@ extern "C" int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, i
     cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     gram_tc_kernel<<<dim3(nt, ct, pz), G_THREADS, smem, irwls_stream()>>>(S, npb, spc, m, cmax, d_part,
                                                                           irwls_dev_flags());
-    g_tc_flops += (double)tiles * npb * GBK * GM * GN * 2.0 * 36;
+    g_tc_flops += (double)tiles * npb * GBK * GM * GN * 2.0 * GPAIRS;
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_GRAM);
     IRWLS_LAUNCH_CHECK("gram_tc");
     return irwls_par_gram_reduce(d_part, pz, m, d_KC, d_K1, ldK1);

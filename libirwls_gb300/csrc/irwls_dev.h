@@ -198,7 +198,7 @@ size_t irwls_par_gram_part_bytes(int m, int P);
 int irwls_par_gram(const double *d_KSC, int m, const int *d_act, int nact, const double *d_sd,
                    const double *d_day, const double *d_KC, double *d_K1, int ldK1, double *d_part, int P);
 /* Precision form of the Gram on the tensor cores (dev_gram_tc.cu): A' as
-   exact base-64 integer digits per column scale, digit-pair products summed
+   exact base-128 integer digits per column scale, digit-pair products summed
    exactly in FP32 tensor memory and drained into 96-bit integers; d_ws holds
    irwls_par_gram_tc_bytes(l, m) bytes for up to l active rows. */
 size_t irwls_par_gram_tc_bytes(int l, int m);

@@ -7,11 +7,11 @@ function of the inputs alone and this model reproduces it bit for bit:
 1. v_pc = fl(sd_p * KSC[act_p, c]) for c < m, day_p for c = m; column scale
    sigma_c = 2^e_c, the smallest power of two >= max_p |v_pc| (e = None: the
    column is zero or subnormal);
-2. N_pc = round(v_pc * 2^(47 - e_c)), ties away from zero, subnormal v -> 0;
-   N in 8 balanced base-64 digits d_0 .. d_7 (d_s in [-32, 31], d_7 the rest);
+2. N_pc = round(v_pc * 2^(48 - e_c)), ties away from zero, subnormal v -> 0;
+   N in 7 balanced base-128 digits d_0 .. d_6 (d_s in [-64, 63], d_6 the rest);
 3. per split-K chunk z (16-row stages [z spc, (z + 1) spc)), the integer
-   T_z(i, j) = sum_p sum_{s + t >= 7} 64^(s + t - 7) d_s(p, i) d_t(p, j);
-4. part_z = ldexp(fma(double(hi), 2^32, lo), e_i + e_j - 52), T = hi 2^32 + lo;
+   T_z(i, j) = sum_p sum_{s + t >= 6} 128^(s + t - 6) d_s(p, i) d_t(p, j);
+4. part_z = ldexp(fma(double(hi), 2^32, lo), e_i + e_j - 54), T = hi 2^32 + lo;
 5. K1 = ((0 + part_0) + part_1 + ...) + KC (row m: no KC).
 
 The digit-level products are formed in FP64 matrix products: every entry is
@@ -21,7 +21,8 @@ import math
 
 import numpy as np
 
-GS, GFRAC, GM, GN, GBK = 8, 47, 128, 64, 16
+GS, GBITS, GFRAC, GM, GN, GBK = 7, 7, 48, 128, 64, 16
+GSCALE = 2 * GFRAC - GBITS * (GS - 1)
 
 
 def column_values(KSC, act, sd, day):
@@ -43,8 +44,8 @@ def column_exponents(A):
     return out
 
 
-def fixed47(v, e):
-    """round(v 2^(47 - e)) for a column v with |v| <= 2^e, from the bits of
+def fixed48(v, e):
+    """round(v 2^(48 - e)) for a column v with |v| <= 2^e, from the bits of
     each entry: ties away from zero, subnormal entries -> 0."""
     v = np.asarray(v, dtype=np.float64)
     if e is None:
@@ -53,21 +54,22 @@ def fixed47(v, e):
     M = (mant * 2.0 ** 53).astype(np.int64)  # |v| = M 2^(ex - 53), M < 2^53
     sh = 53 - ex.astype(np.int64) + e - GFRAC
     normal = np.abs(v) >= 2.2250738585072014e-308
-    assert np.all(sh[normal] >= 5)
+    assert np.all(sh[normal] >= 4)
     shc = np.clip(sh, 1, 63)
     N = np.where(normal & (sh < 64), (M + (np.int64(1) << (shc - 1))) >> shc, 0)
     return np.where(v < 0, -N, N)
 
 
 def digits(N):
-    """Balanced base-64 digits d_0 .. d_7 of N (arrays of Python ints)."""
+    """Balanced base-128 digits d_0 .. d_6 of N (int64 arrays)."""
     out = []
     N = N.copy()
+    base = 1 << GBITS
     for s in range(GS - 1):
-        d = N & 63
-        d = np.where(d >= 32, d - 64, d)
+        d = N & (base - 1)
+        d = np.where(d >= base // 2, d - base, d)
         out.append(d)
-        N = (N - d) >> 6
+        N = (N - d) >> GBITS
     out.append(N)
     return out
 
@@ -92,7 +94,7 @@ def gram(KSC, act, sd, day, KC, P, sms):
     es = column_exponents(A)
     N = np.zeros(A.shape, dtype=np.int64)
     for c in range(m + 1):
-        N[:, c] = fixed47(A[:, c], es[c])
+        N[:, c] = fixed48(A[:, c], es[c])
     D = [d.astype(np.float64) for d in digits(N)]
     pz, spc = chunking(nact, m, P, sms)
     total = np.zeros((m + 1, m))
@@ -104,7 +106,7 @@ def gram(KSC, act, sd, day, KC, P, sms):
             for s in range(u - (GS - 1), GS):
                 L += D[s][r0:r1].T @ D[u - s][r0:r1, :m]
             Li = L.astype(np.int64).astype(object)
-            T = Li if T is None else T * 64 + Li
+            T = Li if T is None else T * (1 << GBITS) + Li
         part = np.zeros((m + 1, m))
         for i in range(m + 1):
             for j in range(min(i + 1, m)):
@@ -113,7 +115,7 @@ def gram(KSC, act, sd, day, KC, P, sms):
                 t = int(T[i, j])
                 hi, lo = t >> 32, t & 0xFFFFFFFF
                 td = float(int(float(hi)) * (1 << 32) + lo)
-                part[i, j] = math.ldexp(td, es[i] + es[j] - 52)
+                part[i, j] = math.ldexp(td, es[i] + es[j] - GSCALE)
         total = total + part
     out = total.copy()
     out[:m] += KC

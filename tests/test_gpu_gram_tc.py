@@ -1,14 +1,14 @@
 """The tensor-core Gram of the precision form's IRWLSpar
 (libirwls_gb300/csrc/dev_gram_tc.cu): K1 = KC + A'^T A' with
-A' = [sd * KSC[act, :], day], from exact base-64 integer digits.
+A' = [sd * KSC[act, :], day], from exact base-128 integer digits.
 
 - Exactness: with integer entries below 2^20 every value is exact in the
-  47-bit fixed point of its column and every sum below 2^53, so the result must
+  48-bit fixed point of its column and every sum below 2^53, so the result must
   equal the int64 product bit for bit -- across drains (one split-K chunk of
-  2500 rows: three drains of 1024 rows) and across chunks.
+  2500 rows: five drains of 512 rows) and across chunks.
 - Accuracy on RBF-like data with weights spread over six decades, against an
   FP64 product: |G - G_ref|_ij <= 2^-40 sigma_i sigma_j sqrt(nact), sigma the
-  column scales (the dropped digit levels weigh 2^-45 sigma_i sigma_j per row
+  column scales (the dropped digit levels weigh about 2^-46 sigma_i sigma_j per row
   and carry random signs).
 - Bit for bit on real-valued data: every step of the kernel is exact or
   correctly rounded, so K1 must equal the host model of its arithmetic

@@ -1,8 +1,9 @@
 """The host model of the tensor-core Gram's arithmetic (tests/gram_digits.py),
 checked on the CPU before it is used to pin the kernel bit for bit:
 
-- the balanced base-64 digits rebuild N exactly and stay within +-33, so every
-  digit product is exact in bf16 and a 1024-row level sum stays below 2^24;
+- the balanced base-128 digits rebuild N exactly and stay within +-64, so
+  every digit product is exact in bf16 and a 512-row level sum stays below
+  2^24;
 - the fixed-point conversion rounds ties away from zero and drops subnormals;
 - on integer columns below 2^20 the model is the exact integer product;
 - on RBF-like columns with weights over six decades it is within the stated
@@ -18,24 +19,24 @@ BIG = 1 << 30  # SM count: any part with at least P x tiles SMs chunks alike
 
 def test_digits_rebuild_and_range():
     rng = np.random.default_rng(1)
-    N = rng.integers(-(1 << 47), (1 << 47) + 1, size=20000)
-    N[:4] = [1 << 47, -(1 << 47), (1 << 47) - 1, 0]
+    N = rng.integers(-(1 << 48), (1 << 48) + 1, size=20000)
+    N[:6] = [1 << 48, -(1 << 48), (1 << 48) - 1, -(1 << 48) + 1, 0, (1 << 47) + (1 << 41)]
     d = gd.digits(N)
-    back = sum(d[s] * (np.int64(64) ** s) for s in range(gd.GS))
+    back = sum(d[s] * (np.int64(128) ** s) for s in range(gd.GS))
     assert np.array_equal(back, N)
     for s in range(gd.GS - 1):
-        assert d[s].min() >= -32 and d[s].max() <= 31
-    assert np.abs(d[gd.GS - 1]).max() <= 33
-    # a level over 1024 rows: at most 8 pairs of products <= 33^2
-    assert 8 * 1024 * 33 * 33 < 1 << 24
+        assert d[s].min() >= -64 and d[s].max() <= 63
+    assert np.abs(d[gd.GS - 1]).max() <= 64
+    # a level over 512 rows: at most 7 pairs of products <= 64^2
+    assert 7 * 512 * 64 * 64 < 1 << 24
 
 
-def test_fixed47_rounding():
+def test_fixed48_rounding():
     e = 0
-    q = 2.0 ** -48  # half a unit of the 47-bit fixed point at sigma = 1
-    v = np.array([3 * q, -3 * q, 5 * q, -5 * q, q, 1.0, -1.0, 0.0, 1e-310, 2.0 ** -47])
-    assert list(gd.fixed47(v, e)) == [2, -2, 3, -3, 1, 1 << 47, -(1 << 47), 0, 0, 1]
-    assert list(gd.fixed47(v, None)) == [0] * len(v)
+    q = 2.0 ** -49  # half a unit of the 48-bit fixed point at sigma = 1
+    v = np.array([3 * q, -3 * q, 5 * q, -5 * q, q, 1.0, -1.0, 0.0, 1e-310, 2.0 ** -48])
+    assert list(gd.fixed48(v, e)) == [2, -2, 3, -3, 1, 1 << 48, -(1 << 48), 0, 0, 1]
+    assert list(gd.fixed48(v, None)) == [0] * len(v)
 
 
 def test_column_exponents():
