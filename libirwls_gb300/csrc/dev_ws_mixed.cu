@@ -61,42 +61,50 @@ constexpr int WWARPS = WT / 32;
 constexpr int LDB = WB + 1;                // padded row of a stored block
 constexpr int BLK = WB * LDB;              // floats per stored block
 constexpr int SR = WNB / WP, SCOL = WNB / WQ;  // owned row / column blocks per CTA
-constexpr int SLOTS = SR * SCOL;
+constexpr int SLOTS = SR * (SR + 1) / 2;       // owned blocks of a CTA (at most 10: p >= q)
 constexpr int MAXIT = 5;                   // refinement steps before giving up
 
-// shared-memory layout (floats)
+// shared-memory layout (floats); the receive and send buffers come in two
+// sets, used by steps of even and odd k
+constexpr int PSET = SR * WB * WB + 2 * SCOL * BLK;  // one set of receive buffers
 constexpr int OFF_A = 0;                       // A slots: the factor L
 constexpr int OFF_W = OFF_A + SLOTS * BLK;     // W slots: L^-1
 constexpr int OFF_PL = OFF_W + SLOTS * BLK;    // panel L_ik of my rows, transposed [t][r]
 constexpr int OFF_PC = OFF_PL + SR * WB * WB;  // panel L_jk of my columns [c][t]
 constexpr int OFF_PW = OFF_PC + SCOL * BLK;    // row k of W for my columns [t][c]
-constexpr int OFF_DK = OFF_PW + SCOL * BLK;    // L_kk, two buffers (step parity)
-constexpr int OFF_STG = OFF_DK + 2 * BLK;      // my panel blocks transposed, for sending
-constexpr int OFF_DI = OFF_STG + SR * WB * WB; // 1 / L_kk[t][t]
+constexpr int OFF_DK = OFF_PL + 2 * PSET;      // L_kk, two buffers
+constexpr int OFF_STG = OFF_DK + 2 * BLK;      // my panel blocks transposed, for sending (two sets)
+constexpr int OFF_DI = OFF_STG + 2 * SR * WB * WB;  // 1 / L_kk[t][t]
 constexpr int SMEM_FLOATS = OFF_DI + WB;
 constexpr size_t SMEM_BYTES = (size_t)SMEM_FLOATS * sizeof(float);
+static_assert(SMEM_BYTES + 256 <= 227 * 1024, "shared memory");
 
 // after the factorization the A slots and the panel buffers hold the solve's
 // vectors (same offsets in every CTA: partial sums are read remotely)
 constexpr int NV = WNB * WB;                   // padded order
-constexpr int OFF_VEC = OFF_A;                 // doubles: y, r, u, v
+constexpr int OFF_VEC = OFF_PL;                // doubles: y, r, u, v
 constexpr int OFF_BF = OFF_VEC + 2 * 4 * NV;   // floats: solve input [2][NV]
 constexpr int OFF_CF = OFF_BF + 2 * NV;        // floats: solve output [2][NV]
 constexpr int OFF_DP = OFF_CF + 2 * NV;        // doubles: per-slot row partials [SLOTS][2][WB]
 constexpr int OFF_DPC = OFF_DP + 2 * SLOTS * 2 * WB;  // doubles: per-slot column partials
 constexpr int OFF_VEND = OFF_DPC + 2 * SLOTS * 2 * WB;
-constexpr int OFF_ZP = OFF_PL;                 // floats: z partials [SR][2][WB]
+constexpr int OFF_ZP = OFF_VEND;               // floats: z partials [SR][2][WB]
 constexpr int OFF_ZF = OFF_ZP + SR * 2 * WB;   // floats: reduced z of my rows
 constexpr int OFF_XP = OFF_ZF + SR * 2 * WB;   // floats: x partials [SCOL][2][WB]
 constexpr int OFF_BP = OFF_XP + SCOL * 2 * WB; // floats: per-slot partials [SLOTS][2][WB]
 constexpr int OFF_RR = OFF_BP + SLOTS * 2 * WB;        // doubles: row residual partials [SR][2][WB]
 constexpr int OFF_RC = OFF_RR + 2 * SR * 2 * WB;       // doubles: column residual partials [SCOL][2][WB]
 constexpr int OFF_PEND = OFF_RC + 2 * SCOL * 2 * WB;
-static_assert(OFF_VEND <= OFF_W, "solve vectors overflow the A slots");
-static_assert(OFF_PEND <= SMEM_FLOATS, "partials overflow the panel buffers");
+static_assert(OFF_PEND <= OFF_DK, "solve vectors overflow the receive buffers");
 static_assert((OFF_PL % 4) == 0 && (OFF_RR % 2) == 0 && (OFF_DP % 2) == 0, "alignment");
 
-__device__ __forceinline__ int slot_of(int i, int j) { return (i / WP) * SCOL + (j / WQ); }
+// Slot of block (i, j), j <= i, on its owner: the owner's blocks in order of
+// (i / WP, j / WQ); a CTA with p >= q owns a + 1 of them in block row a, one
+// with p < q owns a.
+__device__ __forceinline__ int slot_of(int i, int j) {
+    const int a = i / WP, b = j / WQ;
+    return (i % WP >= j % WQ) ? a * (a + 1) / 2 + b : a * (a - 1) / 2 + b;
+}
 __device__ __forceinline__ int owner_of(int i, int j) { return (i % WP) * WQ + (j % WQ); }
 
 // Factors the stored block in place (lane = row), LAPACK's unblocked
@@ -217,6 +225,13 @@ __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity) {
 
 __device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
+// The two halves of a cluster barrier (every thread of every CTA calls them,
+// alternately).
+__device__ __forceinline__ void cluster_arrive() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+
 // Panel blocks of step k that CTA (p, q) receives: L_ik of its row blocks
 // i > k (transposed, 4 KB each), L_jk of its column blocks j > k and W_kj of
 // its column blocks j <= k (4224 bytes each).
@@ -237,18 +252,19 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
     __shared__ int bad_sh, flag_sh;
     __shared__ float redf[WWARPS];
     __shared__ double xn_sh;
-    // panel blocks received; L_kk received, one mbarrier per Dk buffer
-    __shared__ __align__(8) uint64_t pan_bar, dk_bar[2];
+    // panel blocks received, L_kk received: one mbarrier per buffer set
+    __shared__ __align__(8) uint64_t pan_bar[2], dk_bar[2];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int me = (int)cl.block_rank();
     const int p = me / WQ, q = me % WQ;
     const int NB = (n1 + WB - 1) / WB;
     float *A = sm + OFF_A, *W = sm + OFF_W, *PL = sm + OFF_PL, *PC = sm + OFF_PC, *PW = sm + OFF_PW;
     float *Dk = sm + OFF_DK, *STG = sm + OFF_STG, *dinv = sm + OFF_DI;
-    const uint32_t pan_b = smem_u32(&pan_bar), dk_b0 = smem_u32(&dk_bar[0]), dk_b1 = smem_u32(&dk_bar[1]);
+    const uint32_t dk_b0 = smem_u32(&dk_bar[0]), dk_b1 = smem_u32(&dk_bar[1]);
     if (tid == 0) {
         bad_sh = 0;
-        mbar_init(&pan_bar, 1);
+        mbar_init(&pan_bar[0], 1);
+        mbar_init(&pan_bar[1], 1);
         mbar_init(&dk_bar[0], 1);
         mbar_init(&dk_bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -291,13 +307,19 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
     // ---- factorization with W = L^-1 alongside ----
     // Every block a step produces is sent by its owner to the CTAs whose
     // updates read it; a receiver waits on its mbarrier for the bytes it
-    // expects. The cluster barrier at the top of a step keeps the receive
-    // buffers of step k from being written before every CTA finished step
-    // k - 1 (the L_kk buffers and their mbarriers alternate, since
-    // L_{k+1,k+1} is sent during step k).
+    // expects. Steps of even and odd k use separate buffer sets (receive
+    // buffers, send staging, L_kk, mbarriers), and a split cluster barrier
+    // runs one step behind: a CTA arrives when it has finished step k and,
+    // before it sends anything of step k + 2 into the set of step k (L_{k+2,
+    // k+2} at the end of step k + 1, panel blocks in step k + 2), waits until
+    // every CTA has arrived for step k. No CTA waits for the others' step
+    // k + 1.
     int dk_n[2] = {0, 0};  // L_kk blocks received per buffer (the mbarrier phases)
     for (int k = 0; k < NB; ++k) {
-        cl.sync();
+        const int par = k & 1;
+        float *PLk = PL + par * PSET, *PCk = PC + par * PSET, *PWk = PW + par * PSET;
+        float *STGk = STG + par * SR * WB * WB;
+        const uint32_t pan_b = smem_u32(&pan_bar[par]);
         const bool col_k = k % WQ == q, row_k = k % WP == p;
         if (col_k || row_k) {
             const uint32_t bar = (k & 1) ? dk_b1 : dk_b0;
@@ -313,7 +335,7 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
             if (col_k)
                 for (int ib = p; ib < NB; ib += WP) {
                     if (ib <= k || task++ % WWARPS != warp) continue;
-                    float *blk = A + slot_of(ib, k) * BLK, *st = STG + (ib / WP) * WB * WB;
+                    float *blk = A + slot_of(ib, k) * BLK, *st = STGk + (ib / WP) * WB * WB;
                     subst_rows(blk, D, dinv, lane);
                     __syncwarp();
 #pragma unroll 8
@@ -322,9 +344,9 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
                     if (lane == 0) {
                         proxy_fence();
                         for (int qq = 0; qq < WQ; ++qq)
-                            send(smem_u32(PL + (ib / WP) * WB * WB), smem_u32(st), WB * WB * 4, pan_b, p * WQ + qq);
+                            send(smem_u32(PLk + (ib / WP) * WB * WB), smem_u32(st), WB * WB * 4, pan_b, p * WQ + qq);
                         for (int pp = 0; pp < WP; ++pp)
-                            send(smem_u32(PC + (ib / WQ) * BLK), smem_u32(blk), BLK * 4, pan_b, pp * WQ + ib % WQ);
+                            send(smem_u32(PCk + (ib / WQ) * BLK), smem_u32(blk), BLK * 4, pan_b, pp * WQ + ib % WQ);
                     }
                 }
             if (row_k)
@@ -336,12 +358,12 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
                     if (lane == 0) {
                         proxy_fence();
                         for (int pp = 0; pp < WP; ++pp)
-                            send(smem_u32(PW + (jb / WQ) * BLK), smem_u32(blk), BLK * 4, pan_b, pp * WQ + q);
+                            send(smem_u32(PWk + (jb / WQ) * BLK), smem_u32(blk), BLK * 4, pan_b, pp * WQ + q);
                     }
                 }
         }
         if (tid == 0) expect_bytes(pan_b, panel_bytes(k, NB, p, q));
-        if (!wait_phase(pan_b, (uint32_t)k & 1u)) bad_sh = 3;
+        if (!wait_phase(pan_b, (uint32_t)(k >> 1) & 1u)) bad_sh = 3;
         __syncthreads();
         // the next diagonal block first, by warp 0, which then factors it
         // and sends it while the other warps apply the remaining updates
@@ -354,19 +376,21 @@ __global__ void __launch_bounds__(WT, 1) ws_mixed_kernel(const double *__restric
                 if (own_next && ib == k + 1 && jb == k + 1) w = 0;
                 else w = own_next ? 1 + task++ % (WWARPS - 1) : task++ % WWARPS;
                 if (w != warp) continue;
-                if (jb > k) block_update(A + slot_of(ib, jb) * BLK, PL + (ib / WP) * WB * WB, PC + (jb / WQ) * BLK, false, lane);
-                else block_update(W + slot_of(ib, jb) * BLK, PL + (ib / WP) * WB * WB, PW + (jb / WQ) * BLK, true, lane);
+                if (jb > k) block_update(A + slot_of(ib, jb) * BLK, PLk + (ib / WP) * WB * WB, PCk + (jb / WQ) * BLK, false, lane);
+                else block_update(W + slot_of(ib, jb) * BLK, PLk + (ib / WP) * WB * WB, PWk + (jb / WQ) * BLK, true, lane);
             }
         }
         if (own_next && warp == 0) {
             __syncwarp();
             if (!factor_warp(A + slot_of(k + 1, k + 1) * BLK, lane) && lane == 0) bad_sh = 1;
-            send_dk(k + 1);
         }
-        proxy_fence();  // this CTA's reads of the receive buffers precede the next step's sends into them
+        proxy_fence();  // this CTA's reads of the receive buffers precede later sends into them
         __syncthreads();
+        if (k >= 1) cluster_wait();  // every CTA has finished step k - 1
+        if (own_next && warp == 0) send_dk(k + 1);
+        cluster_arrive();  // this CTA has finished step k
     }
-    cl.sync();  // nobody reads the A slots remotely any more
+    if (NB > 0) cluster_wait();  // every CTA has finished the last step: no copy is in flight
 
     // ---- solves with W and FP64 refinement ----
     double *vy = (double *)(sm + OFF_VEC), *vr = vy + NV, *vu = vr + NV, *vv = vu + NV;
