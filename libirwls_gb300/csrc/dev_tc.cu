@@ -506,43 +506,12 @@ __global__ void to_f32_kernel(const double *__restrict__ in, long long n, float 
         out[t] = __double2float_rn(in[t]);
 }
 
-// Kernel values of one row of the set against 8 A rows held densely in FP32
-// (A row j at a + j * lda), each entry of the row read once.
-__device__ __forceinline__ void kentry8_f32(const KViewF &B, const float *a, int lda, const float *qa, int jb,
-                                            float out[8]) {
-    float acc[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
-    if (B.mode == IRWLS_K_RAW_RBF) {
-        const float *b = B.X + (size_t)jb * B.ld;
-        for (int t = 0; t < B.width; ++t) {
-            const float bt = b[t];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const float d = a[j * lda + t] - bt;
-                acc[j] = fmaf(d, d, acc[j]);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * acc[j]);
-        return;
-    }
-    const int p0 = B.rp[jb], p1 = B.rp[jb + 1];
-    for (int p = p0; p < p1; ++p) {
-        const float v = B.cv[p];
-        const int c = B.ci[p];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, a[j * lda + c], acc[j]);
-    }
-    if (B.mode == IRWLS_K_LINEAR) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) out[j] = acc[j];
-        return;
-    }
-    const float qb = B.q[jb];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
-}
+// Candidate rows of the score kernel in shared memory, feature-major: the 64
+// candidates' values of feature k at cat + k * CAT_LD, candidates contiguous
+// (so one float4 load gives four candidates). The stride is 68 floats: 16-byte
+// loads of lanes whose rows hold different features fall in different bank
+// groups for features that differ mod 8.
+constexpr int CAT_LD = 68;
 
 // Scores of the precision form: per candidate, the tile sums in 16 strided
 // groups with Kahan-compensated FP32 adds, the 16 group sums in FP64 in a
@@ -671,46 +640,95 @@ __device__ __forceinline__ TileRows stage_tile_rows(const KViewF &X, int m0, int
     return t;
 }
 
-// kentry8_f32 for tile row r (global row jb) from the staged rows; the same
-// FMA order, so the same values.
-__device__ __forceinline__ void kentry8_tile(const KViewF &B, const TileRows &T, const float *a, int lda,
-                                             const float *qa, int r, int jb, float out[8]) {
-    if (T.kind == 0) {
-        kentry8_f32(B, a, lda, qa, jb, out);
-        return;
-    }
-    float acc[8];
+// Kernel values of tile row r (global row jb) against 32 candidates, the
+// candidates' values of feature k at a[k * CAT_LD + j]. The row is read once
+// (from the staged tile rows, or from global memory when they were too large
+// to stage) and every entry updates the 32 sums; per candidate the FMAs run
+// in the row's entry order from 0, so the values do not depend on the
+// staging.
+__device__ __forceinline__ void kentry32_tile(const KViewF &B, const TileRows &T, const float *a, const float *qa,
+                                              int r, int jb, float out[32]) {
+    float acc[32];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] = 0.f;
-    if (T.kind == 2) {
-        const float *b = T.x + r * T.lds;
+    for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+    if (B.mode == IRWLS_K_RAW_RBF) {
+        const float *b = T.kind == 2 ? T.x + r * T.lds : B.X + (size_t)jb * B.ld;
         for (int t = 0; t < B.width; ++t) {
             const float bt = b[t];
+            const float4 *ap = (const float4 *)(a + t * CAT_LD);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const float d = a[j * lda + t] - bt;
-                acc[j] = fmaf(d, d, acc[j]);
+            for (int q = 0; q < 8; ++q) {
+                const float4 av = ap[q];
+                float d;
+                d = av.x - bt;
+                acc[4 * q] = fmaf(d, d, acc[4 * q]);
+                d = av.y - bt;
+                acc[4 * q + 1] = fmaf(d, d, acc[4 * q + 1]);
+                d = av.z - bt;
+                acc[4 * q + 2] = fmaf(d, d, acc[4 * q + 2]);
+                d = av.w - bt;
+                acc[4 * q + 3] = fmaf(d, d, acc[4 * q + 3]);
             }
         }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * acc[j]);
+        for (int j = 0; j < 32; ++j) out[j] = __expf(B.ng * acc[j]);
         return;
     }
-    const int p0 = T.rp[r], p1 = T.rp[r + 1];
+    const int *ci;
+    const float *cv;
+    int p0, p1;
+    float qb;
+    if (T.kind == 1) {
+        ci = T.ci;
+        cv = T.cv;
+        p0 = T.rp[r];
+        p1 = T.rp[r + 1];
+        qb = B.mode == IRWLS_K_NORM_RBF ? T.q[r] : 0.f;
+    } else {
+        ci = B.ci;
+        cv = B.cv;
+        p0 = B.rp[jb];
+        p1 = B.rp[jb + 1];
+        qb = B.mode == IRWLS_K_NORM_RBF ? B.q[jb] : 0.f;
+    }
     for (int p = p0; p < p1; ++p) {
-        const float v = T.cv[p];
-        const int c = T.ci[p];
+        const float v = cv[p];
+        const float4 *ap = (const float4 *)(a + ci[p] * CAT_LD);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[j] = fmaf(v, a[j * lda + c], acc[j]);
+        for (int q = 0; q < 8; ++q) {
+            const float4 av = ap[q];
+            acc[4 * q] = fmaf(v, av.x, acc[4 * q]);
+            acc[4 * q + 1] = fmaf(v, av.y, acc[4 * q + 1]);
+            acc[4 * q + 2] = fmaf(v, av.z, acc[4 * q + 2]);
+            acc[4 * q + 3] = fmaf(v, av.w, acc[4 * q + 3]);
+        }
     }
     if (B.mode == IRWLS_K_LINEAR) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) out[j] = acc[j];
+        for (int j = 0; j < 32; ++j) out[j] = acc[j];
         return;
     }
-    const float qb = T.q[r];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
+    for (int j = 0; j < 32; ++j) out[j] = __expf(B.ng * fmaxf(qa[j] + qb - 2.f * acc[j], 0.f));
+}
+
+// Sums over the warp's 32 lanes of 32 values per lane (v[j] of every lane for
+// j = 0 ... 31); on return lane j holds the sum for j in v[0]. At each step
+// a lane keeps half of its values and passes the other half to the lane that
+// differs in one index bit, so every sum is the tree that pairs lanes
+// differing in bit 4, then bit 3, ..., bit 0 (31 shuffles instead of 160 for
+// 32 separate butterflies). The adds are rounded explicitly.
+__device__ __forceinline__ void warp_sum32_transposed(float v[32], int lane) {
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const bool up = (lane & h) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const float keep = up ? v[i + h] : v[i];
+            const float send = up ? v[i] : v[i + h];
+            v[i] = __fadd_rn(keep, __shfl_xor_sync(0xffffffffu, send, h));
+        }
+    }
 }
 
 // EG epilogue groups of four warps (warps 4 ... 4 EG + 3), each scoring 64 / EG
@@ -726,12 +744,13 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     __shared__ uint32_t tmem_slot;
     __shared__ float qc[64];
     constexpr int EPI = 128 * EG, CPG = 64 / EG;  // epilogue threads, candidates per group
+    static_assert(CPG == 32, "an epilogue warp scores 32 candidates");
     __shared__ float wred[4 * EG][CPG];
     __shared__ volatile int abort_flag;
     unsigned char *smem = tc_smem + ((1024 - (smem_u32(tc_smem) & 1023)) & 1023);
-    float *ca = (float *)(smem + NS * S::BYTES);
+    float *cat = (float *)(smem + NS * S::BYTES);  // candidate rows, feature-major (CAT_LD)
     // two buffers of xs_bytes: the rows of the tile being scored and of the next
-    unsigned char *xs = (unsigned char *)(ca + 64 * X.ld);
+    unsigned char *xs = (unsigned char *)(cat + CAT_LD * X.ld);
     __shared__ int srp[2][TC_BM + 1];
     __shared__ float sq[2][TC_BM];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -751,8 +770,8 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
         abort_flag = 0;
     }
     for (int t = threadIdx.x; t < 64 * X.ld; t += blockDim.x) {
-        const int c = t / X.ld, k = t % X.ld;
-        ca[t] = X.X[(size_t)cand[c] * X.ld + k];
+        const int c = t & 63, k = t >> 6;
+        cat[k * CAT_LD + c] = X.X[(size_t)cand[c] * X.ld + k];
     }
     if (threadIdx.x < 64) qc[threadIdx.x] = X.q[cand[threadIdx.x]];
     if (warp == 0) {
@@ -849,21 +868,20 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
             // thread finished before the barriers that closed it
             const TileRows Tn = j + 1 < my_tiles ? stage(j + 1) : T;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-            for (int c0 = CPG * g; c0 < CPG * g + CPG; c0 += 8) {
-                float v[8], kv[8];
-                tc_ld8_lanes(tmem + b * 64, 32 * ew, c0, v);
-                if (row < l) kentry8_tile(X, T, ca + (size_t)c0 * X.ld, X.ld, qc + c0, r, row, kv);
+            {
+                // this row's kernel values against the group's 32 candidates,
+                // then r^2 per candidate summed over the warp's 32 rows
+                float v[32];
+                if (row < l) kentry32_tile(X, T, cat + CPG * g, qc + CPG * g, r, row, v);
+                float acc[32];
+                tc_ld32_lanes(tmem + b * 64, 32 * ew, CPG * g, acc);
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                    float r2 = 0.f;
-                    if (row < l) {
-                        const float rr = v[jj] - kv[jj];
-                        r2 = rr * rr;
-                    }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-                    if (lane == 0) wred[4 * g + ew][c0 - CPG * g + jj] = r2;
+                for (int jj = 0; jj < 32; ++jj) {
+                    const float rr = __fsub_rn(acc[jj], v[jj]);
+                    v[jj] = row < l ? __fmul_rn(rr, rr) : 0.f;
                 }
+                warp_sum32_transposed(v, lane);
+                wred[4 * g + ew][lane] = v[0];
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
             if (lane == 0) mbar_arrive(&acce[b]);  // this warp's reads of accumulator b are done
@@ -912,8 +930,8 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
     const int n4 = (s + 3) / 4;  // float4s of a row that can be nonzero
     const bool raw = X.mode == IRWLS_K_RAW_RBF;
     for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += R * stride) {
-        int ir[R], pb[R], pe[R];
-        float acc[R], kd[R], qi[R], qo[R];
+        int ir[R], pb[R], pe[R], ec[R];
+        float acc[R], kd[R], qi[R], qo[R], ev[R];
         // every load of the R rows that does not depend on another is issued first
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -944,18 +962,39 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
                 acc[r] = fmaf(qv[r].w, lv.w, acc[r]);
             }
         }
-        // kernel entry against the new centroid
+        // each lane's first entry of the R rows' kernel entries, loaded
+        // together (one memory latency for the R rows, not one each)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            ev[r] = 0.f;
+            ec[r] = 0;
+            if (ir[r] < l) {
+                if (raw) {
+                    if (lane < X.width) ev[r] = X.X[(size_t)ir[r] * X.ld + lane];
+                } else if (pb[r] + lane < pe[r]) {
+                    ev[r] = X.cv[pb[r] + lane];
+                    ec[r] = X.ci[pb[r] + lane];
+                }
+            }
+        }
+        // kernel entry against the new centroid, each lane's entries in
+        // increasing order
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (ir[r] >= l) continue;
             if (raw) {
+                if (lane < X.width) {
+                    const float d = sc[lane] - ev[r];
+                    kd[r] = fmaf(d, d, kd[r]);
+                }
                 const float *b = X.X + (size_t)ir[r] * X.ld;
-                for (int t = lane; t < X.width; t += 32) {
+                for (int t = lane + 32; t < X.width; t += 32) {
                     const float d = sc[t] - b[t];
                     kd[r] = fmaf(d, d, kd[r]);
                 }
             } else {
-                for (int p = pb[r] + lane; p < pe[r]; p += 32) kd[r] = fmaf(X.cv[p], sc[X.ci[p]], kd[r]);
+                if (pb[r] + lane < pe[r]) kd[r] = fmaf(ev[r], sc[ec[r]], kd[r]);
+                for (int p = pb[r] + lane + 32; p < pe[r]; p += 32) kd[r] = fmaf(X.cv[p], sc[X.ci[p]], kd[r]);
             }
         }
 #pragma unroll
@@ -1051,7 +1090,7 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
         irwls_set_error(-12, "Q leading dimension %d does not hold order %d in 32-column blocks", ldq, s);
         return -12;
     }
-    const size_t fixed = 1024 + (size_t)64 * X->ld * sizeof(float);
+    const size_t fixed = 1024 + (size_t)CAT_LD * X->ld * sizeof(float);
     const size_t stage = TcRing<64, 2, WS_BK>::BYTES;
     if (fixed + 2 * stage > LIMIT) {
         irwls_set_error(-12, "feature width %d too wide for the precision-form SGMA tile", X->width);
