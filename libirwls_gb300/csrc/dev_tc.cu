@@ -904,16 +904,34 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
 }
 
-// New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3, a warp
-// per row, four rows in flight per warp (their independent loads issued
-// together). lrow holds l2 (s floats) then 1 / L3, written by the factor
-// step; the dot runs over the row's first s columns rounded up to 4 (Q's
-// columns >= s are still zero), each lane's float4s in increasing order. The
-// kernel entry is split over the warp's lanes; lane r finishes row r.
+// The sum over a warp's lanes that a butterfly of shuffles (xor 16, 8, 4, 2,
+// 1; each lane adding its partner's value to its own) leaves in every lane,
+// formed by one thread from the 32 lane values: the same pairs at every
+// level, so the same bits.
+__device__ __forceinline__ float butterfly_sum32(float v[32]) {
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1)
+#pragma unroll
+        for (int i = 0; i < h; ++i) v[i] = v[i] + v[i + h];
+    return v[0];
+}
+
+// New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3. lrow
+// holds l2 (s floats) then 1 / L3, written by the factor step. A warp takes
+// 32 consecutive rows, lane r finishing row r:
+// - the kernel entry of each row against the new centroid in the lane that
+//   owns it: the entries a lane of a warp-split loop would take (p = lane,
+//   lane + 32, ...) summed in that order into 32 partials, then combined in
+//   the butterfly's order, so the value is that of the warp-split form (all
+//   of a lane's loads are independent: one memory latency per 32 rows);
+// - the dot Q_i . l2 warp-split, eight rows at a time (their float4 loads
+//   issued together), each lane's float4s in increasing order over the
+//   row's first s columns rounded up to 4 (Q's columns >= s are still zero),
+//   then the butterfly.
 __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
                                                        const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qb,
                                                        int ldq, float *__restrict__ qn) {
-    constexpr int R = 4;  // rows in flight per warp
+    constexpr int R = 8;  // rows of a dot-product pass
     extern __shared__ float qsm[];
     const int s4 = (s + 127) / 128 * 128;  // <= ldq
     float *l2 = qsm;                       // s4 floats, zero past s
@@ -925,34 +943,51 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
     const float inv_l3 = lrow[s];
     const float qa = X.q[gc];
     const int lane = threadIdx.x & 31;
-    const int warps = blockDim.x >> 5;
-    const int stride = gridDim.x * warps;
     const int n4 = (s + 3) / 4;  // float4s of a row that can be nonzero
     const bool raw = X.mode == IRWLS_K_RAW_RBF;
-    for (int i = blockIdx.x * warps + (threadIdx.x >> 5); i < l; i += R * stride) {
-        int ir[R], pb[R], pe[R], ec[R];
-        float acc[R], kd[R], qi[R], qo[R], ev[R];
-        // every load of the R rows that does not depend on another is issued first
+    const int r0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+    if (r0 >= l) return;
+    const int row = r0 + lane;
+    const bool mine = row < l;
+    // this lane's row: norm, running |Q_i|^2 and kernel entry
+    float qi = 0.f, qo = 0.f, kd = 0.f;
+    if (mine) {
+        if (X.mode == IRWLS_K_NORM_RBF) qi = X.q[row];
+        if (qn) qo = qn[row];
+        float part[32];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            ir[r] = i + r * stride;
-            const bool ok = ir[r] < l;
-            pb[r] = pe[r] = 0;
-            qi[r] = qo[r] = 0.f;
-            if (ok && !raw) {
-                pb[r] = X.rp[ir[r]];
-                pe[r] = X.rp[ir[r] + 1];
-            }
-            if (ok && X.mode == IRWLS_K_NORM_RBF) qi[r] = X.q[ir[r]];
-            if (ok && qn) qo[r] = qn[ir[r]];
-            acc[r] = kd[r] = 0.f;
+        for (int k = 0; k < 32; ++k) part[k] = 0.f;
+        if (raw) {
+            const float *b = X.X + (size_t)row * X.ld;
+            for (int t0 = 0; t0 < X.width; t0 += 32)
+#pragma unroll
+                for (int k = 0; k < 32; ++k)
+                    if (t0 + k < X.width) {
+                        const float d = sc[t0 + k] - b[t0 + k];
+                        part[k] = fmaf(d, d, part[k]);
+                    }
+        } else {
+            const int pb = X.rp[row], pe = X.rp[row + 1];
+            for (int p0 = pb; p0 < pe; p0 += 32)
+#pragma unroll
+                for (int k = 0; k < 32; ++k)
+                    if (p0 + k < pe) part[k] = fmaf(X.cv[p0 + k], sc[X.ci[p0 + k]], part[k]);
         }
-        // Q_i . l2: each lane's float4s in increasing order
+        kd = butterfly_sum32(part);
+    }
+    // Q_i . l2 of the warp's rows, R at a time; lane r keeps row r's sum
+    float dot = 0.f;
+    const int nr = min(32, l - r0);
+    for (int g = 0; g < nr; g += R) {
+        float acc[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = 0.f;
         for (int j4 = lane; j4 < n4; j4 += 32) {
             float4 qv[R];
 #pragma unroll
             for (int r = 0; r < R; ++r)
-                qv[r] = ir[r] < l ? ((const float4 *)(Qf + (size_t)ir[r] * ldq))[j4] : make_float4(0.f, 0.f, 0.f, 0.f);
+                qv[r] = g + r < nr ? ((const float4 *)(Qf + (size_t)(r0 + g + r) * ldq))[j4]
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
             const float4 lv = *(const float4 *)(l2 + 4 * j4);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -962,74 +997,25 @@ __global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const in
                 acc[r] = fmaf(qv[r].w, lv.w, acc[r]);
             }
         }
-        // each lane's first entry of the R rows' kernel entries, loaded
-        // together (one memory latency for the R rows, not one each)
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            ev[r] = 0.f;
-            ec[r] = 0;
-            if (ir[r] < l) {
-                if (raw) {
-                    if (lane < X.width) ev[r] = X.X[(size_t)ir[r] * X.ld + lane];
-                } else if (pb[r] + lane < pe[r]) {
-                    ev[r] = X.cv[pb[r] + lane];
-                    ec[r] = X.ci[pb[r] + lane];
-                }
-            }
-        }
-        // kernel entry against the new centroid, each lane's entries in
-        // increasing order
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            if (ir[r] >= l) continue;
-            if (raw) {
-                if (lane < X.width) {
-                    const float d = sc[lane] - ev[r];
-                    kd[r] = fmaf(d, d, kd[r]);
-                }
-                const float *b = X.X + (size_t)ir[r] * X.ld;
-                for (int t = lane + 32; t < X.width; t += 32) {
-                    const float d = sc[t] - b[t];
-                    kd[r] = fmaf(d, d, kd[r]);
-                }
-            } else {
-                if (pb[r] + lane < pe[r]) kd[r] = fmaf(ev[r], sc[ec[r]], kd[r]);
-                for (int p = pb[r] + lane + 32; p < pe[r]; p += 32) kd[r] = fmaf(X.cv[p], sc[X.ci[p]], kd[r]);
-            }
-        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-                acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
-                kd[r] += __shfl_xor_sync(0xffffffffu, kd[r], o);
-            }
-        // lane r finishes row r
-        if (lane < R) {
-            int row = ir[0];
-            float a = acc[0], k = kd[0], qb = qi[0], q0 = qo[0];
+            for (int r = 0; r < R; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
 #pragma unroll
-            for (int r = 1; r < R; ++r)
-                if (lane == r) {
-                    row = ir[r];
-                    a = acc[r];
-                    k = kd[r];
-                    qb = qi[r];
-                    q0 = qo[r];
-                }
-            if (row < l) {
-                float kv;
-                if (raw) kv = __expf(X.ng * k);
-                else if (X.mode == IRWLS_K_LINEAR) kv = k;
-                else kv = __expf(X.ng * fmaxf(qa + qb - 2.f * k, 0.f));
-                const float q = (kv - a) * inv_l3;
-                Qf[(size_t)row * ldq + s] = q;
-                if (qn) qn[row] = fmaf(q, q, q0);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
-                const __nv_bfloat16 h = __float2bfloat16_rn(q);
-                Qb[qb_index(row, s, ldq >> 5, 0)] = h;
-                Qb[qb_index(row, s, ldq >> 5, 1)] = __float2bfloat16_rn(q - __bfloat162float(h));
-            }
-        }
+        for (int r = 0; r < R; ++r)
+            if (lane == g + r) dot = acc[r];
+    }
+    if (mine) {
+        float kv;
+        if (raw) kv = __expf(X.ng * kd);
+        else if (X.mode == IRWLS_K_LINEAR) kv = kd;
+        else kv = __expf(X.ng * fmaxf(qa + qi - 2.f * kd, 0.f));
+        const float q = (kv - dot) * inv_l3;
+        Qf[(size_t)row * ldq + s] = q;
+        if (qn) qn[row] = fmaf(q, q, qo);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
+        const __nv_bfloat16 h = __float2bfloat16_rn(q);
+        Qb[qb_index(row, s, ldq >> 5, 0)] = h;
+        Qb[qb_index(row, s, ldq >> 5, 1)] = __float2bfloat16_rn(q - __bfloat162float(h));
     }
 }
 
@@ -1142,7 +1128,7 @@ extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, cons
     }
     const size_t smem = ((size_t)s4 + X->ld) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int blocks = std::min(ceil_div(l, 32), 4 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148));  // one wave
+    const int blocks = ceil_div(l, 256);  // 32 rows per warp
     q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
                                                             (__nv_bfloat16 *)Qb, ldq, d_qn);
     IRWLS_LAUNCH_CHECK("q_column");
