@@ -214,8 +214,9 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
 }
 
 // Per candidate c: w_e = sum of the chunks of row e in chunk order, W (FP64),
-// eta = 1 - |w|^2 (fixed-order block reduction), and w as bf16 hi/lo of its
-// FP32 rounding in the blocked layout (zero up to the padded width kpad).
+// eta = 1 - |w|^2 (fixed-order block reduction), and w as the bf16 hi/mid/lo
+// pieces of its FP32 rounding in the blocked layout (zero up to the padded
+// width kpad).
 __global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict__ part, int ldp, int s,
                                                        double *__restrict__ W, int ldz, __nv_bfloat16 *Wb, int kpad,
                                                        double *__restrict__ eta) {
@@ -232,9 +233,10 @@ __global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict_
             ss = fma(w, w, ss);
             xf = (float)w;
         }
-        const __nv_bfloat16 h = __float2bfloat16_rn(xf);
-        Wb[wb_index(c, e, 0)] = h;
-        Wb[wb_index(c, e, 1)] = __float2bfloat16_rn(xf - __bfloat162float(h));
+        __nv_bfloat16 pc[3];
+        bf16_pieces3(xf, pc);
+#pragma unroll
+        for (int k = 0; k < QB_NP; ++k) Wb[wb_index(c, e, k)] = pc[k];
     }
     red[threadIdx.x] = ss;
     __syncthreads();

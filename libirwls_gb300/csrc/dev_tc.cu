@@ -463,9 +463,14 @@ extern "C" int irwls_tc_status(void) {
 // K_nm z = Q w, eta = 1 - |w|^2, and the residual is r = Q w - k(c, .). Q and
 // w are bounded, which is what makes the split-BF16 product accurate here
 // (the reference's K_nm z form multiplies K_nm by z = K_CC^-1 k_C, whose
-// entries are large and cancel). Q is kept in FP32 (master copy) and as bf16
-// hi/lo for the tensor cores; a new centroid adds the column
-// q_s = (k(., c_s) - Q l2) / L3 with l2 = L^-1 k_C(c_s), L3 the new pivot.
+// entries are large and cancel). Q is kept as three bf16 pieces per value
+// (exactly its FP32 value), and the tensor cores take the six piece products
+// down to 2^-24 of each term, so Q w has the accuracy of an FP32 dot
+// product. A new centroid c_s adds the column
+//   q_s = (k(., c_s) - Q l2) / L3,  l2 = L^-1 k_C(c_s) = w(c_s), L3 the pivot,
+// which is minus the step's residual of the winning candidate over L3: the
+// score kernel stores the 64 residuals of every row, and the column is read
+// from them instead of from another pass over Q.
 // ===========================================================================
 
 namespace {
@@ -736,8 +741,9 @@ __device__ __forceinline__ void warp_sum32_transposed(float v[32], int lane) {
 template <int NS, int EG>
 __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     KViewF X, int l, const int *__restrict__ cand, const __nv_bfloat16 *__restrict__ Qb, int kbn,
-    const __nv_bfloat16 *__restrict__ Wb, int kst, float *__restrict__ part, int xs_bytes, int *flags) {
-    using S = TcRing<64, 2, WS_BK>;
+    const __nv_bfloat16 *__restrict__ Wb, int kst, float *__restrict__ part, float *__restrict__ resid, int xs_bytes,
+    int *flags) {
+    using S = TcRing<64, QB_NP, WS_BK>;
     static_assert(S::A_BYTES == 2 * QB_PIECE && S::B_BYTES == 2 * WB_PIECE, "blocked pieces are stage images");
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ __align__(8) uint64_t full[NS], empty[NS], accf[2], acce[2], done;
@@ -799,8 +805,8 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
                     const uint32_t sb = base + slot * S::BYTES, fb = smem_u32(&full[slot]);
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb),
                                  "r"((uint32_t)S::BYTES));
-                    bulk_g2s(sb, Qb + (tile * kbn + k) * (2 * QB_PIECE), 2 * S::A_BYTES, fb);
-                    bulk_g2s(sb + 2 * S::A_BYTES, Wb + (size_t)k * (2 * WB_PIECE), 2 * S::B_BYTES, fb);
+                    bulk_g2s(sb, Qb + (tile * kbn + k) * (QB_NP * QB_PIECE), QB_NP * S::A_BYTES, fb);
+                    bulk_g2s(sb + QB_NP * S::A_BYTES, Wb + (size_t)k * (QB_NP * WB_PIECE), QB_NP * S::B_BYTES, fb);
                     issued = u + 1;
                 }
             }
@@ -823,7 +829,7 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
                     }
                     asm volatile("fence.proxy.async.shared::cta;\n" ::);
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-                    ring_mma<64, 2, WS_BK>(smem + slot * S::BYTES, tmem + b * 64, k == 0);
+                    ring_mma<64, QB_NP, WS_BK>(smem + slot * S::BYTES, tmem + b * 64, k == 0);
                     tc_commit(&empty[slot]);
                 }
                 if (!abort_flag) tc_commit(&accf[b]);
@@ -876,10 +882,16 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
                 float acc[32];
                 tc_ld32_lanes(tmem + b * 64, 32 * ew, CPG * g, acc);
 #pragma unroll
-                for (int jj = 0; jj < 32; ++jj) {
-                    const float rr = __fsub_rn(acc[jj], v[jj]);
-                    v[jj] = row < l ? __fmul_rn(rr, rr) : 0.f;
+                for (int jj = 0; jj < 32; ++jj) acc[jj] = __fsub_rn(acc[jj], v[jj]);
+                if (row < l) {
+                    // the residuals, from which the winner's column of Q is taken
+                    float4 *o = (float4 *)(resid + (size_t)row * 64 + CPG * g);
+#pragma unroll
+                    for (int q4 = 0; q4 < 8; ++q4)
+                        o[q4] = make_float4(acc[4 * q4], acc[4 * q4 + 1], acc[4 * q4 + 2], acc[4 * q4 + 3]);
                 }
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) v[jj] = row < l ? __fmul_rn(acc[jj], acc[jj]) : 0.f;
                 warp_sum32_transposed(v, lane);
                 wred[4 * g + ew][lane] = v[0];
             }
@@ -904,121 +916,61 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
 }
 
-// The sum over a warp's lanes that a butterfly of shuffles (xor 16, 8, 4, 2,
-// 1; each lane adding its partner's value to its own) leaves in every lane,
-// formed by one thread from the 32 lane values: the same pairs at every
-// level, so the same bits.
-__device__ __forceinline__ float butterfly_sum32(float v[32]) {
+// Q's column s written as its three pieces, and |Q_i|^2 updated.
+__device__ __forceinline__ void put_q(int row, int s, float q, __nv_bfloat16 *Qb, int ldq, float *qn) {
+    if (qn) qn[row] = fmaf(q, q, qn[row]);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
+    __nv_bfloat16 pc[3];
+    bf16_pieces3(q, pc);
 #pragma unroll
-    for (int h = 16; h >= 1; h >>= 1)
-#pragma unroll
-        for (int i = 0; i < h; ++i) v[i] = v[i] + v[i + h];
-    return v[0];
+    for (int k = 0; k < QB_NP; ++k) Qb[qb_index(row, s, ldq >> 5, k)] = pc[k];
 }
 
-// New column s of Q: q_i = (k(x_i, c_s) - sum_{j<s} Q_ij l2_j) / L3. lrow
-// holds l2 (s floats) then 1 / L3, written by the factor step. A warp takes
-// 32 consecutive rows, lane r finishing row r:
-// - the kernel entry of each row against the new centroid in the lane that
-//   owns it: the entries a lane of a warp-split loop would take (p = lane,
-//   lane + 32, ...) summed in that order into 32 partials, then combined in
-//   the butterfly's order, so the value is that of the warp-split form (all
-//   of a lane's loads are independent: one memory latency per 32 rows);
-// - the dot Q_i . l2 warp-split, eight rows at a time (their float4 loads
-//   issued together), each lane's float4s in increasing order over the
-//   row's first s columns rounded up to 4 (Q's columns >= s are still zero),
-//   then the butterfly.
-__global__ void __launch_bounds__(256) q_column_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
-                                                       const float *__restrict__ lrow, float *Qf, __nv_bfloat16 *Qb,
-                                                       int ldq, float *__restrict__ qn) {
-    constexpr int R = 8;  // rows of a dot-product pass
+// Column s of Q from the score step's residuals r = Q w - k of the winning
+// candidate (slot best[0]): q_i = -r_i / L3. lrow[s] holds 1 / L3.
+__global__ void q_column_resid_kernel(int l, const float *__restrict__ resid, const int *__restrict__ best, int s,
+                                      const float *__restrict__ lrow, __nv_bfloat16 *Qb, int ldq,
+                                      float *__restrict__ qn) {
+    const int c = best[0];
+    const float inv_l3 = lrow[s];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l; i += gridDim.x * blockDim.x)
+        put_q(i, s, -resid[(size_t)i * 64 + c] * inv_l3, Qb, ldq, qn);
+}
+
+// Column s of Q directly, q_i = (k(x_i, c_s) - sum_{t<s} Q_it l2_t) / L3,
+// one row per thread (Q from its pieces). Used for the first columns (the
+// class-mean centroids), which no score step precedes. lrow holds l2 (s
+// floats) then 1 / L3.
+__global__ void __launch_bounds__(256) q_column_direct_kernel(KViewF X, int l, const int *__restrict__ cent, int s,
+                                                              const float *__restrict__ lrow, __nv_bfloat16 *Qb,
+                                                              int ldq, float *__restrict__ qn) {
     extern __shared__ float qsm[];
-    const int s4 = (s + 127) / 128 * 128;  // <= ldq
-    float *l2 = qsm;                       // s4 floats, zero past s
-    float *sc = qsm + s4;                  // centroid row, X.ld floats
+    float *sc = qsm;  // centroid row, X.ld floats
     const int gc = cent[s];
-    for (int t = threadIdx.x; t < s4; t += blockDim.x) l2[t] = t < s ? lrow[t] : 0.f;
     for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sc[t] = X.X[(size_t)gc * X.ld + t];
     __syncthreads();
     const float inv_l3 = lrow[s];
     const float qa = X.q[gc];
-    const int lane = threadIdx.x & 31;
-    const int n4 = (s + 3) / 4;  // float4s of a row that can be nonzero
-    const bool raw = X.mode == IRWLS_K_RAW_RBF;
-    const int r0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
-    if (r0 >= l) return;
-    const int row = r0 + lane;
-    const bool mine = row < l;
-    // this lane's row: norm, running |Q_i|^2 and kernel entry
-    float qi = 0.f, qo = 0.f, kd = 0.f;
-    if (mine) {
-        if (X.mode == IRWLS_K_NORM_RBF) qi = X.q[row];
-        if (qn) qo = qn[row];
-        float part[32];
-#pragma unroll
-        for (int k = 0; k < 32; ++k) part[k] = 0.f;
-        if (raw) {
-            const float *b = X.X + (size_t)row * X.ld;
-            for (int t0 = 0; t0 < X.width; t0 += 32)
-#pragma unroll
-                for (int k = 0; k < 32; ++k)
-                    if (t0 + k < X.width) {
-                        const float d = sc[t0 + k] - b[t0 + k];
-                        part[k] = fmaf(d, d, part[k]);
-                    }
-        } else {
-            const int pb = X.rp[row], pe = X.rp[row + 1];
-            for (int p0 = pb; p0 < pe; p0 += 32)
-#pragma unroll
-                for (int k = 0; k < 32; ++k)
-                    if (p0 + k < pe) part[k] = fmaf(X.cv[p0 + k], sc[X.ci[p0 + k]], part[k]);
-        }
-        kd = butterfly_sum32(part);
-    }
-    // Q_i . l2 of the warp's rows, R at a time; lane r keeps row r's sum
-    float dot = 0.f;
-    const int nr = min(32, l - r0);
-    for (int g = 0; g < nr; g += R) {
-        float acc[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) acc[r] = 0.f;
-        for (int j4 = lane; j4 < n4; j4 += 32) {
-            float4 qv[R];
-#pragma unroll
-            for (int r = 0; r < R; ++r)
-                qv[r] = g + r < nr ? ((const float4 *)(Qf + (size_t)(r0 + g + r) * ldq))[j4]
-                                   : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 lv = *(const float4 *)(l2 + 4 * j4);
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                acc[r] = fmaf(qv[r].x, lv.x, acc[r]);
-                acc[r] = fmaf(qv[r].y, lv.y, acc[r]);
-                acc[r] = fmaf(qv[r].z, lv.z, acc[r]);
-                acc[r] = fmaf(qv[r].w, lv.w, acc[r]);
+    const int kbn = ldq >> 5;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l; i += gridDim.x * blockDim.x) {
+        float dot = 0.f;
+        for (int t = 0; t < s; ++t)
+            dot = fmaf(bf16_join3(Qb[qb_index(i, t, kbn, 0)], Qb[qb_index(i, t, kbn, 1)], Qb[qb_index(i, t, kbn, 2)]),
+                       lrow[t], dot);
+        float kd = 0.f, kv;
+        if (X.mode == IRWLS_K_RAW_RBF) {
+            const float *b = X.X + (size_t)i * X.ld;
+            for (int t = 0; t < X.width; ++t) {
+                const float d = sc[t] - b[t];
+                kd = fmaf(d, d, kd);
             }
+            kv = __expf(X.ng * kd);
+        } else {
+            for (int p = X.rp[i]; p < X.rp[i + 1]; ++p) kd = fmaf(X.cv[p], sc[X.ci[p]], kd);
+            kv = X.mode == IRWLS_K_LINEAR ? kd : __expf(X.ng * fmaxf(qa + X.q[i] - 2.f * kd, 0.f));
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-            for (int r = 0; r < R; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-            if (lane == g + r) dot = acc[r];
-    }
-    if (mine) {
-        float kv;
-        if (raw) kv = __expf(X.ng * kd);
-        else if (X.mode == IRWLS_K_LINEAR) kv = kd;
-        else kv = __expf(X.ng * fmaxf(qa + qi - 2.f * kd, 0.f));
-        const float q = (kv - dot) * inv_l3;
-        Qf[(size_t)row * ldq + s] = q;
-        if (qn) qn[row] = fmaf(q, q, qo);  // |Q_i|^2: the Nystrom residual of row i is k_ii - qn[i]
-        const __nv_bfloat16 h = __float2bfloat16_rn(q);
-        Qb[qb_index(row, s, ldq >> 5, 0)] = h;
-        Qb[qb_index(row, s, ldq >> 5, 1)] = __float2bfloat16_rn(q - __bfloat162float(h));
+        put_q(i, s, (kv - dot) * inv_l3, Qb, ldq, qn);
     }
 }
-
 
 }  // namespace
 
@@ -1069,7 +1021,7 @@ extern "C" void irwls_f32_mirror_free(void *h) {
 }
 
 extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qb,
-                                   int ldq, const void *Wb, int s, float *d_part) {
+                                   int ldq, const void *Wb, int s, float *d_part, float *d_resid) {
     constexpr size_t LIMIT = 220 * 1024, XS = 24 * 1024;  // XS: one of the two row-staging buffers
     const int kst = (s + WS_BK - 1) / WS_BK;
     if (kst * WS_BK > ldq || ldq % WS_BK) {
@@ -1077,7 +1029,7 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
         return -12;
     }
     const size_t fixed = 1024 + (size_t)CAT_LD * X->ld * sizeof(float);
-    const size_t stage = TcRing<64, 2, WS_BK>::BYTES;
+    const size_t stage = TcRing<64, QB_NP, WS_BK>::BYTES;
     if (fixed + 2 * stage > LIMIT) {
         irwls_set_error(-12, "feature width %d too wide for the precision-form SGMA tile", X->width);
         return -12;
@@ -1094,7 +1046,7 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
     auto launch = [&](auto kern) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<grid, 128 + 128 * WS_EG, smem, irwls_stream()>>>(kv, l, d_cand, qb, ldq / 32, wb, kst, d_part,
-                                                                (int)xs, irwls_dev_flags());
+                                                                d_resid, (int)xs, irwls_dev_flags());
     };
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
     switch (ns) {
@@ -1119,19 +1071,34 @@ extern "C" int irwls_sgma_tc_select(const float *d_part, int nblk, const double 
 }
 
 // lrow: row s of L in FP32 (s values, then 1 / L3), from irwls_sgma_linv_update.
+// The direct form (the first columns, s small).
 extern "C" int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s,
-                              const float *lrow, float *Qf, void *Qb, int ldq, float *d_qn) {
-    const int s4 = (s + 127) / 128 * 128;
-    if (s4 > ldq) {
-        irwls_set_error(-12, "Q leading dimension %d below the padded order %d", ldq, s4);
+                              const float *lrow, void *Qb, int ldq, float *d_qn) {
+    if (s >= ldq) {
+        irwls_set_error(-12, "Q leading dimension %d below the order %d", ldq, s + 1);
         return -12;
     }
-    const size_t smem = ((size_t)s4 + X->ld) * sizeof(float);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(q_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int blocks = ceil_div(l, 256);  // 32 rows per warp
-    q_column_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow, Qf,
-                                                            (__nv_bfloat16 *)Qb, ldq, d_qn);
-    IRWLS_LAUNCH_CHECK("q_column");
+    const size_t smem = (size_t)X->ld * sizeof(float);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(q_column_direct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int blocks = std::max(1, std::min(ceil_div(l, 256), 4 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148)));
+    q_column_direct_kernel<<<blocks, 256, smem, irwls_stream()>>>(kviewf(X, (const F32Mirror *)F), l, d_cent, s, lrow,
+                                                                   (__nv_bfloat16 *)Qb, ldq, d_qn);
+    IRWLS_LAUNCH_CHECK("q_column_direct");
+    return 0;
+}
+
+// Column s from the residuals of the score step that chose centroid s.
+extern "C" int irwls_q_column_resid(int l, const float *d_resid, const int *d_best, int s, const float *lrow, void *Qb,
+                                    int ldq, float *d_qn) {
+    if (s >= ldq) {
+        irwls_set_error(-12, "Q leading dimension %d below the order %d", ldq, s + 1);
+        return -12;
+    }
+    const int blocks = std::max(1, std::min(ceil_div(l, 256), 4 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148)));
+    q_column_resid_kernel<<<blocks, 256, 0, irwls_stream()>>>(l, d_resid, d_best, s, lrow, (__nv_bfloat16 *)Qb, ldq,
+                                                              d_qn);
+    IRWLS_LAUNCH_CHECK("q_column_resid");
     return 0;
 }
 

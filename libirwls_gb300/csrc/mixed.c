@@ -37,12 +37,16 @@ int irwls_sgma_tc_select(const float *d_part, int nblk, const double *d_eta, con
                          int *d_best, double *d_bestval, float *d_scores);
 int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const int *d_best, const double *d_W, int ldz,
                       double *d_L, int ldL);
-/* Qb, Wb: the blocked bf16 hi/lo layout of Q and W (blocked_bf16.cuh) */
+/* Qb, Wb: the blocked bf16 hi/mid/lo layout of Q and W (blocked_bf16.cuh);
+   d_rq: the residuals r = Q w - k of every row against the step's 64
+   candidates (rows x 64) */
 int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qb, int ldq,
-                        const void *Wb, int s, float *d_part);
+                        const void *Wb, int s, float *d_part, float *d_rq);
 int irwls_sgma_tc_partials(int l);
-int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const float *lrow, float *Qf,
-                   void *Qb, int ldq, float *d_qn);
+int irwls_q_column(const irwls_dev_set *X, const void *F, int l, const int *d_cent, int s, const float *lrow, void *Qb,
+                   int ldq, float *d_qn);
+int irwls_q_column_resid(int l, const float *d_rq, const int *d_best, int s, const float *lrow, void *Qb, int ldq,
+                         float *d_qn);
 void *irwls_f32_mirror(const irwls_dev_set *X);
 void irwls_f32_mirror_free(void *h);
 void irwls_f32_mirror_view(const void *h, const float **X, const float **q);
@@ -107,7 +111,7 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     double *d_L = NULL, *d_W = NULL, *d_KN = NULL, *d_eta = NULL, *d_val = NULL, *d_Linv = NULL, *d_wpart = NULL,
            *d_lpart = NULL;
     float *d_part = NULL;
-    float *Qf = NULL, *lrow = NULL, *d_qn = NULL, *d_F = NULL, *d_pred = NULL, *d_tfeat = NULL, *d_tscore = NULL;
+    float *d_rq = NULL, *lrow = NULL, *d_qn = NULL, *d_F = NULL, *d_pred = NULL, *d_tfeat = NULL, *d_tscore = NULL;
     int *d_probe = NULL, *d_pool = NULL;
     double *d_resid = NULL;
     void *Qb = NULL, *Wb = NULL;
@@ -129,10 +133,10 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
     rc |= irwls_dev_malloc((void **)&d_eta, 64 * sizeof(double));
     rc |= irwls_dev_malloc((void **)&d_part, (size_t)nblk * 64 * sizeof(float));
     rc |= irwls_dev_malloc((void **)&d_val, (size_t)m * sizeof(double));
-    rc |= irwls_dev_malloc((void **)&Qf, (size_t)l * ldq * sizeof(float));
-    const size_t qb_bytes = (size_t)nblk * 128 * ldq * 4; /* whole 128-row tiles, hi + lo */
+    rc |= irwls_dev_malloc((void **)&d_rq, (size_t)l * 64 * sizeof(float));
+    const size_t qb_bytes = (size_t)nblk * 128 * ldq * 6; /* whole 128-row tiles, three pieces */
     rc |= irwls_dev_malloc(&Qb, qb_bytes);
-    rc |= irwls_dev_malloc(&Wb, (size_t)64 * ldq * 4);
+    rc |= irwls_dev_malloc(&Wb, (size_t)64 * ldq * 6);
     rc |= irwls_dev_malloc((void **)&lrow, (size_t)(m + 1) * sizeof(float));
     rc |= irwls_dev_malloc((void **)&d_Linv, (size_t)m * ldL * sizeof(double));
     rc |= irwls_dev_malloc((void **)&d_wpart, irwls_sgma_wpart_count(m) * sizeof(double));
@@ -159,7 +163,6 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
         rc |= irwls_dev_memset(d_L, 0, (size_t)m * ldL * sizeof(double));
         rc |= irwls_dev_memset(d_Linv, 0, (size_t)m * ldL * sizeof(double));
         rc |= irwls_dev_memset(d_W, 0, (size_t)64 * ldz * sizeof(double));
-        rc |= irwls_dev_memset(Qf, 0, (size_t)l * ldq * sizeof(float));
         rc |= irwls_dev_memset(Qb, 0, qb_bytes);
         rc |= irwls_dev_memset(d_qn, 0, (size_t)(l + 2) * sizeof(float));
         if (learn || trace) {
@@ -184,7 +187,7 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
         for (int s = 0; s < 2 && s < m && !rc; s++) {
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
             rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
-            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qb, ldq, d_qn);
+            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qb, ldq, d_qn);
         }
         const float *X32 = NULL, *q32 = NULL;
         irwls_f32_mirror_view(F, &X32, &q32);
@@ -203,13 +206,13 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
                 rc |= irwls_learn_features(X32, X->ld, X->width, raw, q32, (float)X->neg_gamma, X->y, cs, NCAND,
                                            d_probe, NPROBE, d_qn, d_tfeat + (size_t)(s - 2) * NCAND * nf);
             rc |= irwls_sgma_cand_inv(X, cs, d_cent, s, d_Linv, ldL, d_KN, ldz, d_wpart, m, d_W, Wb, ldq, d_eta);
-            rc |= irwls_sgma_tc_score(X, F, l, cs, Qb, ldq, Wb, s, d_part);
+            rc |= irwls_sgma_tc_score(X, F, l, cs, Qb, ldq, Wb, s, d_part, d_rq);
             irwls_prof_begin(IRWLS_PROF_SGMA_UPDATE);
             rc |= irwls_sgma_tc_select(d_part, nblk, d_eta, cs, s, d_cent, d_best, d_val,
                                        trace ? d_tscore + (size_t)(s - 2) * NCAND : NULL);
             rc |= irwls_sgma_factor(X, s, d_cent, d_best, d_W, ldz, d_L, ldL);
             rc |= irwls_sgma_linv_update(d_L, ldL, d_Linv, ldL, s, d_lpart, lrow);
-            rc |= irwls_q_column(X, F, l, d_cent, s, lrow, Qf, Qb, ldq, d_qn);
+            rc |= irwls_q_column_resid(l, d_rq, d_best, s, lrow, Qb, ldq, d_qn);
             irwls_prof_end(IRWLS_PROF_SGMA_UPDATE);
         }
         /* Nystrom residual trace(K - K_nm K_mm^-1 K_mn) = sum_i (k_ii - |Q_i|^2) */
@@ -244,7 +247,7 @@ int irwls_sgma_mixed_dev(const irwls_dev_set *X, const svm_dataset *ds, properti
 done:
     free(cand);
     {
-        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, Qf, Qb, Wb, lrow,
+        void *bufs[] = {d_cand, d_cent, d_best, d_L, d_W, d_KN, d_eta, d_part, d_val, d_rq, Qb, Wb, lrow,
                         d_Linv, d_wpart, d_lpart, d_qn, d_resid, d_probe, d_F, d_pool, d_pred, d_tfeat, d_tscore};
         for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++) irwls_dev_free(bufs[k]);
         irwls_f32_mirror_free(F);
