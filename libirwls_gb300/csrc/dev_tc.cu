@@ -884,11 +884,10 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) acc[jj] = __fsub_rn(acc[jj], v[jj]);
                 if (row < l) {
-                    // the residuals, from which the winner's column of Q is taken
-                    float4 *o = (float4 *)(resid + (size_t)row * 64 + CPG * g);
+                    // the residuals, from which the winner's column of Q is
+                    // taken, candidate-major (a warp's stores are 128-byte lines)
 #pragma unroll
-                    for (int q4 = 0; q4 < 8; ++q4)
-                        o[q4] = make_float4(acc[4 * q4], acc[4 * q4 + 1], acc[4 * q4 + 2], acc[4 * q4 + 3]);
+                    for (int jj = 0; jj < 32; ++jj) resid[(size_t)(CPG * g + jj) * l + row] = acc[jj];
                 }
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) v[jj] = row < l ? __fmul_rn(acc[jj], acc[jj]) : 0.f;
@@ -926,14 +925,15 @@ __device__ __forceinline__ void put_q(int row, int s, float q, __nv_bfloat16 *Qb
 }
 
 // Column s of Q from the score step's residuals r = Q w - k of the winning
-// candidate (slot best[0]): q_i = -r_i / L3. lrow[s] holds 1 / L3.
+// candidate (slot best[0]; the residuals of candidate c at resid + c * l):
+// q_i = -r_i / L3. lrow[s] holds 1 / L3.
 __global__ void q_column_resid_kernel(int l, const float *__restrict__ resid, const int *__restrict__ best, int s,
                                       const float *__restrict__ lrow, __nv_bfloat16 *Qb, int ldq,
                                       float *__restrict__ qn) {
     const int c = best[0];
     const float inv_l3 = lrow[s];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l; i += gridDim.x * blockDim.x)
-        put_q(i, s, -resid[(size_t)i * 64 + c] * inv_l3, Qb, ldq, qn);
+        put_q(i, s, -resid[(size_t)c * l + i] * inv_l3, Qb, ldq, qn);
 }
 
 // Column s of Q directly, q_i = (k(x_i, c_s) - sum_{t<s} Q_it l2_t) / L3,

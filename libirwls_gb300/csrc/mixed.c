@@ -39,7 +39,7 @@ int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cent, const in
                       double *d_L, int ldL);
 /* Qb, Wb: the blocked bf16 hi/mid/lo layout of Q and W (blocked_bf16.cuh);
    d_rq: the residuals r = Q w - k of every row against the step's 64
-   candidates (rows x 64) */
+   candidates (64 x rows, candidate-major) */
 int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qb, int ldq,
                         const void *Wb, int s, float *d_part, float *d_rq);
 int irwls_sgma_tc_partials(int l);
