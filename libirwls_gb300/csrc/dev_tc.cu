@@ -736,6 +736,32 @@ __device__ __forceinline__ void warp_sum32_transposed(float v[32], int lane) {
     }
 }
 
+// Tensor-memory columns of one score accumulator: three 64-column sums
+// S0 = sum Qhi Whi, S1 = sum (Qhi Wmid + Qmid Whi), S2 = sum (Qhi Wlo + Qmid
+// Wmid + Qlo Whi), so that the small terms are not rounded against the large
+// ones; Q w = S0 + (S1 + S2).
+constexpr int SC_COLS = 192;
+
+// The MMAs of one score stage (one thread): per 16-wide K step, Qhi against
+// the W pieces hi, mid, lo stacked along N (N = 192, into S0 S1 S2), Qmid
+// against hi, mid (N = 128, into S1 S2) and Qlo against hi (N = 64, into S2):
+// three MMAs for the six products, each A piece read once.
+__device__ __forceinline__ void score_mma_stage(unsigned char *sb, uint32_t tmem, bool first) {
+    using S = TcRing<64, QB_NP, WS_BK>;
+    const uint32_t base = smem_u32(sb), wbase = base + QB_NP * S::A_BYTES;
+#pragma unroll
+    for (int kk = 0; kk < WS_BK / 16; ++kk) {
+        const uint32_t off = kk * 256;
+        const uint64_t w = tc_desc_sbo(wbase + off, S::SBO);
+#pragma unroll
+        for (int i = 0; i < QB_NP; ++i) {
+            const uint32_t idesc = tc_idesc(TC_BM, 64 * (QB_NP - i));
+            mma_bf16(tmem + 64 * i, tc_desc_sbo(base + i * S::A_BYTES + off, S::SBO), w, idesc,
+                     first && kk == 0 && i == 0 ? 0u : 1u);
+        }
+    }
+}
+
 // EG epilogue groups of four warps (warps 4 ... 4 EG + 3), each scoring 64 / EG
 // of the candidates for all 128 rows of a tile.
 template <int NS, int EG>
@@ -782,7 +808,7 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     if (threadIdx.x < 64) qc[threadIdx.x] = X.q[cand[threadIdx.x]];
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(128));
+                     "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -829,7 +855,7 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
                     }
                     asm volatile("fence.proxy.async.shared::cta;\n" ::);
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-                    ring_mma<64, QB_NP, WS_BK>(smem + slot * S::BYTES, tmem + b * 64, k == 0);
+                    score_mma_stage(smem + slot * S::BYTES, tmem + b * SC_COLS, k == 0);
                     tc_commit(&empty[slot]);
                 }
                 if (!abort_flag) tc_commit(&accf[b]);
@@ -875,12 +901,27 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
             const TileRows Tn = j + 1 < my_tiles ? stage(j + 1) : T;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
             {
-                // this row's kernel values against the group's 32 candidates,
-                // then r^2 per candidate summed over the warp's 32 rows
-                float v[32];
+                // this row's kernel values against the group's 32 candidates
+                float v[32], acc[32];
                 if (row < l) kentry32_tile(X, T, cat + CPG * g, qc + CPG * g, r, row, v);
-                float acc[32];
-                tc_ld32_lanes(tmem + b * 64, 32 * ew, CPG * g, acc);
+                // Q w: the three accumulators (terms of order 1, 2^-8 and
+                // 2^-16) added smallest first, eight candidates at a time
+                const uint32_t tb = tmem + b * SC_COLS;
+#pragma unroll
+                for (int c8 = 0; c8 < 32; c8 += 8) {
+                    float s1[8], s2[8];
+                    tc_ld8_lanes(tb + 128, 32 * ew, CPG * g + c8, s2);
+                    tc_ld8_lanes(tb + 64, 32 * ew, CPG * g + c8, s1);
+#pragma unroll
+                    for (int jj = 0; jj < 8; ++jj) s2[jj] = __fadd_rn(s1[jj], s2[jj]);
+                    tc_ld8_lanes(tb, 32 * ew, CPG * g + c8, s1);
+#pragma unroll
+                    for (int jj = 0; jj < 8; ++jj) acc[c8 + jj] = __fadd_rn(s1[jj], s2[jj]);
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+                if (lane == 0) mbar_arrive(&acce[b]);  // this warp's reads of accumulator b are done
+                // residuals r = Q w - k, then r^2 per candidate summed over the
+                // warp's 32 rows
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) acc[jj] = __fsub_rn(acc[jj], v[jj]);
                 if (row < l) {
@@ -894,8 +935,6 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
                 warp_sum32_transposed(v, lane);
                 wred[4 * g + ew][lane] = v[0];
             }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
-            if (lane == 0) mbar_arrive(&acce[b]);  // this warp's reads of accumulator b are done
             asm volatile("bar.sync 1, %0;\n" ::"r"(EPI));
             if (et < 64) {
                 // the candidate's four row-quarter sums, in a fixed order
@@ -912,7 +951,7 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     // after the barrier: every role has finished, so a timeout any of them
     // met is in abort_flag
     if (threadIdx.x == 0 && abort_flag) atomicExch(flags + 1, 1);
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512));
 }
 
 // Q's column s written as its three pieces, and |Q_i|^2 updated.
@@ -1022,22 +1061,56 @@ extern "C" void irwls_f32_mirror_free(void *h) {
 
 extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l, const int *d_cand, const void *Qb,
                                    int ldq, const void *Wb, int s, float *d_part, float *d_resid) {
-    constexpr size_t LIMIT = 220 * 1024, XS = 24 * 1024;  // XS: one of the two row-staging buffers
+    constexpr size_t XS = 24 * 1024;  // largest row-staging buffer (one of two)
     const int kst = (s + WS_BK - 1) / WS_BK;
     if (kst * WS_BK > ldq || ldq % WS_BK) {
         irwls_set_error(-12, "Q leading dimension %d does not hold order %d in 32-column blocks", ldq, s);
         return -12;
     }
+    // dynamic shared memory of a CTA: the device's opt-in limit less the
+    // kernel's static shared memory (all instantiations have the same)
+    static size_t limit = 0;
+    if (!limit) {
+        int dev = 0, optin = 0;
+        cudaFuncAttributes fa;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, sgma_tc_score_ws_kernel<2, WS_EG>) != cudaSuccess) {
+            cudaGetLastError();
+            optin = 220 * 1024 + 4096;
+            fa.sharedSizeBytes = 4096;
+        }
+        limit = (size_t)optin - fa.sharedSizeBytes;
+    }
     const size_t fixed = 1024 + (size_t)CAT_LD * X->ld * sizeof(float);
     const size_t stage = TcRing<64, QB_NP, WS_BK>::BYTES;
-    if (fixed + 2 * stage > LIMIT) {
+    if (fixed + 2 * stage > limit) {
         irwls_set_error(-12, "feature width %d too wide for the precision-form SGMA tile", X->width);
         return -12;
     }
-    // row staging when it leaves room for at least four ring stages
-    const size_t xs = fixed + 2 * XS + 4 * stage <= LIMIT ? XS : 0;
-    int ns = 8;
-    while (ns > 2 && fixed + 2 * xs + (size_t)ns * stage > LIMIT) ns = ns == 8 ? 6 : ns - 2;
+    // Row staging: what a typical tile needs (raw rows, or its CSR slice at the
+    // set's mean row length plus a sixteenth; a tile above that reads its rows
+    // from global memory), then as many ring stages as fit, then the rest of
+    // the shared memory to the staging buffers (up to XS each).
+    size_t need;
+    if (X->mode == IRWLS_K_RAW_RBF) need = (size_t)TC_BM * (X->width | 1) * sizeof(float);
+    else need = (size_t)(TC_BM * 8.0 * 1.0625 * (double)X->nnz / std::max(1, X->n_rows)) + 256;
+    need = std::min((need + 127) / 128 * 128, XS);
+    static const int kStages[] = {8, 6, 5, 4, 2};
+    int ns = 2;
+    size_t xs = 0;
+    for (int c : kStages)
+        if (fixed + 2 * need + (size_t)c * stage <= limit) {
+            ns = c;
+            xs = std::min(XS, (limit - fixed - (size_t)c * stage) / 2 / 128 * 128);
+            break;
+        }
+    if (xs == 0)  // no staging: rows from global memory
+        for (int c : kStages)
+            if (fixed + (size_t)c * stage <= limit) {
+                ns = c;
+                break;
+            }
     const size_t smem = fixed + 2 * xs + (size_t)ns * stage;
     const int ntiles = ceil_div(l, TC_BM);
     const int grid = std::max(1, std::min(ntiles, irwls_num_sms() > 0 ? irwls_num_sms() : 148));
@@ -1052,6 +1125,7 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
     switch (ns) {
         case 8: launch(sgma_tc_score_ws_kernel<8, WS_EG>); break;
         case 6: launch(sgma_tc_score_ws_kernel<6, WS_EG>); break;
+        case 5: launch(sgma_tc_score_ws_kernel<5, WS_EG>); break;
         case 4: launch(sgma_tc_score_ws_kernel<4, WS_EG>); break;
         default: launch(sgma_tc_score_ws_kernel<2, WS_EG>); break;
     }
