@@ -276,7 +276,6 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
     } else if (warp == 1) {
         // MMA issue: level u - 6 += sum_{s+t=u} A_s B_t, u = 6 ... 12
         if (lane == 0) {
-            constexpr uint32_t idesc = tc_idesc(GM, GN);
             const uint32_t base = smem_u32(smem);
             for (int k = 0; k < nst && !abort_flag; ++k) {
                 const int blk = k / GDRAIN, kin = k % GDRAIN;
@@ -295,15 +294,24 @@ __global__ void __launch_bounds__(G_THREADS, 1) gram_tc_kernel(const __nv_bfloat
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
                 const uint32_t sa = base + slot * G_STAGE, sbb = sa + A_STAGE;
+                // A piece s against the B pieces t = GS-1-s ... GS-1, which lie
+                // consecutively in shared memory and so form one operand of
+                // 64 (s + 1) rows whose products land on the consecutive
+                // levels 0 ... s: ten MMAs of N <= 256 for the 28 pairs, each A
+                // piece read once per MMA instead of once per pair. Piece GS-1
+                // comes first and covers every level, so it alone starts a
+                // drain block. The sums are exact integers, so the grouping
+                // does not change them.
 #pragma unroll
-                for (int u = GS - 1; u <= 2 * (GS - 1); ++u) {
+                for (int s = GS - 1; s >= 0; --s) {
+                    const uint64_t da = tc_desc_lbo_sbo(sa + s * (GPIECE * 2), 128, 256);
 #pragma unroll
-                    for (int s = u - (GS - 1); s < GS; ++s) {
-                        const int t = u - s;
-                        const uint64_t da = tc_desc_lbo_sbo(sa + s * (GPIECE * 2), 128, 256);
-                        const uint64_t db = tc_desc_lbo_sbo(sbb + t * B_PIECE, 128, 256);
-                        const bool acc = kin > 0 || s > u - (GS - 1);
-                        mma_bf16(tmem + (uint32_t)(u - (GS - 1)) * GN, da, db, idesc, acc ? 1u : 0u);
+                    for (int t0 = GS - 1 - s; t0 < GS; t0 += 4) {
+                        const int np = GS - t0 < 4 ? GS - t0 : 4;  // B pieces of this MMA
+                        const uint64_t db = tc_desc_lbo_sbo(sbb + t0 * B_PIECE, 128, 256);
+                        const bool acc = kin > 0 || s < GS - 1;
+                        mma_bf16(tmem + (uint32_t)(s + t0 - (GS - 1)) * GN, da, db, tc_idesc(GM, GN * np),
+                                 acc ? 1u : 0u);
                     }
                 }
                 tc_commit(&empty[slot]);
