@@ -11,8 +11,9 @@ step (the count the reference hard-codes).
 One step = one complete training (SGMA + IRWLSpar) of that workload. Both
 forms are timed in the same run, on the same resident dataset:
   plain FP64 : the reference's arithmetic, the form the parity tests pin;
-  precision  : SGMA scores in split BF16 on the tensor cores, IRWLSpar's Gram
-               from exact integer digit products on the tensor cores,
+  precision  : SGMA scores on the tensor cores from three bf16 pieces of Q
+               and W (exactly their FP32 values), IRWLSpar's Gram from
+               exact integer digit products on the tensor cores,
                factors/solves/residuals in FP64.
   value : train seconds per step of the precision form when it meets the
           accuracy bars against the plain run of the same job (the budgeted
@@ -116,6 +117,21 @@ def parse():
                     help="forms to time: both (headline = precision form if it meets the accuracy bars), "
                          "or only one of them")
     return ap.parse_args()
+
+
+# One score launch at order s on the budgeted workload: Q's three bf16 pieces
+# of the s columns rounded up to a 32-column block (6 B per entry), the 64
+# residuals of every row (4 B each) and the rows' FP32 CSR (value and index,
+# 8 B per stored entry, plus the row pointer and norm, 8 B per row).
+def score_launch_bytes(rows, s, hd):
+    nnz = len(hd.features) - hd.l
+    return rows * (-(-s // 32) * 32) * 6 + rows * 64 * 4 + nnz * 8 + rows * 8
+
+
+# The score kernel's 501st launch on the 200000-row workload (order 502), one
+# ncu pass: dram bytes read + written, and its duration (ms).
+SCORE_TRAFFIC_502 = 635705088 + 42572544
+SCORE_MS_502 = 0.120
 
 
 def workload(rows):
@@ -516,28 +532,37 @@ def run_ours(args):
             "share_of_step": round(gr_s / runs[1]["s"], 4),
             "slicing_share_of_step": round(runs[1]["prof"]["irwls_gram_slicing"][0] / runs[1]["s"], 4)}
         sc_s = runs[1]["prof"]["sgma_scores"][0]
-        ach = sgma_flops / sc_s / 1e12 if sc_s > 0 else 0.0
-        kernels["sgma_tc_score_ws_kernel (precision form, tcgen05 split BF16)"] = {
-            "bound": "tensor", "achieved": round(ach, 2), "peak": peaks.get("bf16_tflops"),
-            "unit": "TFLOP/s algorithmic (2 l s 64 flops per SGMA step; 3 bf16 products each)",
-            "frac": round(ach / peaks["bf16_tflops"], 4) if peaks.get("bf16_tflops") else None,
-            "peak_source": peak_src + " bf16 burst", "share_of_step": round(sc_s / runs[1]["s"], 4)}
+        nl = max(1, args.budget - 2)  # score launches (orders 2 ... m - 1)
+        sc_bytes = sum(score_launch_bytes(args.rows, s, hd) for s in range(2, args.budget))
+        ach = sc_bytes / sc_s / 1e9 if sc_s > 0 else 0.0
+        kernels["sgma_tc_score_ws_kernel (precision form, tcgen05 on three bf16 pieces)"] = {
+            "bound": "hbm", "achieved": round(ach, 1), "peak": peaks.get("hbm_gbs"),
+            "unit": "GB/s algorithmic (per launch at order s: Q's three bf16 pieces of the s columns rounded up "
+                    "to 32, read once; the 64 residuals of every row written; the rows' FP32 CSR read)",
+            "frac": round(ach / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None,
+            "peak_source": peak_src + " HBM copy", "launches": nl,
+            "avg_launch_us": round(sc_s / nl * 1e6, 2),
+            "algorithmic_tflops": round(sgma_flops / sc_s / 1e12, 2) if sc_s > 0 else None,
+            "share_of_step": round(sc_s / runs[1]["s"], 4)}
     # roofline: the dominant kernel of the headline form
     if head == 1:
-        k = kernels["gram_tc_kernel (precision form, exact integer digit products on tcgen05)"]
+        k = kernels["sgma_tc_score_ws_kernel (precision form, tcgen05 on three bf16 pieces)"]
         # DRAM traffic of one launch from a full-size, one-pass ncu capture (the
-        # last IRWLSpar iteration of this workload, 62357 active rows):
-        # profiles/gram_tc_kernel_200k_m1000_traffic.md. Its algorithmic bytes
-        # are the FP64 operand the SYRK reads once, the active rows of
-        # [sqrt(D_a) KSC, D_a y] (62357 x 1001 x 8 B).
-        alg_bytes = 62357 * 1001 * 8
-        traffic = 894839296 + 3229696
-        roofline = dict(k, kernel="gram_tc_kernel", traffic=traffic,
-                        traffic_launch={"launch": "last of 42 (active rows 62357)", "duration_ms": 2.192,
-                                        "algorithmic_bytes": alg_bytes,
-                                        "traffic_over_algorithmic": round(traffic / alg_bytes, 2),
+        # 501st score launch of this workload, order 502, the mean order of
+        # the run): profiles/sgma_tc_score_ws_kernel_200k_traffic.md
+        lb = score_launch_bytes(args.rows, 502, hd)
+        traffic = SCORE_TRAFFIC_502
+        roofline = dict(k, kernel="sgma_tc_score_ws_kernel", traffic=traffic,
+                        traffic_launch={"launch": "501st of 998 (order 502)", "duration_ms": SCORE_MS_502,
+                                        "algorithmic_bytes": lb,
+                                        "traffic_over_algorithmic": round(traffic / lb, 3) if traffic else None,
                                         "source": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,"
                                                   "gpu__time_duration.sum (one pass)"})
+        g = kernels["gram_tc_kernel (precision form, exact integer digit products on tcgen05)"]
+        # the Gram's last launch (62357 active rows), from the same kind of
+        # capture: profiles/gram_tc_kernel_200k_m1000_traffic.md
+        g["traffic_launch"] = {"launch": "last of 42 (active rows 62357)", "duration_ms": 1.517,
+                               "traffic": 894986752 + 3068672, "algorithmic_bytes": 62357 * 1001 * 8}
     else:
         k = kernels["sgma_gemm_kernel (plain FP64)"]
         roofline = dict(k, kernel="sgma_gemm_kernel", traffic=None,
@@ -573,7 +598,7 @@ def run_ours(args):
     line = {"metric": METRIC, "value": round(value, 3), "unit": "s", "n_gpus": world if world > 1 else args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value * 1000, 1),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if head == 0 else "bf16x3 (SGMA scores) + exact bf16 digit products (IRWLSpar Gram) + f64 (factors, solves)",
+            "dtype": "f64" if head == 0 else "bf16 pieces x6 (SGMA scores) + exact bf16 digit products (IRWLSpar Gram) + f64 (factors, solves)",
             "data": "synthetic (seeded generator)",
             "config": config(args, {"form": form, "par_iterations": runs[head]["iters"],
                                     "active_rows_final": runs[head]["nact"]}),
@@ -1451,7 +1476,7 @@ def run_learned(args):
     line = {"metric": METRIC, "value": round(L["s"], 3), "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(L["s"] * 1000, 1), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16x3 (SGMA scores) + f32 (network) + exact bf16 digit products (IRWLSpar Gram) + f64",
+            "dtype": "bf16 pieces x6 (SGMA scores) + f32 (network) + exact bf16 digit products (IRWLSpar Gram) + f64",
             "data": "synthetic (seeded generator)",
             "config": {"workload": LEARN_DESC % (cfg["n"], budget, cfg["pool"], cfg["trace_sets"], cfg["trace_rows"],
                                                  budget),
