@@ -65,9 +65,41 @@ static_assert((long long)GS * GDRAIN * GBK * (1 << (2 * (GBITS - 1))) < (1LL << 
 // digit piece: 8 x 8 core matrices, 128 bytes apart along k, 256 along r.
 __device__ __forceinline__ int piece_off(int r, int k) { return (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7); }
 
-// Column maxima of |A'| as FP64 bit patterns (non-negative doubles order like
-// their bits). Thread = column, block = 256 columns x GCM rows, eight rows'
-// loads in flight per thread.
+// ceil(log2 |v|) from the bits of a normal double v: its exponent, plus one
+// unless v is a power of two.
+__device__ __forceinline__ int ceil_log2_bits(unsigned long long b) {
+    return (int)((b >> 52) & 0x7ff) - 1023 + ((b & ((1ULL << 52) - 1)) != 0 ? 1 : 0);
+}
+
+constexpr int NO_EXP = -2000;  // zero or subnormal: no scale
+
+// ceil(log2 |v|) of v = RN(a * b), the FP64 product, or NO_EXP when v is zero
+// or subnormal. Away from the products whose rounding can land on a power
+// of two (mantissa products within 2^-18 of 2 or 4) and from the exponent
+// range's ends, it follows from the operands' exponents and an FP32 product
+// of their leading mantissa bits (relative error below 2^-21), with no FP64
+// operation; the rest take the FP64 product.
+__device__ __forceinline__ int prod_ceil_log2(double a, double b) {
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffULL;
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b) & 0x7fffffffffffffffULL;
+    const int Ea = (int)(ua >> 52), Eb = (int)(ub >> 52);
+    if (Ea > 0 && Eb > 0 && Ea + Eb >= 1030 && Ea + Eb <= 3060) {
+        const unsigned long long ma = ua & ((1ULL << 52) - 1), mb = ub & ((1ULL << 52) - 1);
+        const int e = Ea + Eb - 2046;  // exponent of the product of the leading ones
+        if (ma == 0 && mb == 0) return e;  // two powers of two: the exact product
+        const float pr = __uint_as_float(0x3f800000u | (uint32_t)(ma >> 29)) *
+                         __uint_as_float(0x3f800000u | (uint32_t)(mb >> 29));
+        if (pr <= 2.0f - 0x1p-18f) return e + 1;                       // in (1, 2): not a power of two
+        if (pr >= 2.0f + 0x1p-17f && pr <= 4.0f - 0x1p-17f) return e + 2;  // in (2, 4)
+    }
+    const unsigned long long v = (unsigned long long)__double_as_longlong(__dmul_rn(a, b)) & 0x7fffffffffffffffULL;
+    return (v >> 52) == 0 ? NO_EXP : ceil_log2_bits(v);
+}
+
+// Column scales of A': per column the largest ceil(log2 |v|) over the active
+// rows, stored as the bits of 2^that (so that col_exp reads it back; a
+// column with no normal entry stays 0). Thread = column, block = 256
+// columns x GCM rows, eight rows' loads in flight per thread.
 constexpr int GCM = 256;
 __global__ void __launch_bounds__(256) gram_colmax_kernel(const double *__restrict__ KSC, int m,
                                                           const int *__restrict__ act, int nact,
@@ -77,25 +109,36 @@ __global__ void __launch_bounds__(256) gram_colmax_kernel(const double *__restri
     const int c = blockIdx.x * 256 + threadIdx.x;
     if (c > m) return;
     const int p0 = blockIdx.y * GCM, p1 = min(nact, p0 + GCM);
-    // |v| and the maximum on the bit patterns (integer operations): only the
-    // product itself uses the FP64 pipe
-    unsigned long long mx[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) mx[u] = 0ULL;
+    int mx = NO_EXP;
     for (int p = p0; p < p1; p += 8) {
+        double x[8], f[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const int pp = p + u;
+            x[u] = 0.0;
+            f[u] = 1.0;
             if (pp < p1) {
-                const double v = c < m ? __dmul_rn(sd[pp], KSC[(size_t)act[pp] * m + c]) : day[pp];
-                const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
-                mx[u] = a > mx[u] ? a : mx[u];
+                if (c < m) {
+                    x[u] = KSC[(size_t)act[pp] * m + c];
+                    f[u] = sd[pp];
+                } else {
+                    x[u] = day[pp];
+                }
             }
         }
-    }
 #pragma unroll
-    for (int u = 1; u < 8; ++u) mx[0] = mx[u] > mx[0] ? mx[u] : mx[0];
-    if (p1 > p0) atomicMax(cmax + c, mx[0]);
+        for (int u = 0; u < 8; ++u) {
+            int k;
+            if (c < m) {
+                k = prod_ceil_log2(f[u], x[u]);
+            } else {
+                const unsigned long long b = (unsigned long long)__double_as_longlong(x[u]) & 0x7fffffffffffffffULL;
+                k = (b >> 52) == 0 ? NO_EXP : ceil_log2_bits(b);
+            }
+            mx = k > mx ? k : mx;
+        }
+    }
+    if (mx > NO_EXP) atomicMax(cmax + c, (unsigned long long)(mx + 1023) << 52);
 }
 
 // sigma_c = 2^e_c, the smallest power of two >= the column maximum (e = -1100:
