@@ -156,8 +156,12 @@ __global__ void __launch_bounds__(128) cand_rows_kernel(KView X, const int *__re
 // Partial W^T over one chunk of WT columns of Linv: item (eb, tc) covers rows
 // e in [WE eb, WE eb + WE) and t in [WT tc, WT tc + WT) (t <= e only, Linv is
 // zero above); part[(tc * 64 + c) * ldp + e]. Rows of Linv and KN stream
-// through a cp.async double buffer of WK columns.
-constexpr int WE = 16, WT = 64, WK = 16;
+// through a cp.async double buffer of WK columns. Four rows per item, one
+// (row, candidate) sum per thread, so that the grid covers the SMs already
+// at small orders; every sum runs over its chunk in increasing t whatever
+// the item shape (the terms past the row's diagonal are zeros).
+constexpr int WE = 4, WT = 64, WK = 16;
+static_assert(WT % WE == 0, "row blocks must not straddle chunks");
 __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ Linv, int ldi,
                                                      const double *__restrict__ KN, int ldz, int s,
                                                      double *__restrict__ part, int ldp) {
@@ -167,8 +171,9 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
     const int t1 = min(min(t0 + WT, e0 + WE), s);
     __shared__ __align__(16) double Ls[2][WE][WK + 1];
     __shared__ __align__(16) double Ks[2][NCAND][WK + 1];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;  // row e0 + ty, candidates tx + 16 b
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int tid = threadIdx.x, c = tid & (NCAND - 1), ty = tid / NCAND;  // row e0 + ty, candidate c
+    static_assert(WE * NCAND == 256, "one (row, candidate) per thread");
+    double acc = 0.0;
     auto load = [&](int buf, int t) {
         for (int u = tid; u < (WE + NCAND) * WK; u += 256) {
             const int r = u / WK, k = u % WK;
@@ -179,9 +184,9 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
                 cp_async8(&Ls[buf][r][k], ok ? (const void *)(Linv + (size_t)e * ldi + tt) : (const void *)Linv,
                           ok ? 8 : 0);
             } else {
-                const int c = r - WE;
+                const int cr = r - WE;
                 const bool ok = tt < t1;
-                cp_async8(&Ks[buf][c][k], ok ? (const void *)(KN + (size_t)c * ldz + tt) : (const void *)KN,
+                cp_async8(&Ks[buf][cr][k], ok ? (const void *)(KN + (size_t)cr * ldz + tt) : (const void *)KN,
                           ok ? 8 : 0);
             }
         }
@@ -199,18 +204,11 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < WK; ++k) {
-            const double l0 = Ls[buf][ty][k];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[b] = fma(l0, Ks[buf][tx + 16 * b][k], acc[b]);
-        }
+        for (int k = 0; k < WK; ++k) acc = fma(Ls[buf][ty][k], Ks[buf][c][k], acc);
         __syncthreads();
     }
     const int e = e0 + ty;
-    if (e < s) {
-#pragma unroll
-        for (int b = 0; b < 4; ++b) part[((size_t)tc * NCAND + tx + 16 * b) * ldp + e] = acc[b];
-    }
+    if (e < s) part[((size_t)tc * NCAND + c) * ldp + e] = acc;
 }
 
 // Per candidate c: w_e = sum of the chunks of row e in chunk order, W (FP64),
