@@ -225,8 +225,15 @@ __global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict_
         float xf = 0.f;
         if (e < s) {
             const int ntc = (e / WE * WE + WE - 1) / WT + 1;
+            // the chunk partials loaded together, then summed in chunk order
+            double pv[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) pv[u] = u < ntc ? part[((size_t)u * NCAND + c) * ldp + e] : 0.0;
             double w = 0.0;
-            for (int tc = 0; tc < ntc; ++tc) w += part[((size_t)tc * NCAND + c) * ldp + e];
+#pragma unroll
+            for (int u = 0; u < 16; ++u)
+                if (u < ntc) w += pv[u];
+            for (int tc = 16; tc < ntc; ++tc) w += part[((size_t)tc * NCAND + c) * ldp + e];
             W[(size_t)c * ldz + e] = w;
             ss = fma(w, w, ss);
             xf = (float)w;
@@ -257,7 +264,19 @@ __global__ void __launch_bounds__(128) linv_partial_kernel(const double *__restr
     if (t >= s) return;
     const double *l2 = L + (size_t)s * ldL;
     double acc = 0.0;
-    for (int e = max(e0, t); e < e1; ++e) acc = fma(l2[e], Linv[(size_t)e * ldi + t], acc);
+    // sixteen rows' loads in flight ahead of the (serial) sum, e increasing
+    for (int e = max(e0, t); e < e1; e += 16) {
+        double v[16], w[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const bool ok = e + u < e1;
+            v[u] = ok ? Linv[(size_t)(e + u) * ldi + t] : 0.0;
+            w[u] = ok ? l2[e + u] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+            if (e + u < e1) acc = fma(w[u], v[u], acc);
+    }
     part2[(size_t)blockIdx.y * s + t] = acc;
 }
 
@@ -269,8 +288,17 @@ __global__ void __launch_bounds__(256) linv_finish_kernel(const double *__restri
                                                           float *__restrict__ lrow) {
     const double L3 = L[(size_t)s * ldL + s];
     for (int t = threadIdx.x; t < s; t += blockDim.x) {
+        // the chunk partials (at most 16 at order 1024) loaded together, then
+        // summed in chunk order
+        double pv[16];
+        const int c0 = t / LE;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) pv[u] = c0 + u < nch ? part2[(size_t)(c0 + u) * s + t] : 0.0;
         double acc = 0.0;
-        for (int ch = t / LE; ch < nch; ++ch) acc += part2[(size_t)ch * s + t];
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+            if (c0 + u < nch) acc += pv[u];
+        for (int ch = c0 + 16; ch < nch; ++ch) acc += part2[(size_t)ch * s + t];
         Linv[(size_t)s * ldi + t] = -acc / L3;
         lrow[t] = __double2float_rn(L[(size_t)s * ldL + t]);
     }
