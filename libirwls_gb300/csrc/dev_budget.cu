@@ -145,6 +145,8 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 __global__ void __launch_bounds__(128) cand_rows_kernel(KView X, const int *__restrict__ cand,
                                                         const int *__restrict__ cent, int s, double *__restrict__ KN,
                                                         int ldz) {
+    chain_wait();
+    chain_open();
     extern __shared__ double sa[];
     const int c = blockIdx.y, gc = cand[c];
     for (int t = threadIdx.x; t < X.ld; t += blockDim.x) sa[t] = X.X[(size_t)gc * X.ld + t];
@@ -165,6 +167,8 @@ static_assert(WT % WE == 0, "row blocks must not straddle chunks");
 __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ Linv, int ldi,
                                                      const double *__restrict__ KN, int ldz, int s,
                                                      double *__restrict__ part, int ldp) {
+    chain_wait();
+    chain_open();
     const int eb = blockIdx.x, tc = blockIdx.y;
     const int e0 = eb * WE, t0 = tc * WT;
     if (t0 > e0 + WE - 1) return;
@@ -218,6 +222,8 @@ __global__ void __launch_bounds__(256) w_gemm_kernel(const double *__restrict__ 
 __global__ void __launch_bounds__(256) w_finish_kernel(const double *__restrict__ part, int ldp, int s,
                                                        double *__restrict__ W, int ldz, __nv_bfloat16 *Wb, int kpad,
                                                        double *__restrict__ eta) {
+    chain_wait();
+    chain_open();
     __shared__ double red[256];
     const int c = blockIdx.x;
     double ss = 0.0;
@@ -259,6 +265,8 @@ constexpr int LE = 64;
 __global__ void __launch_bounds__(128) linv_partial_kernel(const double *__restrict__ L, int ldL,
                                                            const double *__restrict__ Linv, int ldi, int s,
                                                            double *__restrict__ part2) {
+    chain_wait();
+    chain_open();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int e0 = blockIdx.y * LE, e1 = min(s, e0 + LE);
     if (t >= s) return;
@@ -286,6 +294,8 @@ __global__ void __launch_bounds__(256) linv_finish_kernel(const double *__restri
                                                           double *__restrict__ Linv, int ldi, int s,
                                                           const double *__restrict__ part2, int nch,
                                                           float *__restrict__ lrow) {
+    chain_wait();
+    chain_open();
     const double L3 = L[(size_t)s * ldL + s];
     for (int t = threadIdx.x; t < s; t += blockDim.x) {
         // the chunk partials (at most 16 at order 1024) loaded together, then
@@ -437,6 +447,8 @@ __global__ void __launch_bounds__(NCAND) sgma_select_kernel(const double *__rest
 __global__ void __launch_bounds__(128) sgma_factor_kernel(KView X, int s, const int *__restrict__ cent,
                                                           const int *__restrict__ best, const double *__restrict__ W,
                                                           int ldz, double *__restrict__ L, int ldL, int tree) {
+    chain_wait();
+    chain_open();
     extern __shared__ double sA[];
     __shared__ double red[128];
     const int gc = cent[s];
@@ -798,13 +810,14 @@ extern "C" int irwls_sgma_cand_inv(const irwls_dev_set *X, const int *d_cand, co
         return -12;
     }
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_CAND);
-    cand_rows_kernel<<<dim3(ceil_div(s, 128), NCAND), 128, smem, irwls_stream()>>>(kview(X), d_cand, d_cent, s, d_KN,
-                                                                                 ldz);
+    launch_chained(cand_rows_kernel, dim3(ceil_div(s, 128), NCAND), dim3(128), smem, kview(X), d_cand, d_cent, s, d_KN,
+                   ldz);
     IRWLS_LAUNCH_CHECK("cand_rows");
-    w_gemm_kernel<<<dim3(ceil_div(s, WE), ceil_div(s, WT)), 256, 0, irwls_stream()>>>(d_Linv, ldi, d_KN, ldz, s,
-                                                                                    d_wpart, ldp);
+    launch_chained(w_gemm_kernel, dim3(ceil_div(s, WE), ceil_div(s, WT)), dim3(256), 0, d_Linv, ldi, d_KN, ldz, s,
+                   d_wpart, ldp);
     IRWLS_LAUNCH_CHECK("w_gemm");
-    w_finish_kernel<<<NCAND, 256, 0, irwls_stream()>>>(d_wpart, ldp, s, d_W, ldz, (__nv_bfloat16 *)Wb, kpad, d_eta);
+    launch_chained(w_finish_kernel, dim3(NCAND), dim3(256), 0, d_wpart, ldp, s, d_W, ldz, (__nv_bfloat16 *)Wb, kpad,
+                   d_eta);
     if (irwls_prof_on()) irwls_prof_end(IRWLS_PROF_SGMA_CAND);
     IRWLS_LAUNCH_CHECK("w_finish");
     return 0;
@@ -815,10 +828,11 @@ extern "C" int irwls_sgma_linv_update(const double *d_L, int ldL, double *d_Linv
                                       float *d_lrow) {
     const int nch = ceil_div(s, LE);
     if (s > 0) {
-        linv_partial_kernel<<<dim3(ceil_div(s, 128), nch), 128, 0, irwls_stream()>>>(d_L, ldL, d_Linv, ldi, s, d_lpart);
+        launch_chained(linv_partial_kernel, dim3(ceil_div(s, 128), nch), dim3(128), 0, d_L, ldL, d_Linv, ldi, s,
+                       d_lpart);
         IRWLS_LAUNCH_CHECK("linv_partial");
     }
-    linv_finish_kernel<<<1, 256, 0, irwls_stream()>>>(d_L, ldL, d_Linv, ldi, s, d_lpart, nch, d_lrow);
+    launch_chained(linv_finish_kernel, dim3(1), dim3(256), 0, d_L, ldL, d_Linv, ldi, s, d_lpart, nch, d_lrow);
     IRWLS_LAUNCH_CHECK("linv_finish");
     return 0;
 }
@@ -828,7 +842,7 @@ extern "C" int irwls_sgma_factor(const irwls_dev_set *X, int s, const int *d_cen
                                  int ldz, double *d_L, int ldL) {
     const size_t smem = (size_t)X->ld * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(sgma_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    sgma_factor_kernel<<<1, 128, smem, irwls_stream()>>>(kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL, 1);
+    launch_chained(sgma_factor_kernel, dim3(1), dim3(128), smem, kview(X), s, d_cent, d_best, d_W, ldz, d_L, ldL, 1);
     IRWLS_LAUNCH_CHECK("sgma_factor");
     return 0;
 }

@@ -18,6 +18,30 @@ int irwls_num_sms();
         if (_rc) return _rc;                             \
     } while (0)
 
+// Chained launches (programmatic dependent launch): a kernel launched with
+// launch_chained may be scheduled while the kernel before it on the stream
+// is finishing, and starts with chain_wait(), which returns once that kernel
+// has completed and its writes are visible; nothing before chain_wait() may
+// touch global memory. chain_open() lets the next chained kernel be scheduled.
+// Outside a chained launch both are no-ops.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void chain_open() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_chained(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = irwls_stream();
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // Device-side status words (dev_context.cu), a device array of 8 ints:
 // [0] first failed Cholesky pivot of the last factorization (1-based, 0 if none).
 int *irwls_dev_flags();

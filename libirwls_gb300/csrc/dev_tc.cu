@@ -525,6 +525,8 @@ __global__ void __launch_bounds__(1024) sgma_select_f32_kernel(const float *__re
                                                               const double *__restrict__ eta,
                                                               const int *__restrict__ cand, int s, int *cent,
                                                               int *best, double *bestval, float *scores) {
+    chain_wait();
+    chain_open();
     __shared__ double grp[16][64];
     __shared__ double sc[64];
     const int c = threadIdx.x & 63, g = threadIdx.x >> 6;
@@ -769,6 +771,8 @@ __global__ void __launch_bounds__(128 + 128 * EG, 1) sgma_tc_score_ws_kernel(
     KViewF X, int l, const int *__restrict__ cand, const __nv_bfloat16 *__restrict__ Qb, int kbn,
     const __nv_bfloat16 *__restrict__ Wb, int kst, float *__restrict__ part, float *__restrict__ resid, int xs_bytes,
     int *flags) {
+    chain_wait();
+    chain_open();
     using S = TcRing<64, QB_NP, WS_BK>;
     static_assert(S::A_BYTES == 2 * QB_PIECE && S::B_BYTES == 2 * WB_PIECE, "blocked pieces are stage images");
     extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -969,6 +973,8 @@ __device__ __forceinline__ void put_q(int row, int s, float q, __nv_bfloat16 *Qb
 __global__ void q_column_resid_kernel(int l, const float *__restrict__ resid, const int *__restrict__ best, int s,
                                       const float *__restrict__ lrow, __nv_bfloat16 *Qb, int ldq,
                                       float *__restrict__ qn) {
+    chain_wait();
+    chain_open();
     const int c = best[0];
     const float inv_l3 = lrow[s];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < l; i += gridDim.x * blockDim.x)
@@ -1118,8 +1124,8 @@ extern "C" int irwls_sgma_tc_score(const irwls_dev_set *X, const void *F, int l,
     const __nv_bfloat16 *qb = (const __nv_bfloat16 *)Qb, *wb = (const __nv_bfloat16 *)Wb;
     auto launch = [&](auto kern) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kern<<<grid, 128 + 128 * WS_EG, smem, irwls_stream()>>>(kv, l, d_cand, qb, ldq / 32, wb, kst, d_part,
-                                                                d_resid, (int)xs, irwls_dev_flags());
+        launch_chained(kern, dim3(grid), dim3(128 + 128 * WS_EG), smem, kv, l, d_cand, qb, ldq / 32, wb, kst, d_part,
+                       d_resid, (int)xs, irwls_dev_flags());
     };
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_SGMA_GEMM);
     switch (ns) {
@@ -1138,8 +1144,8 @@ extern "C" int irwls_sgma_tc_partials(int l) { return ceil_div(l, TC_BM); }
 
 extern "C" int irwls_sgma_tc_select(const float *d_part, int nblk, const double *d_eta, const int *d_cand, int s,
                                     int *d_cent, int *d_best, double *d_bestval, float *d_scores) {
-    sgma_select_f32_kernel<<<1, 1024, 0, irwls_stream()>>>(d_part, nblk, d_eta, d_cand, s, d_cent, d_best, d_bestval,
-                                                           d_scores);
+    launch_chained(sgma_select_f32_kernel, dim3(1), dim3(1024), 0, d_part, nblk, d_eta, d_cand, s, d_cent, d_best,
+                   d_bestval, d_scores);
     IRWLS_LAUNCH_CHECK("sgma_select_f32");
     return 0;
 }
@@ -1170,8 +1176,8 @@ extern "C" int irwls_q_column_resid(int l, const float *d_resid, const int *d_be
         return -12;
     }
     const int blocks = std::max(1, std::min(ceil_div(l, 256), 4 * (irwls_num_sms() > 0 ? irwls_num_sms() : 148)));
-    q_column_resid_kernel<<<blocks, 256, 0, irwls_stream()>>>(l, d_resid, d_best, s, lrow, (__nv_bfloat16 *)Qb, ldq,
-                                                              d_qn);
+    launch_chained(q_column_resid_kernel, dim3(blocks), dim3(256), 0, l, d_resid, d_best, s, lrow, (__nv_bfloat16 *)Qb,
+                   ldq, d_qn);
     IRWLS_LAUNCH_CHECK("q_column_resid");
     return 0;
 }
