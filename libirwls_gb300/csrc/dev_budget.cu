@@ -620,19 +620,41 @@ __global__ void gram_reduce_kernel(const double *__restrict__ part, int P, int m
     }
 }
 
-// e = y - KSC beta, then Da (src/budgeted-train.c:431-457). One warp per row.
+// e = y - KSC beta, then Da (src/budgeted-train.c:431-457). A warp per row,
+// two rows in flight (their loads interleaved); per row each lane's terms in
+// increasing j, then a butterfly over the lanes.
 __global__ void residual_kernel(const double *__restrict__ KSC, int l, int m, const double *__restrict__ beta,
                                 const double *__restrict__ y, double C, double M, double *__restrict__ e,
                                 double *__restrict__ Da) {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int i = warp; i < l; i += nw) {
-        const double *row = KSC + (size_t)i * m;
-        double acc = 0.0;
-        for (int j = lane; j < m; j += 32) acc = fma(row[j], beta[j], acc);
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
+    for (int i0 = warp; i0 < l; i0 += 2 * nw) {
+        const int i1 = i0 + nw;
+        const bool two = i1 < l;
+        const double *r0 = KSC + (size_t)i0 * m, *r1 = KSC + (size_t)(two ? i1 : i0) * m;
+        double a0 = 0.0, a1 = 0.0;
+        int j = lane;
+        for (; j + 32 < m; j += 64) {
+            const double b0 = beta[j], b1 = beta[j + 32];
+            const double x0 = r0[j], x1 = r1[j], y0 = r0[j + 32], y1 = r1[j + 32];
+            a0 = fma(x0, b0, a0);
+            a1 = fma(x1, b0, a1);
+            a0 = fma(y0, b1, a0);
+            a1 = fma(y1, b1, a1);
+        }
+        if (j < m) {
+            const double b0 = beta[j];
+            a0 = fma(r0[j], b0, a0);
+            a1 = fma(r1[j], b0, a1);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        }
+        if (lane < 2 && (lane == 0 || two)) {
+            const int i = lane == 0 ? i0 : i1;
+            const double acc = lane == 0 ? a0 : a1;
             const double yi = y[i];
             const double ei = yi - acc;
             e[i] = ei;
