@@ -81,11 +81,11 @@ int irwls_gpu_available(void);
 
 /* Arithmetic of the training paths:
  * IRWLS_PRECISION_FP64 (default): FP64 throughout, reference parity;
- * IRWLS_PRECISION_MIXED: the precision form -- SGMA candidate scores as
- * split-BF16 tensor-core products (FP32 accumulation) on the Nystrom
- * features of the current centroids, with the K_mm factorization and its
- * solves in FP64 (it can pick a different centroid where two candidates
- * score within about 1e-5 of each other); the IRWLSpar Gram from exact
+ * IRWLS_PRECISION_MIXED: the precision form -- SGMA candidate scores from
+ * tensor-core products of three bf16 pieces per value (FP32 accuracy) on
+ * the Nystrom features of the current centroids, with the K_mm
+ * factorization and its solves in FP64 (it can pick a different centroid
+ * where two candidates score within about 1e-7 of each other); the IRWLSpar Gram from exact
  * integer digit products on the tensor cores (about 2^-45 of the column
  * scales per row), its Cholesky, solves, residual and stop test in FP64;
  * in full IRWLS, the error updates of rows away from the margin on the

@@ -461,7 +461,7 @@ extern "C" int irwls_tc_status(void) {
 // SGMA works on Q = K_nm L^-T (row i = the Nystrom features of sample i, all
 // of norm <= 1) instead of K_nm: for a candidate c with w = L^-1 k_C(c),
 // K_nm z = Q w, eta = 1 - |w|^2, and the residual is r = Q w - k(c, .). Q and
-// w are bounded, which is what makes the split-BF16 product accurate here
+// w are bounded, which is what makes a product of bf16 pieces accurate here
 // (the reference's K_nm z form multiplies K_nm by z = K_CC^-1 k_C, whose
 // entries are large and cancel). Q is kept as three bf16 pieces per value
 // (exactly its FP32 value), and the tensor cores take the six piece products

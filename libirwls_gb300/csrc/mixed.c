@@ -4,9 +4,11 @@
  *   SGMA: candidate kernel rows, the factor L of K_CC + jitter and its
  *         inverse (kept explicitly, as the reference keeps invKC) in FP64;
  *         the candidate solves W = K_CN L^-T as one FP64 GEMM; scores from
- *         Q w on the tensor cores in split BF16 (Q = K_nm L^-T, kept in FP32
- *         and as bf16 hi/lo), candidate kernel rows of the score epilogue in
- *         FP32.
+ *         Q w on the tensor cores (Q = K_nm L^-T and W held as three bf16
+ *         pieces each, exactly their FP32 values; six piece products, so
+ *         Q w has FP32 accuracy), candidate kernel rows of the score
+ *         epilogue in FP32; each new column of Q taken from the score
+ *         step's residuals of the winning candidate.
  *   IRWLSpar (budgeted_train.c, irwls_par_dev) forms its Gram on the tensor
  *   cores from exact integer digits of its operand (dev_gram_tc.cu); its
  *   factor, solves, residuals and convergence test stay FP64. Its system

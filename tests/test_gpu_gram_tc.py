@@ -15,7 +15,9 @@ A' = [sd * KSC[act, :], day], from exact base-128 integer digits.
   (tests/gram_digits.py) -- RBF-like columns with weights over six decades;
   and columns that hit the edge cases: ties of the fixed-point rounding, a
   power-of-two and a just-above maximum, a zero column, subnormal entries,
-  tiny columns, and a constant column whose integer sum passes 2^63.
+  tiny columns, a constant column whose integer sum passes 2^63, and column
+  maxima that are products rounding onto or next to a power of two (the
+  column scales' exact fallback).
 - No active rows: K1 = KC.
 """
 import ctypes as C
@@ -171,8 +173,28 @@ def _edge_case(rng):
     return KSC, act, sd, day, KC
 
 
+def _scale_boundary_case(rng):
+    """Columns whose largest entry sd_i * KSC_ic is an FP64 product that
+    rounds onto, just below or just above a power of two, so that the column
+    scale comes from the kernel's exact fallback next to those boundaries."""
+    l, m, nact = 2000, 65, 1800
+    act = np.sort(rng.choice(l, nact, replace=False))
+    sd = rng.uniform(1.0, 2.0, nact)
+    KSC = rng.uniform(-1.0, 1.0, (l, m)) * 0.2
+    for c in range(1, m - 1):
+        p = int(rng.integers(nact))
+        target = 2.0 ** int(rng.integers(-4, 4))
+        k = target / sd[p]
+        k += int(rng.integers(-3, 4)) * np.spacing(k)
+        KSC[:, c] *= target
+        KSC[act[p], c] = k if c % 2 else -k
+    day = rng.standard_normal(nact)
+    KC = rng.standard_normal((m, m))
+    return KSC, act, sd, day, KC
+
+
 @pytest.mark.parametrize("P", [1, 4])
-@pytest.mark.parametrize("make", [_rbf_case, _edge_case])
+@pytest.mark.parametrize("make", [_rbf_case, _edge_case, _scale_boundary_case])
 def test_gram_tc_bit_exact_against_host_model(make, P):
     KSC, act, sd, day, KC = make(np.random.default_rng(11))
     G = _gram(KSC, act, sd, day, KC, P)

@@ -1,11 +1,12 @@
 """Precision form (irwls_set_precision(IRWLS_PRECISION_MIXED)) of budgeted and
 full IRWLS.
 
-SGMA: the candidate scores come from split-BF16 tensor-core products on the
-Nystrom features Q = K_nm L^-T, with the factor and its solves in FP64. Its
-scores differ from the FP64 form by about 1e-5 relative, so it may pick a
-different centroid where two candidates score within that margin; on the
-seeded reference cases below every step's argmax agrees with the reference.
+SGMA: the candidate scores come from tensor-core products of three bf16
+pieces per value (FP32 accuracy) on the Nystrom features Q = K_nm L^-T, with
+the factor and its solves in FP64. Its scores differ from the FP64 form by
+about 1e-7 relative, so it may pick a different centroid where two
+candidates score within that margin; on the seeded reference cases below
+every step's argmax agrees with the reference.
 
 IRWLSpar: the Gram K1 = KC + A'^T A' is formed on the tensor cores from
 exact integer digits of A' (48-bit fixed point per column, about 2^-45 of

@@ -154,7 +154,7 @@ BUDGET_CFG2_TOL = 1e-8
 
 def test_budget_cfg2_full_precision_meets_its_contract():
     """The precision form on the same 200000-row workload, against the
-    reference's run: its 1000 centroids (the split-BF16 scores rank the
+    reference's run: its 1000 centroids (the tensor-core scores rank the
     candidates as the FP64 ones do here), the budgeted primal objective
     1/2 w^T (K_mm + 1e-5 I) w + C sum_i max(0, 1 - y_i f_i) within 1e-4
     relative (the model has no dual; the IRWLSpar system's condition number
