@@ -98,47 +98,54 @@ __device__ __forceinline__ int prod_ceil_log2(double a, double b) {
 
 // Column scales of A': per column the largest ceil(log2 |v|) over the active
 // rows, stored as the bits of 2^that (so that col_exp reads it back; a
-// column with no normal entry stays 0). Thread = column, block = 256
-// columns x GCM rows, eight rows' loads in flight per thread.
-constexpr int GCM = 256;
+// column with no normal entry stays 0). A CTA takes GCM rows and a block of
+// 1024 columns (all of a row's columns when m < 1024: one contiguous stream
+// per row), thread t the columns t, t + 256, ... of the block; two rows'
+// loads in flight. The maximum does not depend on the order the entries are
+// visited in.
+constexpr int GCM = 64;
 __global__ void __launch_bounds__(256) gram_colmax_kernel(const double *__restrict__ KSC, int m,
                                                           const int *__restrict__ act, int nact,
                                                           const double *__restrict__ sd,
                                                           const double *__restrict__ day,
                                                           unsigned long long *__restrict__ cmax) {
-    const int c = blockIdx.x * 256 + threadIdx.x;
-    if (c > m) return;
-    const int p0 = blockIdx.y * GCM, p1 = min(nact, p0 + GCM);
-    int mx = NO_EXP;
-    for (int p = p0; p < p1; p += 8) {
-        double x[8], f[8];
+    constexpr int CPT = 4;  // columns per thread: 1024 per block
+    const int p0 = blockIdx.x * GCM, p1 = min(nact, p0 + GCM);
+    const int cb = 1024 * blockIdx.y;
+    int mx[CPT];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int pp = p + u;
-            x[u] = 0.0;
-            f[u] = 1.0;
-            if (pp < p1) {
-                if (c < m) {
-                    x[u] = KSC[(size_t)act[pp] * m + c];
-                    f[u] = sd[pp];
-                } else {
-                    x[u] = day[pp];
-                }
-            }
-        }
+    for (int u = 0; u < CPT; ++u) mx[u] = NO_EXP;
+    auto visit = [&](int p, const double *x) {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            int k;
+        for (int u = 0; u < CPT; ++u) {
+            const int c = cb + threadIdx.x + 256 * u;
+            int k = NO_EXP;
             if (c < m) {
-                k = prod_ceil_log2(f[u], x[u]);
-            } else {
-                const unsigned long long b = (unsigned long long)__double_as_longlong(x[u]) & 0x7fffffffffffffffULL;
+                k = prod_ceil_log2(sd[p], x[u]);
+            } else if (c == m) {
+                const unsigned long long b = (unsigned long long)__double_as_longlong(day[p]) & 0x7fffffffffffffffULL;
                 k = (b >> 52) == 0 ? NO_EXP : ceil_log2_bits(b);
             }
-            mx = k > mx ? k : mx;
+            mx[u] = k > mx[u] ? k : mx[u];
         }
+    };
+    for (int p = p0; p < p1; p += 2) {
+        double x0[CPT], x1[CPT];
+        const double *r0 = KSC + (size_t)act[p] * m, *r1 = KSC + (size_t)act[p + 1 < p1 ? p + 1 : p] * m;
+#pragma unroll
+        for (int u = 0; u < CPT; ++u) {
+            const int c = cb + threadIdx.x + 256 * u;
+            x0[u] = c < m ? r0[c] : 0.0;
+            x1[u] = c < m ? r1[c] : 0.0;
+        }
+        visit(p, x0);
+        if (p + 1 < p1) visit(p + 1, x1);
     }
-    if (mx > NO_EXP) atomicMax(cmax + c, (unsigned long long)(mx + 1023) << 52);
+#pragma unroll
+    for (int u = 0; u < CPT; ++u) {
+        const int c = cb + threadIdx.x + 256 * u;
+        if (c <= m && mx[u] > NO_EXP) atomicMax(cmax + c, (unsigned long long)(mx[u] + 1023) << 52);
+    }
 }
 
 // sigma_c = 2^e_c, the smallest power of two >= the column maximum (e = -1100:
@@ -484,7 +491,7 @@ extern "C" int irwls_par_gram_tc(const double *d_KSC, int m, const int *d_act, i
     if (irwls_prof_on()) irwls_prof_begin(IRWLS_PROF_GRAM_SLICE);
     if (irwls_dev_memset(cmax, 0, (size_t)(m + 1) * sizeof(unsigned long long))) return -1;
     if (nact > 0) {
-        gram_colmax_kernel<<<dim3(ceil_div(m + 1, 256), ceil_div(nact, GCM)), 256, 0, irwls_stream()>>>(
+        gram_colmax_kernel<<<dim3(ceil_div(nact, GCM), ceil_div(m + 1, 1024)), 256, 0, irwls_stream()>>>(
             d_KSC, m, d_act, nact, d_sd, d_day, cmax);
         IRWLS_LAUNCH_CHECK("gram_colmax");
     }
