@@ -80,3 +80,58 @@ def test_model_accuracy_and_chunking():
     assert np.all(np.abs(G1 - ref)[low] <= bound[low])
     # the chunks differ from one sum only by the roundings of the partials
     assert np.all(np.abs(G4 - G1)[low] <= 4 * 2.0 ** -52 * np.abs(ref)[low] + bound[low] * 2.0 ** -10)
+
+
+def _fast_ceil_log2_product(a, b):
+    """The column-scale rule of gram_colmax_kernel (prod_ceil_log2 in
+    libirwls_gb300/csrc/dev_gram_tc.cu), restated: ceil(log2 |RN(a b)|) from
+    the operands' exponents and an FP32 product of their leading 23 mantissa
+    bits, or None where the kernel takes the FP64 product instead."""
+    import struct
+    ua = struct.unpack("<Q", struct.pack("<d", abs(a)))[0]
+    ub = struct.unpack("<Q", struct.pack("<d", abs(b)))[0]
+    Ea, Eb = ua >> 52, ub >> 52
+    if not (Ea > 0 and Eb > 0 and 1030 <= Ea + Eb <= 3060):
+        return None
+    m52 = (1 << 52) - 1
+    ma, mb = ua & m52, ub & m52
+    e = Ea + Eb - 2046
+    if ma == 0 and mb == 0:
+        return e
+    fa = np.frombuffer(struct.pack("<I", 0x3F800000 | (ma >> 29)), np.float32)[0]
+    fb = np.frombuffer(struct.pack("<I", 0x3F800000 | (mb >> 29)), np.float32)[0]
+    pr = np.float32(fa * fb)
+    if pr <= np.float32(2.0) - np.float32(2.0 ** -18):
+        return e + 1
+    if np.float32(2.0) + np.float32(2.0 ** -17) <= pr <= np.float32(4.0) - np.float32(2.0 ** -17):
+        return e + 2
+    return None
+
+
+def test_column_scale_rule_matches_exact_products():
+    """Where the rule decides, it gives ceil(log2) of the FP64 product:
+    random pairs over wide exponent ranges, and pairs built next to the
+    mantissa products 2 and 4 (where rounding can land on a power of two and
+    the kernel falls back to the FP64 product)."""
+    rng = np.random.default_rng(17)
+    pairs = [(rng.uniform(1, 2) * 2.0 ** rng.integers(-40, 40), rng.uniform(1, 2) * 2.0 ** rng.integers(-40, 40))
+             for _ in range(20000)]
+    for _ in range(4000):
+        a = rng.uniform(1, 2)
+        for t in (2.0, 4.0):
+            for k in (-3, -1, 0, 1, 3):
+                b = t / a
+                pairs.append((a * 2.0 ** int(rng.integers(-8, 8)), b + k * np.spacing(b)))
+    decided = 0
+    for a, b in pairs:
+        got = _fast_ceil_log2_product(a, b)
+        if got is None:
+            continue
+        decided += 1
+        v = abs(a * b)
+        m, ex = np.frexp(v)  # v = m 2^ex, m in [0.5, 1)
+        want = int(ex) - (1 if m == 0.5 else 0)
+        assert got == want, (a, b, got, want)
+    # the random pairs are decided by the rule; the built ones sit within
+    # 2^-50 of the boundaries and go to the FP64 product
+    assert decided >= 19900
